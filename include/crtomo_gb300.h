@@ -1,0 +1,187 @@
+/*
+ * crtomo_gb300 -- C ABI of the GB300 (sm_103a) implementation of the
+ * CRMod/CRTomo forward + sensitivity hot path.
+ *
+ * Every entry point replaces one reference routine (or one block of a
+ * reference driver); the comment above each names it (paths relative to the
+ * reference project root).  A Fortran host binds these with ISO_C_BINDING;
+ * the binding is shown in INTEGRATION.md.
+ *
+ * Conventions
+ *  - All array arguments are HOST pointers unless the name ends in _device.
+ *  - Integer arrays keep the reference's 1-based numbering (node numbers in
+ *    nrel/enr, element numbers in rnr, electrodes in strnr/vnr encoded as
+ *    A*10000+B) and its Fortran column-major layout.
+ *  - Complex values are interleaved (re, im) double pairs, i.e. Fortran
+ *    COMPLEX(KIND(0D0)).
+ *  - Every function returns 0 on success or the reference's error number
+ *    (src/error.txt: 19 band width exceeded, 26 bad element geometry,
+ *    27 zero diagonal, 28 zero pivot, 35 degenerate boundary element,
+ *    73 duplicate electrodes, 82 zero voltage, 93 zero geometry factor,
+ *    94/97 allocation, 101 mixed and Dirichlet boundaries together).
+ *    Codes >= 1000 are this library's own (1000 CUDA error, 1001 bad
+ *    argument, 1002 unsupported option).  crgpu_last_error() gives the text
+ *    (the reference's fetxt).
+ *  - One context owns one CUDA stream; calls on one context must not overlap.
+ */
+#ifndef CRTOMO_GB300_H
+#define CRTOMO_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct crgpu_ctx crgpu_ctx;
+
+/* FE grid as read by src/relem.f90 (module elemmod, src/elemmod.f90). */
+typedef struct {
+    int32_t sanz, typanz, mb;
+    const int32_t *typ, *nelanz, *selanz; /* typanz each; boundary types (>10) last */
+    const int32_t *snr;                   /* sanz: node -> coordinate index */
+    const double *sx, *sy;                /* sanz */
+    const int32_t *nrel;                  /* nrel(ld_nrel, maxnk), column-major */
+    int32_t ld_nrel;                      /* elanz + relanz */
+    const int32_t *rnr;                   /* relanz: boundary element -> element */
+} crgpu_grid;
+
+/* Electrodes, measurements and wavenumbers (src/electrmod.f90,
+ * src/datmod.f90, src/wavenmod.f90) and the crmod.cfg switches. */
+typedef struct {
+    int32_t eanz;
+    const int32_t *enr;      /* eanz: electrode node numbers */
+    int32_t nanz;
+    const int32_t *strnr;    /* nanz: current electrodes  A*10000+B */
+    const int32_t *vnr;      /* nanz: voltage electrodes  M*10000+N */
+    const double *strom;     /* nanz or NULL (unit current) */
+    int32_t kwnanz;
+    const double *kwn;       /* kwnanz wavenumbers (src/rwaven.f90) */
+    const double *kwnwi;     /* kwnanz quadrature weights */
+    int32_t swrtr;           /* 0: 2D (kwnanz = 1, kwn = 0), 1: 2.5D */
+    int32_t lsr;             /* singularity removal, mswitch bit 2 */
+    int32_t lsink, nsink;    /* fictitious sink node */
+    int32_t lsytop;          /* image plane at mean Neumann-boundary y */
+} crgpu_survey;
+
+/* Precision of the factorisation. */
+enum {
+    CRGPU_PLAIN = 0, /* complex128 throughout (reference arithmetic) */
+    CRGPU_MIXED = 1  /* complex64 factor + FP64 iterative refinement */
+};
+
+/* ------------------------------------------------------------------ */
+/* set-up                                                               */
+/* ------------------------------------------------------------------ */
+
+/* Uploads grid and survey and computes the element matrices, the mixed-
+ * boundary factors and the band pattern on the device.
+ * Replaces src/precal.f90:13-222 (with src/elem1.f90, src/elem3.f90,
+ * src/elem5.f90, src/elem8.f90, src/beta.f90, src/bessk0.f90,
+ * src/bessk1.f90, src/bsytop.f90) and the allocations of src/fem.f90:314-327. */
+int crgpu_create(const crgpu_grid *grid, const crgpu_survey *survey, int32_t precision,
+                 crgpu_ctx **ctx);
+
+/* Frees the context and its device memory. */
+int crgpu_destroy(crgpu_ctx *ctx);
+
+/* Message of the last error on this context (the reference's fetxt). */
+const char *crgpu_last_error(const crgpu_ctx *ctx);
+
+/* Iterative refinement of the mixed mode: at most maxit corrections, stop a
+ * system when max|dx| <= tol * max|x|.  Defaults: 6, 1e-12. */
+int crgpu_set_refinement(crgpu_ctx *ctx, int32_t maxit, double tol);
+
+/* Upper bound of device memory for the per-system band factors; systems are
+ * processed in batches that fit.  Default: 60% of free device memory. */
+int crgpu_set_memory_budget(crgpu_ctx *ctx, int64_t bytes);
+
+/* ------------------------------------------------------------------ */
+/* forward modelling                                                    */
+/* ------------------------------------------------------------------ */
+
+/* Forward block of src/fem.f90:327-400 (== src/inv.f90:426-491): for every
+ * wavenumber k and current electrode l: src/potana.f90 (if lsr),
+ * src/kompab.f90 / src/kompb.f90, src/randb.f90, src/scalab.f90,
+ * src/chol.f90, src/vre.f90 and the unscaling into kpot; then
+ * src/rtrafo.f90, then src/bvolt.f90 (volt_mode 0: sigmaa = kfak*V, kfak
+ * may be NULL) or src/bvolti.f90 (volt_mode 1: sigmaa = -log V).
+ *   sigma  : elanz complex (src/sigmamod.f90)
+ *   kpot   : kpot(sanz, eanz, kwnanz) complex, or NULL
+ *   hpot   : hpot(sanz, eanz) complex, or NULL
+ *   volt, sigmaa : nanz complex (either may be NULL) */
+int crgpu_forward(crgpu_ctx *ctx, const double *sigma, double *kpot, double *hpot,
+                  int32_t volt_mode, const double *kfak, double *volt, double *sigmaa);
+
+/* The same with every array in device memory (inputs resident in HBM). */
+int crgpu_forward_device(crgpu_ctx *ctx, const void *sigma_device, int32_t volt_mode,
+                         const void *kfak_device, void *volt_device, void *sigmaa_device);
+
+/* Sensitivities of the last forward: src/bsens.f90:23-197 (mode 0, CRMod:
+ * sens -= strom/pi * sum_k w_k ...) or src/bsensi.f90:23-194 (mode 1,
+ * CRTomo: sens += sum_k w_k/pi ... * sigma_e / V_i).
+ *   sens : sens(nanz, elanz) complex, column-major (src/alloci.f90) */
+int crgpu_sens(crgpu_ctx *ctx, int32_t mode, double *sens);
+int crgpu_sens_device(crgpu_ctx *ctx, int32_t mode, void *sens_device);
+
+/* Device buffers of the last forward (valid until the next call):
+ * kpot(sanz, eanz, kwnanz), hpot(sanz, eanz), fak per system. */
+int crgpu_device_buffers(crgpu_ctx *ctx, void **kpot_device, void **hpot_device);
+
+/* Band factor of one system (k, l) (1-based) as src/chol.f90 leaves it in
+ * a((mb+1)*sanz) -- complex128 even in the mixed mode (converted) -- and the
+ * scaling vector fak(sanz) of src/scalab.f90.  Recomputes that system. */
+int crgpu_factor_system(crgpu_ctx *ctx, const double *sigma, int32_t k, int32_t l,
+                        double *a, double *fak);
+
+/* ------------------------------------------------------------------ */
+/* inversion update                                                     */
+/* ------------------------------------------------------------------ */
+
+/* src/update.f90:27-353 with the complex PCG of src/cg_mod.f90:426-726
+ * (cjggra, bap, bp / bptri, bb) on the sensitivities of the last
+ * crgpu_sens(ctx, 1, ...) call.
+ *   ltri  : 0 structured smoothness (smatm(manz,3), nx) or 1/2 triangular
+ *           (smatm(manz,maxnk+1) over nachbar(manz,maxnk+1))
+ *   par   : in/out model (log sigma), manz complex
+ *   dpar  : out update, manz complex;  cgfac : out, manz
+ *   cgres : out, ncgmax+2 floats (cgres(1) = number of CG steps)
+ * Returns the error code; *ncg receives the number of CG steps. */
+int crgpu_update(crgpu_ctx *ctx, const double *wmatd, const int32_t *wdfak, const double *dat,
+                 const double *sigmaa, int32_t ltri, const double *smatm, int32_t nx,
+                 const int32_t *nachbar, double lam, double eps, int32_t ncgmax, double step,
+                 double *par, double *dpar, double *cgfac, float *cgres, int32_t *ncg);
+
+/* ------------------------------------------------------------------ */
+/* host-side set-up routines                                            */
+/* ------------------------------------------------------------------ */
+
+/* src/rwaven.f90:22-171 with the Gauss-Legendre / Gauss-Laguerre rules of
+ * src/gauleg.f90 and src/gaulag.f90.  kwn, kwnwi: room for 30. */
+int crgpu_rwaven(const crgpu_grid *grid, int32_t eanz, const int32_t *enr, int32_t nanz,
+                 const int32_t *strnr, const int32_t *vnr, double *kwn, double *kwnwi,
+                 int32_t *kwnanz);
+
+/* Cuthill-McKee renumbering of cutmckee/cutmck.f:125-337: renumbers nrel,
+ * snr and enr in place and returns the band width in *mb. */
+int crgpu_cutmck(int32_t sanz, int32_t typanz, const int32_t *typ, const int32_t *nelanz,
+                 const int32_t *selanz, int32_t *nrel, int32_t ld_nrel, int32_t *snr,
+                 int32_t eanz, int32_t *enr, int32_t *mb);
+
+/* Geometric factors of src/bkfak.f90:7-149 (kfak(nanz)). */
+int crgpu_bkfak(const crgpu_grid *grid, const crgpu_survey *survey, double *kfak);
+
+/* Counters of the last call: kernels launched, and device time (ms) of the
+ * forward, factorisation, sensitivity and update phases. */
+typedef struct {
+    int64_t kernel_launches;
+    double ms_forward, ms_factor, ms_solve, ms_sens, ms_update;
+    int32_t refine_iterations;
+    int32_t nsystems, nbatches;
+} crgpu_stats;
+int crgpu_get_stats(const crgpu_ctx *ctx, crgpu_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,61 @@
+"""Copy the reference's own test fixtures that pin the forward path into
+tests/golden/.
+
+Run in a container where the reference checkout is present:
+
+    python tests/golden/make_golden.py /path/to/reference
+
+Forward cases (<case>/): the CRMod inputs (elem.dat, elec.dat, rho.dat,
+crmod.cfg) and the CRMod output volt.dat of a reference tomodir.  The
+measurement configurations are the (strnr, vnr) columns of volt.dat.
+
+CutMcK cases (cutmck_<case>/): the grid before (elem.dat.orig, elec.dat.orig)
+and after (elem.dat, elec.dat) the reference's Cuthill-McKee renumbering.
+
+The files are data fixtures of the reference's tests/ and examples/ trees,
+copied byte for byte.
+"""
+import os
+import shutil
+import sys
+
+FORWARD = {
+    # name: (tomodir, pin note)
+    "minimal": "tests/minimal/Reference",
+    "testmodinv": "tests/TestModInv/Reference",
+    "mixed_surf": "tests/2.5D_mixed_surf/Reference",
+    "decoupling_2d_sink": "tests/GridDecoupling/regular_grids/01_no_decoupling",
+}
+
+CUTMCK = {
+    "minimal": "tests/minimal/Reference/grid",
+    "mixed_surf": "tests/2.5D_mixed_surf/Reference/grid",
+    "decoupling": "tests/GridDecoupling/regular_grids/GRID",
+    "rect_complex": "examples/Grids/Rectangular/02_complex/grid",
+    "mgs_advanced": "examples/MGS/02_advanced/GRID",
+    "error_parameters": "tests/error_parameters/skeleton_files/grid",
+}
+
+
+def main(ref: str):
+    here = os.path.dirname(os.path.abspath(__file__))
+    for name, d in FORWARD.items():
+        out = os.path.join(here, name)
+        os.makedirs(out, exist_ok=True)
+        src = os.path.join(ref, d)
+        for f in ("grid/elem.dat", "grid/elec.dat", "rho/rho.dat", "exe/crmod.cfg", "mod/volt.dat"):
+            shutil.copyfile(os.path.join(src, f), os.path.join(out, os.path.basename(f)))
+        with open(os.path.join(out, "SOURCE"), "w") as fh:
+            fh.write(d + "\n")
+    for name, d in CUTMCK.items():
+        out = os.path.join(here, "cutmck_" + name)
+        os.makedirs(out, exist_ok=True)
+        src = os.path.join(ref, d)
+        for f in ("elem.dat.orig", "elec.dat.orig", "elem.dat", "elec.dat"):
+            shutil.copyfile(os.path.join(src, f), os.path.join(out, f))
+        with open(os.path.join(out, "SOURCE"), "w") as fh:
+            fh.write(d + "\n")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,132 @@
+"""GPU parity: the CUDA forward, factor and sensitivities against the oracle.
+
+Tolerances (relative, max-norm over the array):
+  plain complex128 mode : 1e-10 for kpot, volt, sensitivities
+  mixed complex64+refinement : 1e-6 voltages, 1e-5 sensitivities
+"""
+import numpy as np
+import pytest
+
+from conftest import FORWARD_CASES, load_case, relerr
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+PLAIN_TOL = 1e-10
+MIXED_VOLT_TOL = 1e-6
+MIXED_SENS_TOL = 1e-5
+
+
+def _oracle_forward(g, sv, sig, cfg_swrtr=1, lsink=False, nsink=0):
+    P = O.Problem(g, sv)
+    if cfg_swrtr:
+        kwn, kwnwi = P.rwaven()
+    else:
+        kwn, kwnwi = np.zeros(1), np.zeros(1)
+    kp = P.forward(sig, kwn, kwnwi, swrtr=cfg_swrtr, lsink=lsink, nsink=nsink)
+    hp = P.rtrafo(kp, kwnwi, cfg_swrtr)
+    volt, sigmaa = P.bvolt(hp, 0, None)
+    return P, kwn, kwnwi, kp, hp, volt
+
+
+@pytest.mark.parametrize("case", FORWARD_CASES)
+def test_plain_forward_matches_oracle(gpu_lib, case):
+    from titatest_gb300 import PLAIN, CRMod
+    g, sv, sig, cfg, _ = load_case(case)
+    P, kwn, kwnwi, kp, hp, volt = _oracle_forward(g, sv, sig, cfg.swrtr, cfg.lsink, cfg.nsink)
+    with CRMod(g, sv, kwn, kwnwi, swrtr=cfg.swrtr, lsink=cfg.lsink, nsink=cfg.nsink,
+               precision=PLAIN) as m:
+        out = m.forward(sig, kpot=True, hpot=True)
+    assert relerr(out["kpot"], kp) < PLAIN_TOL
+    assert relerr(out["hpot"], hp) < PLAIN_TOL
+    assert relerr(out["volt"], volt) < PLAIN_TOL
+
+
+@pytest.mark.parametrize("case", ["minimal", "testmodinv"])
+def test_plain_factor_matches_oracle_chol(gpu_lib, case):
+    from titatest_gb300 import PLAIN, CRMod
+    g, sv, sig, cfg, _ = load_case(case)
+    P = O.Problem(g, sv)
+    kwn, kwnwi = P.rwaven()
+    with CRMod(g, sv, kwn, kwnwi, precision=PLAIN) as m:
+        for k, l in [(1, 1), (len(kwn), sv.eanz), (3, 5)]:
+            a_ref, fak_ref = P.factor(sig, kwn, k, l)
+            a, fak = m.factor_system(sig, k, l)
+            np.testing.assert_allclose(fak, fak_ref, rtol=1e-14)
+            # entries outside the band start (columns < 1) are unused in both
+            for i in range(g.sanz):
+                lo = max(0, g.mb - i)
+                assert relerr(a[i, lo:], a_ref[i, lo:]) < 1e-11 or np.max(np.abs(a_ref[i, lo:])) < 1e-300
+
+
+@pytest.mark.parametrize("case", ["minimal", "testmodinv", "mixed_surf"])
+def test_mixed_forward_matches_oracle(gpu_lib, case):
+    from titatest_gb300 import MIXED, CRMod
+    g, sv, sig, cfg, _ = load_case(case)
+    P, kwn, kwnwi, kp, hp, volt = _oracle_forward(g, sv, sig)
+    with CRMod(g, sv, kwn, kwnwi, precision=MIXED) as m:
+        out = m.forward(sig, kpot=True)
+        st = m.stats()
+    assert relerr(out["volt"], volt) < MIXED_VOLT_TOL
+    assert relerr(out["kpot"], kp) < 1e-6
+    assert st["refine_iterations"] >= 1
+
+
+@pytest.fixture(scope="module")
+def cfg1():
+    from titatest_gb300 import synth
+    s = synth.config1()
+    P, kwn, kwnwi, kp, hp, volt = _oracle_forward(s.grid, s.survey, s.sigma)
+    sens0 = P.bsens(kp, kwn, kwnwi, s.sigma, volt, mode=0)
+    sens1 = P.bsens(kp, kwn, kwnwi, s.sigma, volt, mode=1)
+    return s, kwn, kwnwi, kp, volt, sens0, sens1
+
+
+def test_cfg1_plain_forward_and_sensitivities(gpu_lib, cfg1):
+    from titatest_gb300 import PLAIN, CRMod
+    s, kwn, kwnwi, kp, volt, sens0, sens1 = cfg1
+    with CRMod(s.grid, s.survey, kwn, kwnwi, precision=PLAIN) as m:
+        out = m.forward(s.sigma, kpot=True)
+        assert relerr(out["kpot"], kp) < PLAIN_TOL
+        assert relerr(out["volt"], volt) < PLAIN_TOL
+        J0 = m.bsens()
+        assert relerr(J0, sens0) < PLAIN_TOL
+        J1 = m.bsensi()
+        assert relerr(J1, sens1) < PLAIN_TOL
+
+
+def test_cfg1_mixed_forward_and_sensitivities(gpu_lib, cfg1):
+    from titatest_gb300 import MIXED, CRMod
+    s, kwn, kwnwi, kp, volt, sens0, sens1 = cfg1
+    with CRMod(s.grid, s.survey, kwn, kwnwi, precision=MIXED) as m:
+        out = m.forward(s.sigma)
+        assert relerr(out["volt"], volt) < MIXED_VOLT_TOL
+        assert relerr(m.bsens(), sens0) < MIXED_SENS_TOL
+        assert relerr(m.bsensi(), sens1) < MIXED_SENS_TOL
+
+
+def test_volt_matches_reference_golden(gpu_lib):
+    """End to end against the reference's own CRMod output (real*4)."""
+    from titatest_gb300 import PLAIN, CRMod
+    from titatest_gb300 import formats as F
+    g, sv, sig, cfg, (bet, pha) = load_case("testmodinv")
+    with CRMod(g, sv, precision=PLAIN) as m:
+        out = m.forward(sig)
+    b2, p2, v2 = F.volt_record(out["sigmaa"], sv.strnr, sv.vnr)
+    assert np.array_equal(v2, sv.vnr)
+    assert (np.abs(b2 - bet) / np.abs(bet)).max() < 1e-7
+    assert np.abs(p2 - pha).max() < 1e-3
+
+
+def test_zero_conductivity_raises_reference_error(gpu_lib):
+    """A zero diagonal (all-zero sigma) reports src/scalab.f90's error 27."""
+    from titatest_gb300 import PLAIN, CRMod
+    from titatest_gb300._lib import CRGPUError
+    g, sv, sig, cfg, _ = load_case("minimal")
+    with CRMod(g, sv, precision=PLAIN) as m:
+        with pytest.raises(CRGPUError) as ei:
+            m.forward(np.zeros_like(sig))
+        assert ei.value.errnr == 27
+        out = m.forward(sig)  # context still usable
+        assert np.all(np.isfinite(out["volt"]))

@@ -1,0 +1,255 @@
+"""Host-side mirror of the reference's forward-modelling interface.
+
+``CRMod`` follows the control flow of the CRMod driver (src/fem.f90): read the
+inputs, pick the wavenumbers (src/rwaven.f90), then the forward block,
+back-transform, voltages (src/bvolt.f90) and optionally the sensitivities
+(src/bsens.f90) -- every numerical step running in libcrtomo_gb300 on the GPU.
+The routine names of the reference are kept as method names where a method
+stands for one routine (rwaven, bkfak, bsens, bsensi, cutmck).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import formats
+from ._lib import (CGrid, CRGPUError, CStats, CSurvey, f32p, f64p, i32p, lib, make_cgrid, ptr)
+
+PLAIN = 0
+MIXED = 1
+
+
+def _check(ctx, code):
+    if code != 0:
+        text = lib().crgpu_last_error(ctx).decode() if ctx else ""
+        raise CRGPUError(code, text)
+
+
+def rwaven(grid: formats.Grid, survey: formats.Survey):
+    """Wavenumbers and weights of src/rwaven.f90 (computed by the library)."""
+    cg, keep = make_cgrid(grid)
+    enr = np.ascontiguousarray(survey.enr, np.int32)
+    s = np.ascontiguousarray(survey.strnr, np.int32)
+    v = np.ascontiguousarray(survey.vnr, np.int32)
+    kwn = np.zeros(32)
+    kwnwi = np.zeros(32)
+    n = C.c_int32(0)
+    code = lib().crgpu_rwaven(C.byref(cg), survey.eanz, ptr(enr, i32p), survey.nanz, ptr(s, i32p),
+                              ptr(v, i32p), ptr(kwn, f64p), ptr(kwnwi, f64p), C.byref(n))
+    if code:
+        raise CRGPUError(code, "rwaven")
+    return kwn[: n.value].copy(), kwnwi[: n.value].copy()
+
+
+def cutmck(grid: formats.Grid, enr: np.ndarray):
+    """Cuthill-McKee renumbering of cutmckee/cutmck.f: (new grid, new enr)."""
+    g = grid.copy()
+    nrel = g.nrel_colmajor()
+    snr = np.ascontiguousarray(g.snr, np.int32).copy()
+    en = np.ascontiguousarray(enr, np.int32).copy()
+    mb = C.c_int32(0)
+    code = lib().crgpu_cutmck(g.sanz, g.typanz, ptr(np.ascontiguousarray(g.typ, np.int32), i32p),
+                              ptr(np.ascontiguousarray(g.nelanz, np.int32), i32p),
+                              ptr(np.ascontiguousarray(g.selanz, np.int32), i32p), ptr(nrel, i32p),
+                              g.nrel.shape[0], ptr(snr, i32p), len(en), ptr(en, i32p), C.byref(mb))
+    if code:
+        raise CRGPUError(code, "cutmck")
+    g.nrel = np.ascontiguousarray(nrel.T)
+    g.snr = snr
+    g.mb = mb.value
+    return g, en
+
+
+class CRMod:
+    """One grid + survey on the GPU; forward and sensitivities for any sigma.
+
+    precision: PLAIN (complex128, the reference arithmetic) or MIXED (complex64
+    factorisation with FP64 iterative refinement).
+    """
+
+    def __init__(self, grid: formats.Grid, survey: formats.Survey, kwn=None, kwnwi=None,
+                 swrtr: int = 1, lsink: bool = False, nsink: int = 0, lsytop: bool = False,
+                 precision: int = PLAIN, lsr: bool = False):
+        self.grid = grid
+        self.survey = survey
+        if kwn is None:
+            if swrtr:
+                kwn, kwnwi = rwaven(grid, survey)
+            else:
+                kwn, kwnwi = np.zeros(1), np.zeros(1)
+        self.kwn = np.ascontiguousarray(kwn, np.float64)
+        self.kwnwi = np.ascontiguousarray(kwnwi, np.float64)
+        self.swrtr = swrtr
+        self.precision = precision
+        self._cg, self._keep = make_cgrid(grid)
+        self._keep.update(
+            enr=np.ascontiguousarray(survey.enr, np.int32),
+            strnr=np.ascontiguousarray(survey.strnr, np.int32),
+            vnr=np.ascontiguousarray(survey.vnr, np.int32),
+            strom=np.ascontiguousarray(survey.strom, np.float64))
+        k = self._keep
+        self._cs = CSurvey(survey.eanz, ptr(k["enr"], i32p), survey.nanz, ptr(k["strnr"], i32p),
+                           ptr(k["vnr"], i32p), ptr(k["strom"], f64p), len(self.kwn),
+                           ptr(self.kwn, f64p), ptr(self.kwnwi, f64p), int(swrtr), int(lsr),
+                           int(lsink), int(nsink), int(lsytop))
+        h = C.c_void_p()
+        code = lib().crgpu_create(C.byref(self._cg), C.byref(self._cs), int(precision), C.byref(h))
+        self._h = h
+        if code:
+            msg = lib().crgpu_last_error(h).decode() if h.value else ""
+            if h.value:
+                lib().crgpu_destroy(h)
+            self._h = C.c_void_p()
+            raise CRGPUError(code, msg)
+
+    # -- lifetime ---------------------------------------------------------
+    def close(self):
+        if self._h and self._h.value:
+            lib().crgpu_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- options ----------------------------------------------------------
+    def set_refinement(self, maxit: int, tol: float):
+        _check(self._h, lib().crgpu_set_refinement(self._h, int(maxit), C.c_double(tol)))
+
+    def set_memory_budget(self, nbytes: int):
+        _check(self._h, lib().crgpu_set_memory_budget(self._h, C.c_int64(int(nbytes))))
+
+    @property
+    def kwnanz(self) -> int:
+        return len(self.kwn)
+
+    # -- forward ----------------------------------------------------------
+    def forward(self, sigma, kpot: bool = False, hpot: bool = False, volt_mode: int = 0,
+                kfak: Optional[np.ndarray] = None):
+        """Forward block + rtrafo + bvolt/bvolti.  Returns a dict with
+        'volt', 'sigmaa' (nanz complex) and optionally 'kpot'
+        (kwnanz, eanz, sanz) and 'hpot' (eanz, sanz)."""
+        g, sv = self.grid, self.survey
+        sig = np.ascontiguousarray(sigma, np.complex128)
+        out = {"volt": np.zeros(sv.nanz, np.complex128), "sigmaa": np.zeros(sv.nanz, np.complex128)}
+        kp = np.zeros((self.kwnanz, sv.eanz, g.sanz), np.complex128) if kpot else None
+        hp = np.zeros((sv.eanz, g.sanz), np.complex128) if hpot else None
+        kf = None if kfak is None else np.ascontiguousarray(kfak, np.float64)
+        code = lib().crgpu_forward(self._h, ptr(sig, f64p), None if kp is None else ptr(kp, f64p),
+                                   None if hp is None else ptr(hp, f64p), int(volt_mode),
+                                   None if kf is None else ptr(kf, f64p), ptr(out["volt"], f64p),
+                                   ptr(out["sigmaa"], f64p))
+        _check(self._h, code)
+        if kp is not None:
+            out["kpot"] = kp
+        if hp is not None:
+            out["hpot"] = hp
+        return out
+
+    def forward_device(self, sigma_ptr: int, volt_ptr: int, sigmaa_ptr: int = 0, volt_mode: int = 0,
+                       kfak_ptr: int = 0):
+        """Forward with device pointers (e.g. torch tensor data_ptr())."""
+        code = lib().crgpu_forward_device(self._h, C.c_void_p(sigma_ptr), int(volt_mode),
+                                          C.c_void_p(kfak_ptr or None), C.c_void_p(volt_ptr or None),
+                                          C.c_void_p(sigmaa_ptr or None))
+        _check(self._h, code)
+
+    # -- sensitivities ----------------------------------------------------
+    def sens(self, mode: int = 0) -> np.ndarray:
+        """src/bsens.f90 (mode 0) / src/bsensi.f90 (mode 1) of the last
+        forward: array (nanz, elanz) complex128."""
+        sv, g = self.survey, self.grid
+        buf = np.zeros((g.elanz, sv.nanz), np.complex128)  # column-major (nanz, manz)
+        _check(self._h, lib().crgpu_sens(self._h, int(mode), ptr(buf, f64p)))
+        return buf.T
+
+    def bsens(self) -> np.ndarray:
+        return self.sens(0)
+
+    def bsensi(self) -> np.ndarray:
+        return self.sens(1)
+
+    def sens_device(self, mode: int, sens_ptr: int):
+        _check(self._h, lib().crgpu_sens_device(self._h, int(mode), C.c_void_p(sens_ptr)))
+
+    def device_buffers(self):
+        kp = C.c_void_p()
+        hp = C.c_void_p()
+        _check(self._h, lib().crgpu_device_buffers(self._h, C.byref(kp), C.byref(hp)))
+        return kp.value, hp.value
+
+    def factor_system(self, sigma, k: int, l: int):
+        """Band factor a((mb+1)*sanz) and fak of system (k, l), 1-based."""
+        g = self.grid
+        sig = np.ascontiguousarray(sigma, np.complex128)
+        a = np.zeros((g.sanz, g.mb + 1), np.complex128)
+        fak = np.zeros(g.sanz)
+        _check(self._h, lib().crgpu_factor_system(self._h, ptr(sig, f64p), int(k), int(l),
+                                                  ptr(a, f64p), ptr(fak, f64p)))
+        return a, fak
+
+    def bkfak(self) -> np.ndarray:
+        kf = np.zeros(self.survey.nanz)
+        code = lib().crgpu_bkfak(C.byref(self._cg), C.byref(self._cs), ptr(kf, f64p))
+        if code:
+            raise CRGPUError(code, "bkfak")
+        return kf
+
+    def stats(self) -> dict:
+        s = CStats()
+        _check(self._h, lib().crgpu_get_stats(self._h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in CStats._fields_}
+
+    # -- inversion update ---------------------------------------------------
+    def update(self, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx=0, nachbar=None, lam=1.0, eps=1e-4,
+               ncgmax=100, step=1.0, par=None):
+        """src/update.f90 + cjggra on the sensitivities of the last sens(1)."""
+        sv, g = self.survey, self.grid
+        manz = g.elanz
+        par = np.zeros(manz, np.complex128) if par is None else np.array(par, np.complex128)
+        dpar = np.zeros(manz, np.complex128)
+        cgfac = np.zeros(manz)
+        cgres = np.zeros(ncgmax + 2, np.float32)
+        ncg = C.c_int32(0)
+        nb = np.ascontiguousarray(nachbar if nachbar is not None else np.zeros(1), np.int32)
+        code = lib().crgpu_update(
+            self._h, ptr(np.ascontiguousarray(wmatd, np.float64), f64p),
+            ptr(np.ascontiguousarray(wdfak, np.int32), i32p),
+            ptr(np.ascontiguousarray(dat, np.complex128), f64p),
+            ptr(np.ascontiguousarray(sigmaa, np.complex128), f64p), int(ltri),
+            ptr(np.ascontiguousarray(smatm, np.float64), f64p), int(nx), ptr(nb, i32p),
+            C.c_double(lam), C.c_double(eps), int(ncgmax), C.c_double(step), ptr(par, f64p),
+            ptr(dpar, f64p), ptr(cgfac, f64p), ptr(cgres, f32p), C.byref(ncg))
+        _check(self._h, code)
+        return par, dpar, cgfac, cgres, ncg.value
+
+
+def run_tomodir(exe_dir: str, precision: int = PLAIN, write: bool = True):
+    """CRMod on a tomodir: reads exe_dir/crmod.cfg and its inputs, runs the
+    forward (and the sensitivities if requested) and writes volt.dat."""
+    import os
+    td = formats.load_crmod(exe_dir)
+    cfg = td.cfg
+    m = CRMod(td.grid, td.survey, swrtr=cfg.swrtr, lsink=cfg.lsink, nsink=cfg.nsink,
+              precision=precision, lsr=cfg.lsr)
+    try:
+        kfak = m.bkfak() if (cfg.wkfak and td.grid.relanz and 11 in set(td.grid.typ.tolist())) else None
+        out = m.forward(td.sigma, kfak=kfak)
+        if write and cfg.lvolt:
+            formats.write_volt(os.path.normpath(os.path.join(exe_dir, cfg.dvolt)), td.survey.strnr,
+                               td.survey.vnr, out["sigmaa"])
+        if cfg.lsens:
+            out["sens"] = m.bsens()
+        return out
+    finally:
+        m.close()

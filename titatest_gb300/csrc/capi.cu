@@ -1,0 +1,632 @@
+// C ABI of libcrtomo_gb300 (include/crtomo_gb300.h): context management and
+// the orchestration of the forward block (src/fem.f90:327-400), the
+// sensitivities (src/bsens.f90, src/bsensi.f90) and the model update
+// (src/update.f90).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "crgpu_internal.h"
+#include "kernels.h"
+
+using namespace crgpu;
+
+struct crgpu_ctx {
+    HostGrid hg;
+    Pattern pat;
+    DevProblem P{};
+    int precision = CRGPU_PLAIN;
+    int eanz = 0, nanz = 0, K = 0;
+    int swrtr = 1, lsr = 0, lsink = 0, nsink = -1, lsytop = 0;
+    cudaStream_t st = nullptr;
+    int nsm = 0;
+    std::vector<void *> allocs;
+    // device state
+    double2 *d_sigma = nullptr, *d_adom = nullptr, *d_kpot = nullptr, *d_hpot = nullptr;
+    double2 *d_volt = nullptr, *d_sigmaa = nullptr, *d_sens = nullptr;
+    double *d_kfak = nullptr;
+    int *d_err = nullptr;
+    // batch buffers
+    int batch_cap = 0, nrhs = 1;
+    DevBatch Bmax{};
+    int32_t *d_ks = nullptr, *d_ls = nullptr;
+    std::vector<int32_t> sys_k, sys_l;
+    // options
+    int refine_maxit = 6;
+    double refine_tol = 1e-12;
+    int64_t mem_budget = 0;
+    bool have_forward = false;
+    std::string last_error;
+    crgpu_stats stats{};
+    // update work space
+    void *d_upd = nullptr;
+    size_t upd_bytes = 0;
+};
+
+namespace {
+
+int fail(crgpu_ctx *c, int code, const std::string &msg) {
+    if (c) c->last_error = msg;
+    return code;
+}
+
+#define CUCHECK(c, call)                                                              \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess)                                                        \
+            return fail(c, ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T>
+int dalloc(crgpu_ctx *c, T **p, size_t count) {
+    void *q = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+    if (e != cudaSuccess) return fail(c, 94, std::string("device allocation: ") + cudaGetErrorString(e));
+    c->allocs.push_back(q);
+    *p = (T *)q;
+    return 0;
+}
+
+template <typename T>
+int upload(crgpu_ctx *c, const T **dst, const std::vector<T> &v) {
+    T *p = nullptr;
+    int e = dalloc(c, &p, std::max<size_t>(v.size(), 1));
+    if (e) return e;
+    if (!v.empty()) {
+        cudaError_t ce = cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c->st);
+        if (ce != cudaSuccess) return fail(c, ERR_CUDA, cudaGetErrorString(ce));
+    }
+    *dst = p;
+    return 0;
+}
+
+void free_batch(crgpu_ctx *c) {
+    void *ptrs[] = {c->Bmax.As, c->Bmax.fak, c->Bmax.b, c->Bmax.x, c->Bmax.r, c->Bmax.L, c->Bmax.y,
+                    c->Bmax.status, c->Bmax.active, c->d_ks, c->d_ls};
+    for (void *p : ptrs)
+        if (p) {
+            cudaFree(p);
+            c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), p), c->allocs.end());
+        }
+    c->Bmax = DevBatch{};
+    c->d_ks = c->d_ls = nullptr;
+    c->batch_cap = 0;
+}
+
+size_t bytes_per_system(const crgpu_ctx *c) {
+    const size_t n = c->hg.n, W = c->hg.mb + 1, nnz = c->pat.nnz, nr = c->nrhs;
+    size_t esz = c->precision == CRGPU_MIXED ? sizeof(float2) : sizeof(double2);
+    return n * W * esz + nnz * sizeof(double2) + n * sizeof(double) +
+           nr * n * (3 * sizeof(double2) + esz) + 64;
+}
+
+int ensure_batch(crgpu_ctx *c, int want) {
+    if (c->batch_cap >= want) return 0;
+    free_batch(c);
+    const size_t n = c->hg.n, W = c->hg.mb + 1, nnz = c->pat.nnz, nr = c->nrhs;
+    size_t esz = c->precision == CRGPU_MIXED ? sizeof(float2) : sizeof(double2);
+    DevBatch &B = c->Bmax;
+    int e = 0;
+    e = e ? e : dalloc(c, &B.As, (size_t)want * nnz);
+    e = e ? e : dalloc(c, &B.fak, (size_t)want * n);
+    e = e ? e : dalloc(c, &B.b, (size_t)want * nr * n);
+    e = e ? e : dalloc(c, &B.x, (size_t)want * nr * n);
+    e = e ? e : dalloc(c, &B.r, (size_t)want * nr * n);
+    char *L = nullptr, *y = nullptr;
+    e = e ? e : dalloc(c, &L, (size_t)want * n * W * esz);
+    e = e ? e : dalloc(c, &y, (size_t)want * nr * n * esz);
+    e = e ? e : dalloc(c, &B.status, (size_t)want);
+    e = e ? e : dalloc(c, &B.active, (size_t)want * nr);
+    e = e ? e : dalloc(c, &c->d_ks, (size_t)want);
+    e = e ? e : dalloc(c, &c->d_ls, (size_t)want);
+    if (e) return e;
+    B.L = L;
+    B.y = y;
+    c->batch_cap = want;
+    return 0;
+}
+
+int check_device_errors(crgpu_ctx *c, const int *d_status, int nsys) {
+    int h_err = 0;
+    CUCHECK(c, cudaMemcpyAsync(&h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    std::vector<int> st(nsys > 0 ? nsys : 0);
+    if (nsys > 0) CUCHECK(c, cudaMemcpyAsync(st.data(), d_status, sizeof(int) * nsys, cudaMemcpyDeviceToHost, c->st));
+    CUCHECK(c, cudaStreamSynchronize(c->st));
+    if (h_err) return fail(c, h_err, "device reported error " + std::to_string(h_err));
+    for (int s = 0; s < nsys; s++)
+        if (st[s]) {
+            int k = c->sys_k.empty() ? 0 : c->sys_k[s];
+            return fail(c, st[s], "system (k=" + std::to_string(k + 1) + ") failed with error " +
+                                      std::to_string(st[s]));
+        }
+    return 0;
+}
+
+// the forward block on device-resident sigma
+int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const double *d_kfak, double2 *d_volt,
+                double2 *d_sigmaa) {
+    DevProblem &P = c->P;
+    c->stats = crgpu_stats{};
+    cudaEvent_t ev[4];
+    for (auto &e : ev) cudaEventCreate(&e);
+    cudaEventRecord(ev[0], c->st);
+    CUCHECK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+    launch_adom(P, d_sigma, c->d_adom, c->st);
+    c->stats.kernel_launches += 1;
+    const bool mixed = c->precision == CRGPU_MIXED;
+    const int nsys_total = (int)c->sys_k.size();
+    // batch size from the memory budget
+    size_t per = bytes_per_system(c);
+    int64_t budget = c->mem_budget;
+    if (budget <= 0) {
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        budget = (int64_t)(0.6 * (double)(fr + (size_t)c->batch_cap * per));
+    }
+    int bs = (int)std::max<int64_t>(1, std::min<int64_t>(nsys_total, budget / (int64_t)per));
+    if (c->batch_cap > 0 && c->batch_cap < bs && c->batch_cap >= nsys_total) bs = c->batch_cap;
+    int e = ensure_batch(c, bs);
+    if (e) return e;
+    c->stats.nsystems = nsys_total;
+    float t_factor = 0.f, t_solve = 0.f;
+    cudaEvent_t f0, f1, f2;
+    cudaEventCreate(&f0);
+    cudaEventCreate(&f1);
+    cudaEventCreate(&f2);
+    int worst = 0;
+    for (int s0 = 0; s0 < nsys_total; s0 += bs) {
+        int ns = std::min(bs, nsys_total - s0);
+        DevBatch B = c->Bmax;
+        B.nsys = ns;
+        B.ks = c->d_ks;
+        B.ls = c->d_ls;
+        CUCHECK(c, cudaMemcpyAsync(c->d_ks, c->sys_k.data() + s0, sizeof(int32_t) * ns, cudaMemcpyHostToDevice, c->st));
+        CUCHECK(c, cudaMemcpyAsync(c->d_ls, c->sys_l.data() + s0, sizeof(int32_t) * ns, cudaMemcpyHostToDevice, c->st));
+        CUCHECK(c, cudaMemsetAsync(B.status, 0, sizeof(int) * ns, c->st));
+        const int nr = c->nrhs;
+        const int fuse = nr == 1 ? 1 : 0;
+        launch_assemble(P, B, d_sigma, c->d_adom, c->st);
+        launch_rhs(P, B, nr, c->lsink, c->nsink, c->st);
+        c->stats.kernel_launches += 3;
+        cudaEventRecord(f0, c->st);
+        if (mixed) {
+            e = launch_factor_mixed(P, B, fuse, c->nsm, c->st);
+            if (e) return fail(c, e, "mixed precision: band width beyond the supported window");
+        } else {
+            launch_factor_plain(P, B, fuse, c->nsm, c->st);
+        }
+        c->stats.kernel_launches += 1;
+        cudaEventRecord(f1, c->st);
+        DevBatch Bs = B;
+        Bs.active = nullptr;
+        if (!fuse) {
+            launch_forward_solve(P, Bs, nr, mixed, B.b, c->st);
+            c->stats.kernel_launches += 1;
+        }
+        launch_back_solve(P, Bs, nr, mixed, c->st);
+        c->stats.kernel_launches += 1;
+        if (mixed) {
+            CUCHECK(c, cudaMemsetAsync(B.active, 0, sizeof(int) * ns * nr, c->st));
+            // all items active: fill with ones through a tiny memset pattern
+            std::vector<int> ones((size_t)ns * nr, 1);
+            CUCHECK(c, cudaMemcpyAsync(B.active, ones.data(), sizeof(int) * ones.size(), cudaMemcpyHostToDevice, c->st));
+            launch_accumulate(P, B, nr, true, c->refine_tol, c->st);
+            c->stats.kernel_launches += 1;
+            for (int it = 0; it < c->refine_maxit; it++) {
+                launch_residual(P, B, nr, c->st);
+                launch_forward_solve(P, B, nr, true, B.r, c->st);
+                launch_back_solve(P, B, nr, true, c->st);
+                launch_accumulate(P, B, nr, false, c->refine_tol, c->st);
+                c->stats.kernel_launches += 4;
+                c->stats.refine_iterations = it + 1;
+            }
+        } else {
+            launch_copy_solution(P, B, nr, c->st);
+            c->stats.kernel_launches += 1;
+        }
+        launch_kpot(P, B, nr, c->d_kpot, c->st);
+        c->stats.kernel_launches += 1;
+        cudaEventRecord(f2, c->st);
+        c->stats.nbatches++;
+        int ce = check_device_errors(c, B.status, ns);
+        if (ce) {
+            worst = ce;
+            break;
+        }
+        float a = 0, b = 0;
+        cudaEventElapsedTime(&a, f0, f1);
+        cudaEventElapsedTime(&b, f1, f2);
+        t_factor += a;
+        t_solve += b;
+    }
+    cudaEventDestroy(f0);
+    cudaEventDestroy(f1);
+    cudaEventDestroy(f2);
+    if (worst) {
+        for (auto &ev_ : ev) cudaEventDestroy(ev_);
+        return worst;
+    }
+    launch_rtrafo(P, c->d_kpot, c->d_hpot, c->st);
+    launch_bvolt(P, c->d_hpot, volt_mode, d_kfak, d_volt, d_sigmaa, c->st);
+    c->stats.kernel_launches += 2;
+    cudaEventRecord(ev[1], c->st);
+    int ce = check_device_errors(c, nullptr, 0);
+    float tf = 0.f;
+    cudaEventElapsedTime(&tf, ev[0], ev[1]);
+    c->stats.ms_forward = tf;
+    c->stats.ms_factor = t_factor;
+    c->stats.ms_solve = t_solve;
+    for (auto &ev_ : ev) cudaEventDestroy(ev_);
+    CUCHECK(c, cudaGetLastError());
+    if (ce) return ce;
+    c->have_forward = true;
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precision, crgpu_ctx **out) {
+    if (!out) return ERR_ARG;
+    *out = nullptr;
+    crgpu_ctx *c = new crgpu_ctx();
+    int e = build_grid(grid, c->hg, c->last_error);
+    if (!e && (!sv || sv->eanz <= 0 || !sv->enr || sv->nanz < 0 || sv->kwnanz <= 0 || !sv->kwn || !sv->kwnwi)) {
+        e = ERR_ARG;
+        c->last_error = "crgpu_survey: missing arrays";
+    }
+    if (!e && precision != CRGPU_PLAIN && precision != CRGPU_MIXED) {
+        e = ERR_ARG;
+        c->last_error = "precision";
+    }
+    if (!e && sv->lsr) {
+        e = ERR_UNSUPPORTED;
+        c->last_error = "singularity removal (mswitch bit 2) is not supported";
+    }
+    if (!e) e = build_pattern(c->hg, c->pat, c->last_error);
+    if (e) {
+        *out = c;  // keep the message available
+        return e;
+    }
+    c->precision = precision;
+    c->eanz = sv->eanz;
+    c->nanz = sv->nanz;
+    c->K = sv->kwnanz;
+    c->swrtr = sv->swrtr;
+    c->lsink = sv->lsink;
+    c->nsink = sv->lsink ? sv->nsink - 1 : -1;
+    c->lsytop = sv->lsytop;
+    cudaError_t ce = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) {
+        c->last_error = cudaGetErrorString(ce);
+        *out = c;
+        return ERR_CUDA;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev);
+    // device problem
+    DevProblem &P = c->P;
+    const HostGrid &hg = c->hg;
+    P.n = hg.n;
+    P.mb = hg.mb;
+    P.W = hg.mb + 1;
+    P.elanz = hg.elanz;
+    P.relanz = hg.relanz;
+    P.eanz = c->eanz;
+    P.nanz = c->nanz;
+    P.K = c->K;
+    P.nnz = c->pat.nnz;
+    P.nnz_full = c->pat.nnz_full;
+    P.swrtr = c->swrtr;
+    P.sytop = sv->lsytop ? host_sytop(grid) : 0.0;
+    std::vector<int32_t> enr0(c->eanz), meas((size_t)c->nanz * 4);
+    for (int i = 0; i < c->eanz; i++) {
+        if (sv->enr[i] < 1 || sv->enr[i] > hg.n) {
+            c->last_error = "electrode node beyond sanz";
+            *out = c;
+            return 29;
+        }
+        enr0[i] = sv->enr[i] - 1;
+    }
+    for (int i = 0; i < c->nanz; i++) {
+        int a1 = sv->strnr[i] % 10000, a2 = (sv->strnr[i] - a1) / 10000;
+        int a3 = sv->vnr[i] % 10000, a4 = (sv->vnr[i] - a3) / 10000;
+        int el[4] = {a1, a2, a3, a4};
+        for (int q = 0; q < 4; q++) {
+            if (el[q] < 0 || el[q] > c->eanz) {
+                c->last_error = "Electrode pair " + std::to_string(i + 1) + " not correct";
+                *out = c;
+                return 46;
+            }
+            meas[(size_t)i * 4 + q] = el[q] - 1;
+        }
+    }
+    std::vector<double> strom(c->nanz, 1.0), kwn(sv->kwn, sv->kwn + c->K), kwnwi(sv->kwnwi, sv->kwnwi + c->K);
+    if (sv->strom)
+        for (int i = 0; i < c->nanz; i++) strom[i] = sv->strom[i];
+    if (!e) e = upload(c, &P.x, hg.x);
+    if (!e) e = upload(c, &P.y, hg.y);
+    if (!e) e = upload(c, &P.etype, hg.etype);
+    if (!e) e = upload(c, &P.enodes, hg.enodes);
+    if (!e) e = upload(c, &P.btype, hg.btype);
+    if (!e) e = upload(c, &P.bnodes, hg.bnodes);
+    if (!e) e = upload(c, &P.brnr, hg.brnr);
+    if (!e) e = upload(c, &P.dirichlet, hg.dirichlet);
+    if (!e) e = upload(c, &P.rowptr, c->pat.rowptr);
+    if (!e) e = upload(c, &P.col, c->pat.col);
+    if (!e) e = upload(c, &P.row, c->pat.row);
+    if (!e) e = upload(c, &P.dom_ptr, c->pat.dom_ptr);
+    if (!e) e = upload(c, &P.dom_list, c->pat.dom_list);
+    if (!e) e = upload(c, &P.bnd_ptr, c->pat.bnd_ptr);
+    if (!e) e = upload(c, &P.bnd_list, c->pat.bnd_list);
+    if (!e) e = upload(c, &P.fptr, c->pat.fptr);
+    if (!e) e = upload(c, &P.fcol, c->pat.fcol);
+    if (!e) e = upload(c, &P.fidx, c->pat.fidx);
+    if (!e) e = upload(c, &P.enr0, enr0);
+    if (!e) e = upload(c, &P.meas, meas);
+    if (!e) e = upload(c, &P.strom, strom);
+    if (!e) e = upload(c, &P.kwn, kwn);
+    if (!e) e = upload(c, &P.kwnwi, kwnwi);
+    if (!e) e = dalloc(c, &P.elbg, (size_t)c->K * hg.elanz * 10);
+    if (!e) e = dalloc(c, &P.relbg, (size_t)std::max(hg.relanz, 1) * 3);
+    if (!e) e = dalloc(c, &P.kg, (size_t)c->K * c->eanz * std::max(hg.relanz, 1));
+    if (!e) e = dalloc(c, &c->d_err, 1);
+    if (!e) e = dalloc(c, &c->d_sigma, (size_t)hg.elanz);
+    if (!e) e = dalloc(c, &c->d_adom, (size_t)c->K * c->pat.nnz);
+    if (!e) e = dalloc(c, &c->d_kpot, (size_t)c->K * c->eanz * hg.n);
+    if (!e) e = dalloc(c, &c->d_hpot, (size_t)c->eanz * hg.n);
+    if (!e) e = dalloc(c, &c->d_volt, (size_t)std::max(c->nanz, 1));
+    if (!e) e = dalloc(c, &c->d_sigmaa, (size_t)std::max(c->nanz, 1));
+    if (!e) e = dalloc(c, &c->d_kfak, (size_t)std::max(c->nanz, 1));
+    if (e) {
+        *out = c;
+        return e;
+    }
+    P.err = c->d_err;
+    cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st);
+    launch_precal(P, c->st);
+    c->stats.kernel_launches += 3;
+    // systems: one factorisation per (k, l) with mixed boundaries, else one
+    // per k shared by all electrodes (src/fem.f90:355-376)
+    if (hg.lbeta) {
+        c->nrhs = 1;
+        for (int k = 0; k < c->K; k++)
+            for (int l = 0; l < c->eanz; l++) {
+                c->sys_k.push_back(k);
+                c->sys_l.push_back(l);
+            }
+    } else {
+        c->nrhs = c->eanz;
+        for (int k = 0; k < c->K; k++) {
+            c->sys_k.push_back(k);
+            c->sys_l.push_back(0);
+        }
+    }
+    if (precision == CRGPU_MIXED && !mixed_window_supported(hg.mb + 1)) {
+        c->last_error = "mixed precision supports band widths up to 175";
+        *out = c;
+        return ERR_UNSUPPORTED;
+    }
+    int ce2 = check_device_errors(c, nullptr, 0);
+    *out = c;
+    return ce2;
+}
+
+int crgpu_destroy(crgpu_ctx *c) {
+    if (!c) return 0;
+    for (void *p : c->allocs) cudaFree(p);
+    if (c->d_upd) cudaFree(c->d_upd);
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+    return 0;
+}
+
+const char *crgpu_last_error(const crgpu_ctx *c) { return c ? c->last_error.c_str() : "null context"; }
+
+int crgpu_set_refinement(crgpu_ctx *c, int32_t maxit, double tol) {
+    if (!c || maxit < 0 || !(tol >= 0.0)) return ERR_ARG;
+    c->refine_maxit = maxit;
+    c->refine_tol = tol;
+    return 0;
+}
+
+int crgpu_set_memory_budget(crgpu_ctx *c, int64_t bytes) {
+    if (!c) return ERR_ARG;
+    c->mem_budget = bytes;
+    free_batch(c);
+    return 0;
+}
+
+int crgpu_forward_device(crgpu_ctx *c, const void *sigma_device, int32_t volt_mode, const void *kfak_device,
+                         void *volt_device, void *sigmaa_device) {
+    if (!c || !sigma_device) return ERR_ARG;
+    return run_forward(c, (const double2 *)sigma_device, volt_mode, (const double *)kfak_device,
+                       (double2 *)volt_device, (double2 *)sigmaa_device);
+}
+
+int crgpu_forward(crgpu_ctx *c, const double *sigma, double *kpot, double *hpot, int32_t volt_mode,
+                  const double *kfak, double *volt, double *sigmaa) {
+    if (!c || !sigma) return ERR_ARG;
+    const size_t ne = c->hg.elanz, nn = c->hg.n;
+    CUCHECK(c, cudaMemcpyAsync(c->d_sigma, sigma, ne * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+    const double *dk = nullptr;
+    if (kfak) {
+        CUCHECK(c, cudaMemcpyAsync(c->d_kfak, kfak, c->nanz * sizeof(double), cudaMemcpyHostToDevice, c->st));
+        dk = c->d_kfak;
+    }
+    int e = run_forward(c, c->d_sigma, volt_mode, dk, c->d_volt, c->d_sigmaa);
+    if (e) return e;
+    if (kpot)
+        CUCHECK(c, cudaMemcpyAsync(kpot, c->d_kpot, (size_t)c->K * c->eanz * nn * sizeof(double2),
+                                   cudaMemcpyDeviceToHost, c->st));
+    if (hpot)
+        CUCHECK(c, cudaMemcpyAsync(hpot, c->d_hpot, (size_t)c->eanz * nn * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+    if (volt)
+        CUCHECK(c, cudaMemcpyAsync(volt, c->d_volt, (size_t)c->nanz * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+    if (sigmaa)
+        CUCHECK(c, cudaMemcpyAsync(sigmaa, c->d_sigmaa, (size_t)c->nanz * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+    CUCHECK(c, cudaStreamSynchronize(c->st));
+    return 0;
+}
+
+int crgpu_sens_device(crgpu_ctx *c, int32_t mode, void *sens_device) {
+    if (!c || !sens_device || (mode != 0 && mode != 1)) return ERR_ARG;
+    if (!c->have_forward) return fail(c, ERR_ARG, "crgpu_sens before crgpu_forward");
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, c->st);
+    launch_bsens(c->P, c->d_kpot, c->d_sigma, c->d_volt, mode, (double2 *)sens_device, c->st);
+    cudaEventRecord(b, c->st);
+    c->stats.kernel_launches += 1;
+    CUCHECK(c, cudaStreamSynchronize(c->st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    c->stats.ms_sens = ms;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    CUCHECK(c, cudaGetLastError());
+    return 0;
+}
+
+int crgpu_sens(crgpu_ctx *c, int32_t mode, double *sens) {
+    if (!c || !sens) return ERR_ARG;
+    size_t cnt = (size_t)c->nanz * c->hg.elanz;
+    if (!c->d_sens) {
+        int e = dalloc(c, &c->d_sens, cnt);
+        if (e) return e;
+    }
+    int e = crgpu_sens_device(c, mode, c->d_sens);
+    if (e) return e;
+    CUCHECK(c, cudaMemcpyAsync(sens, c->d_sens, cnt * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+    CUCHECK(c, cudaStreamSynchronize(c->st));
+    return 0;
+}
+
+int crgpu_device_buffers(crgpu_ctx *c, void **kpot_device, void **hpot_device) {
+    if (!c) return ERR_ARG;
+    if (kpot_device) *kpot_device = c->d_kpot;
+    if (hpot_device) *hpot_device = c->d_hpot;
+    return 0;
+}
+
+int crgpu_factor_system(crgpu_ctx *c, const double *sigma, int32_t k, int32_t l, double *a, double *fak) {
+    if (!c || !sigma || k < 1 || k > c->K || l < 1 || l > c->eanz) return ERR_ARG;
+    const int n = c->hg.n, W = c->hg.mb + 1;
+    CUCHECK(c, cudaMemcpyAsync(c->d_sigma, sigma, c->hg.elanz * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+    launch_adom(c->P, c->d_sigma, c->d_adom, c->st);
+    int e = ensure_batch(c, std::max(1, c->batch_cap));
+    if (e) return e;
+    DevBatch B = c->Bmax;
+    B.nsys = 1;
+    B.ks = c->d_ks;
+    B.ls = c->d_ls;
+    int32_t kk = k - 1, ll = c->P.relanz && c->hg.lbeta ? l - 1 : 0;
+    CUCHECK(c, cudaMemcpyAsync(c->d_ks, &kk, sizeof(int32_t), cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemcpyAsync(c->d_ls, &ll, sizeof(int32_t), cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemsetAsync(B.status, 0, sizeof(int), c->st));
+    launch_assemble(c->P, B, c->d_sigma, c->d_adom, c->st);
+    launch_rhs(c->P, B, 1, c->lsink, c->nsink, c->st);
+    if (c->precision == CRGPU_MIXED) {
+        e = launch_factor_mixed(c->P, B, 1, c->nsm, c->st);
+        if (e) return fail(c, e, "mixed window");
+    } else {
+        launch_factor_plain(c->P, B, 1, c->nsm, c->st);
+    }
+    e = check_device_errors(c, B.status, 1);
+    if (e) return e;
+    if (a) {
+        if (c->precision == CRGPU_MIXED) {
+            std::vector<float> tmp((size_t)n * W * 2);
+            CUCHECK(c, cudaMemcpy(tmp.data(), B.L, tmp.size() * sizeof(float), cudaMemcpyDeviceToHost));
+            for (size_t q = 0; q < tmp.size(); q++) a[q] = tmp[q];
+        } else {
+            CUCHECK(c, cudaMemcpy(a, B.L, (size_t)n * W * sizeof(double2), cudaMemcpyDeviceToHost));
+        }
+    }
+    if (fak) CUCHECK(c, cudaMemcpy(fak, B.fak, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int crgpu_rwaven(const crgpu_grid *grid, int32_t eanz, const int32_t *enr, int32_t nanz, const int32_t *strnr,
+                 const int32_t *vnr, double *kwn, double *kwnwi, int32_t *kwnanz) {
+    if (!grid || !enr || !strnr || !vnr || !kwn || !kwnwi || !kwnanz) return ERR_ARG;
+    HostGrid hg;
+    std::string msg;
+    int e = build_grid(grid, hg, msg);
+    if (e) return e;
+    for (int i = 0; i < eanz; i++)
+        if (enr[i] < 1 || enr[i] > hg.n) return 29;
+    return host_rwaven(hg, eanz, enr, nanz, strnr, vnr, kwn, kwnwi, kwnanz);
+}
+
+int crgpu_cutmck(int32_t sanz, int32_t typanz, const int32_t *typ, const int32_t *nelanz, const int32_t *selanz,
+                 int32_t *nrel, int32_t ld_nrel, int32_t *snr, int32_t eanz, int32_t *enr, int32_t *mb) {
+    if (!typ || !nelanz || !selanz || !nrel || !snr || !mb || (eanz > 0 && !enr)) return ERR_ARG;
+    return host_cutmck(sanz, typanz, typ, nelanz, selanz, nrel, ld_nrel, snr, eanz, enr, mb);
+}
+
+int crgpu_bkfak(const crgpu_grid *grid, const crgpu_survey *sv, double *kfak) {
+    if (!grid || !sv || !kfak) return ERR_ARG;
+    HostGrid hg;
+    std::string msg;
+    int e = build_grid(grid, hg, msg);
+    if (e) return e;
+    const double pi = 3.14159265358979323846264338327950288;
+    double xk[4] = {0, 0, 0, 0}, yk[4] = {0, 0, 0, 0};
+    for (int i = 0; i < sv->nanz; i++) {
+        int el[4];
+        el[0] = sv->strnr[i] % 10000;
+        el[1] = (sv->strnr[i] - el[0]) / 10000;
+        el[2] = sv->vnr[i] % 10000;
+        el[3] = (sv->vnr[i] - el[2]) / 10000;
+        for (int q = 0; q < 4; q++)
+            if (el[q] > 0) {
+                int nd = sv->enr[el[q] - 1] - 1;
+                xk[q] = hg.x[nd];
+                yk[q] = hg.y[nd];
+            }
+        // r1 (4,2), r2 (4,1), r3 (3,2), r4 (3,1): src/bkfak.f90:79-134
+        const int pr[4][2] = {{3, 1}, {3, 0}, {2, 1}, {2, 0}};
+        double r[4];
+        for (int q = 0; q < 4; q++) {
+            int a = pr[q][0], b = pr[q][1];
+            if (el[a] > 0 && el[b] > 0) {
+                double dx = xk[a] - xk[b], dym = yk[a] - yk[b], dyp = yk[a] + yk[b];
+                dym = 1.0 / std::sqrt(dx * dx + dym * dym);
+                dyp = 1.0 / std::sqrt(dx * dx + dyp * dyp);
+                r[q] = dym + dyp;
+            } else {
+                r[q] = 0.0;
+            }
+        }
+        double dum = (r[0] - r[1]) - (r[2] - r[3]);
+        if (std::fabs(dum) == 0.0) return 93;
+        kfak[i] = 4.0 * pi / dum;
+    }
+    return 0;
+}
+
+int crgpu_get_stats(const crgpu_ctx *c, crgpu_stats *s) {
+    if (!c || !s) return ERR_ARG;
+    *s = c->stats;
+    return 0;
+}
+
+int crgpu_update(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, const double *dat, const double *sigmaa,
+                 int32_t ltri, const double *smatm, int32_t nx, const int32_t *nachbar, double lam, double eps,
+                 int32_t ncgmax, double step, double *par, double *dpar, double *cgfac, float *cgres,
+                 int32_t *ncg) {
+    (void)wmatd; (void)wdfak; (void)dat; (void)sigmaa; (void)ltri; (void)smatm; (void)nx; (void)nachbar;
+    (void)lam; (void)eps; (void)ncgmax; (void)step; (void)par; (void)dpar; (void)cgfac; (void)cgres; (void)ncg;
+    return fail(c, ERR_UNSUPPORTED, "crgpu_update: not built yet");
+}
+
+}  // extern "C"

@@ -1,0 +1,50 @@
+// Device-side problem description shared by the kernels.
+#pragma once
+
+#include <cstdint>
+
+#include "cplx.cuh"
+
+namespace crgpu {
+
+struct DevProblem {
+    int n, mb, W, elanz, relanz, eanz, nanz, K, nnz, nnz_full;
+    int swrtr;
+    double sytop;
+    // grid (node order, 0-based)
+    const double *x, *y;
+    const int32_t *etype, *enodes;          // elanz, elanz*4
+    const int32_t *btype, *bnodes, *brnr;   // relanz, relanz*2, relanz
+    const uint8_t *dirichlet;               // n
+    // band pattern
+    const int32_t *rowptr, *col, *row;
+    const int32_t *dom_ptr, *dom_list, *bnd_ptr, *bnd_list;
+    const int32_t *fptr, *fcol, *fidx;
+    // survey
+    const int32_t *enr0;   // eanz: electrode -> node (0-based)
+    const int32_t *meas;   // nanz*4: electrodes e1,e2,e3,e4 (0-based, -1 = none)
+    const double *strom;   // nanz
+    const double *kwn, *kwnwi;
+    // element matrices (src/precal.f90)
+    double *elbg;          // [K][elanz][10]
+    double *relbg;         // [relanz][3]
+    double *kg;            // [K][eanz][relanz]
+    int *err;              // first error code raised on the device
+};
+
+// Batch of band systems: system s solves wavenumber ks[s], electrode ls[s].
+struct DevBatch {
+    int nsys;
+    const int32_t *ks, *ls;
+    double2 *As;      // [nsys][nnz]   scaled lower-pattern values (FP64)
+    double *fak;      // [nsys][n]     scaling factors of src/scalab.f90
+    double2 *b;       // [nsys][n]     scaled right-hand side (FP64)
+    double2 *x;       // [nsys][n]     solution of A x = b (FP64)
+    double2 *r;       // [nsys][n]     residual / work (FP64)
+    void *L;          // [nsys][n][mb+1] band factor (complex128 or complex64)
+    void *y;          // [nsys][n]     forward-substitution vector (L's type)
+    int *status;      // [nsys]        0 or reference error code
+    int *active;      // [nsys]        refinement still running
+};
+
+}  // namespace crgpu

@@ -1,0 +1,67 @@
+// Kernel launchers (defined in the .cu files) used by the C ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+
+namespace crgpu {
+
+void launch_precal(const DevProblem &P, cudaStream_t st);
+
+// assembly (src/kompab.f90, src/randb.f90, src/scalab.f90, src/kompb.f90)
+void launch_adom(const DevProblem &P, const double2 *sigma, double2 *adom, cudaStream_t st);
+void launch_assemble(const DevProblem &P, const DevBatch &B, const double2 *sigma,
+                     const double2 *adom, cudaStream_t st);
+void launch_rhs(const DevProblem &P, const DevBatch &B, int nrhs, int lsink, int nsink,
+                cudaStream_t st);
+
+// factorisation (src/chol.f90) with fused forward substitution when fuse != 0
+void launch_factor_plain(const DevProblem &P, const DevBatch &B, int fuse, int nsm,
+                         cudaStream_t st);
+int launch_factor_mixed(const DevProblem &P, const DevBatch &B, int fuse, int nsm,
+                        cudaStream_t st);
+int mixed_window_supported(int W);
+
+// triangular solves (src/vre.f90); item = system * nrhs + rhs
+void launch_forward_solve(const DevProblem &P, const DevBatch &B, int nrhs, bool mixed,
+                          const double2 *rin, cudaStream_t st);
+void launch_back_solve(const DevProblem &P, const DevBatch &B, int nrhs, bool mixed,
+                       cudaStream_t st);
+// refinement helpers (FP64)
+void launch_residual(const DevProblem &P, const DevBatch &B, int nrhs, cudaStream_t st);
+void launch_accumulate(const DevProblem &P, const DevBatch &B, int nrhs, bool first,
+                       double tol, cudaStream_t st);
+void launch_copy_solution(const DevProblem &P, const DevBatch &B, int nrhs, cudaStream_t st);
+void launch_kpot(const DevProblem &P, const DevBatch &B, int nrhs, double2 *kpot,
+                 cudaStream_t st);
+
+// back-transform and voltages (src/rtrafo.f90, src/bvolt.f90, src/bvolti.f90)
+void launch_rtrafo(const DevProblem &P, const double2 *kpot, double2 *hpot, cudaStream_t st);
+void launch_bvolt(const DevProblem &P, const double2 *hpot, int mode, const double *kfak,
+                  double2 *volt, double2 *sigmaa, cudaStream_t st);
+
+// sensitivities (src/bsens.f90, src/bsensi.f90)
+void launch_bsens(const DevProblem &P, const double2 *kpot, const double2 *sigma,
+                  const double2 *volt, int mode, double2 *sens, cudaStream_t st);
+
+// update / CG (src/update.f90, src/cg_mod.f90)
+struct CGArgs {
+    int nanz, manz, ltri, nx, maxnk, ncgmax;
+    double lam, eps, step;
+    const double2 *sens;    // column-major (nanz, manz)
+    const double *wmatd;    // nanz
+    const int32_t *wdfak;   // nanz
+    const double2 *dat, *sigmaa;
+    const double *smatm;    // column-major (manz, 3) or (manz, maxnk+1)
+    const int32_t *nachbar; // column-major (manz, maxnk+1)
+    double2 *par, *dpar;
+    double *cgfac;
+    float *cgres;           // ncgmax+2
+    double2 *work;          // 4*manz + nanz + partials
+    double *scal;           // scalars
+    int nblocks;
+};
+int run_update(const CGArgs &a, cudaStream_t st, int *ncg_out);
+
+}  // namespace crgpu

@@ -1,0 +1,175 @@
+// Wavenumber back-transform, voltages and sensitivities:
+// src/rtrafo.f90:13-92, src/bvolt.f90:7-89, src/bvolti.f90:8-100,
+// src/bsens.f90:23-197, src/bsensi.f90:23-194.
+#include "device.cuh"
+#include "kernels.h"
+
+namespace crgpu {
+
+static constexpr double kPi = 3.14159265358979323846264338327950288;
+
+// hpot(j, l) = sum_k kpot(j, l, k) * kwnwi(k) / pi  (2D: kpot(j, l, 1))
+__global__ void k_rtrafo(DevProblem P, const double2 *__restrict__ kpot, double2 *__restrict__ hpot) {
+    size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t tot = (size_t)P.eanz * P.n;
+    if (gid >= tot) return;
+    if (P.swrtr == 0) {
+        hpot[gid] = kpot[gid];
+        return;
+    }
+    double2 s = cz(0.0, 0.0);
+    for (int k = 0; k < P.K; k++) {
+        double2 v = kpot[(size_t)k * tot + gid];
+        double w = P.kwnwi[k];
+        s = cadd(s, cz(v.x * w, v.y * w));
+    }
+    hpot[gid] = cz(s.x / kPi, s.y / kPi);
+}
+
+void launch_rtrafo(const DevProblem &P, const double2 *kpot, double2 *hpot, cudaStream_t st) {
+    size_t tot = (size_t)P.eanz * P.n;
+    int nt = 256;
+    k_rtrafo<<<(unsigned)((tot + nt - 1) / nt), nt, 0, st>>>(P, kpot, hpot);
+}
+
+// V_i = (phi_e2(P_e4) - phi_e1(P_e4)) - (phi_e2(P_e3) - phi_e1(P_e3))
+__global__ void k_bvolt(DevProblem P, const double2 *__restrict__ hpot, int mode,
+                        const double *__restrict__ kfak, double2 *volt, double2 *sigmaa) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.nanz) return;
+    int e1 = P.meas[i * 4], e2 = P.meas[i * 4 + 1], e3 = P.meas[i * 4 + 2], e4 = P.meas[i * 4 + 3];
+    auto hp = [&](int node_e, int src_e) -> double2 {
+        if (node_e < 0 || src_e < 0) return cz(0.0, 0.0);
+        return hpot[(size_t)src_e * P.n + P.enr0[node_e]];
+    };
+    double2 d1 = hp(e4, e2), d2 = hp(e4, e1), d3 = hp(e3, e2), d4 = hp(e3, e1);
+    double2 v = csub(csub(d1, d2), csub(d3, d4));
+    if (volt) volt[i] = v;
+    if (mode == 0) {
+        double kf = kfak ? kfak[i] : 1.0;
+        if (sigmaa) sigmaa[i] = cz(kf * v.x, kf * v.y);
+    } else {
+        double a = cabsd(v);
+        if (!(a > 0.0)) {  // src/bvolti.f90:80-85
+            atomicCAS(P.err, 0, 82);
+            if (sigmaa) sigmaa[i] = cz(0.0, 0.0);
+            return;
+        }
+        if (sigmaa) sigmaa[i] = cz(-log(a), -atan2(v.y, v.x));
+    }
+}
+
+void launch_bvolt(const DevProblem &P, const double2 *hpot, int mode, const double *kfak, double2 *volt,
+                  double2 *sigmaa, cudaStream_t st) {
+    int nt = 128;
+    k_bvolt<<<(P.nanz + nt - 1) / nt, nt, 0, st>>>(P, hpot, mode, kfak, volt, sigmaa);
+}
+
+// ---------------------------------------------------------------------------
+// Sensitivities by reciprocity.  For element e, wavenumber k and measurement
+// i with current electrodes (e1, e2) and voltage electrodes (e3, e4):
+//   hsens_k = sum_{m,n} K_k[m][n] (kpot(node_m,e4) - kpot(node_m,e3))
+//                                 (kpot(node_n,e2) - kpot(node_n,e1))
+// with K_k the element matrix elbg; then the quadrature over k.
+// One block per element; the element's kpot values of all electrodes are
+// staged in shared memory one wavenumber at a time, threads run over
+// measurements and keep their k-sums in registers.
+// ---------------------------------------------------------------------------
+constexpr int kSensThreads = 256;
+constexpr int kSensMPT = 4;  // measurements per thread per pass
+
+template <int MODE>
+__global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P, const double2 *__restrict__ kpot,
+                                                         const double2 *__restrict__ sigma,
+                                                         const double2 *__restrict__ volt,
+                                                         double2 *__restrict__ sens) {
+    extern __shared__ double2 kp_sh[];  // [4][eanz]
+    __shared__ double kel[10];
+    const int e = blockIdx.x;
+    const int nk = P.etype[e] == 3 ? 3 : 4;
+    int nodes[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) nodes[q] = P.enodes[e * 4 + q];
+    const int eanz = P.eanz;
+    for (int i0 = 0; i0 < P.nanz; i0 += kSensThreads * kSensMPT) {
+        double2 acc[kSensMPT];
+        int ee[kSensMPT][4];
+#pragma unroll
+        for (int m = 0; m < kSensMPT; m++) {
+            acc[m] = cz(0.0, 0.0);
+            int i = i0 + m * kSensThreads + threadIdx.x;
+#pragma unroll
+            for (int q = 0; q < 4; q++) ee[m][q] = (i < P.nanz) ? P.meas[i * 4 + q] : -1;
+        }
+        for (int k = 0; k < P.K; k++) {
+            __syncthreads();
+            for (int t = threadIdx.x; t < nk * eanz; t += kSensThreads) {
+                int q = t / eanz, l = t % eanz;
+                kp_sh[t] = kpot[((size_t)k * eanz + l) * P.n + nodes[q]];
+            }
+            if (threadIdx.x < 10) kel[threadIdx.x] = P.elbg[((size_t)k * P.elanz + e) * 10 + threadIdx.x];
+            __syncthreads();
+            const double w = P.swrtr ? P.kwnwi[k] : 1.0;
+#pragma unroll
+            for (int m = 0; m < kSensMPT; m++) {
+                int i = i0 + m * kSensThreads + threadIdx.x;
+                if (i >= P.nanz) continue;
+                double2 u[4], v[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    double2 s1 = ee[m][0] >= 0 ? kp_sh[q * eanz + ee[m][0]] : cz(0.0, 0.0);
+                    double2 s2 = ee[m][1] >= 0 ? kp_sh[q * eanz + ee[m][1]] : cz(0.0, 0.0);
+                    double2 s3 = ee[m][2] >= 0 ? kp_sh[q * eanz + ee[m][2]] : cz(0.0, 0.0);
+                    double2 s4 = ee[m][3] >= 0 ? kp_sh[q * eanz + ee[m][3]] : cz(0.0, 0.0);
+                    u[q] = csub(s2, s1);
+                    v[q] = csub(s4, s3);
+                    if (q >= nk) { u[q] = cz(0.0, 0.0); v[q] = cz(0.0, 0.0); }
+                }
+                double2 hs = cz(0.0, 0.0);
+#pragma unroll
+                for (int mi = 0; mi < 4; mi++) {
+                    if (mi >= nk) continue;
+                    double2 ku = cz(0.0, 0.0);
+#pragma unroll
+                    for (int mj = 0; mj < 4; mj++) {
+                        if (mj >= nk) continue;
+                        int imax = mi > mj ? mi : mj, imin = mi < mj ? mi : mj;
+                        double kk = kel[imax * (imax + 1) / 2 + imin];
+                        ku.x = fma(kk, u[mj].x, ku.x);
+                        ku.y = fma(kk, u[mj].y, ku.y);
+                    }
+                    hs.x = fma(v[mi].x, ku.x, hs.x);
+                    hs.x = fma(-v[mi].y, ku.y, hs.x);
+                    hs.y = fma(v[mi].x, ku.y, hs.y);
+                    hs.y = fma(v[mi].y, ku.x, hs.y);
+                }
+                acc[m].x = fma(hs.x, w, acc[m].x);
+                acc[m].y = fma(hs.y, w, acc[m].y);
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < kSensMPT; m++) {
+            int i = i0 + m * kSensThreads + threadIdx.x;
+            if (i >= P.nanz) continue;
+            double2 d = acc[m];
+            double2 out;
+            if (MODE == 0) {
+                double f = P.swrtr ? P.strom[i] / kPi : P.strom[i];
+                out = cz(-d.x * f, -d.y * f);
+            } else {
+                if (P.swrtr) d = cz(d.x / kPi, d.y / kPi);
+                out = cdiv(cmul(d, sigma[e]), volt[i]);
+            }
+            sens[(size_t)e * P.nanz + i] = out;
+        }
+    }
+}
+
+void launch_bsens(const DevProblem &P, const double2 *kpot, const double2 *sigma, const double2 *volt, int mode,
+                  double2 *sens, cudaStream_t st) {
+    size_t smem = sizeof(double2) * 4 * P.eanz;
+    if (mode == 0) k_bsens<0><<<P.elanz, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens);
+    else k_bsens<1><<<P.elanz, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens);
+}
+
+}  // namespace crgpu
