@@ -1,0 +1,381 @@
+"""Benchmark: 2.5D complex-resistivity forward + Jacobian units per second.
+
+One unit (a "step") is the complete forward -- every wavenumber x current
+electrode assembled, factorised and solved, back-transformed, voltages -- plus
+the full Jacobian (src/bsens.f90), for one conductivity model.  The workload
+is the 200x60-quad, 96-electrode, 4000-quadrupole configuration (synthetic,
+seeded; titatest_gb300.synth.config2).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+value : mixed mode (complex64 factor + FP64 refinement), inputs resident on
+        the device, timed with CUDA events on the library's stream;
+e2e   : the same unit through the host C ABI (crgpu_forward + crgpu_sens with
+        pinned host buffers: sigma in, voltages and the Jacobian out);
+plain : the complex128 mode on the same inputs (the reference arithmetic),
+        with the mixed/plain speed-up and the error of mixed against plain.
+--impl reference times the oracle (the plain-C restatement of the reference
+routines, OpenMP over all host cores) on a bounded sample of the same unit.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "2.5D CR forward+Jacobian/s, mixed vs FP64 plain at 1e-6 rel err; % roofline"
+
+
+def _dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 3 + i and s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def fp32_peak_tflops(torch):
+    """FP32 (SIMT) peak measured here with cuBLAS SGEMM, TF32 disabled."""
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device="cuda", dtype=torch.float32)
+    b = torch.randn(n, n, device="cuda", dtype=torch.float32)
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 0.0
+    for _ in range(5):
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    torch.backends.cuda.matmul.allow_tf32 = old
+    del a, b
+    torch.cuda.empty_cache()
+    return best
+
+
+def read_profile_traffic(name: str):
+    """DRAM bytes per launch recorded from an ncu capture (profiles/<name>)."""
+    p = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(p):
+            if line.startswith("dram_bytes_per_launch_full_workload:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle (plain-C restatement, OpenMP) on a bounded sample
+# ---------------------------------------------------------------------------
+def cpu_baseline(s, kwn, kwnwi, kpot, target_s=12.0, threads=None):
+    from oracle import oracle as O
+    threads = threads or os.cpu_count() or 1
+    P = O.Problem(s.grid, s.survey)
+    K, E = len(kwn), s.survey.eanz
+    nsys = K * E
+    rng = np.random.default_rng(7)
+    # set-up (precal for all wavenumbers and electrodes) is timed once; then
+    # systems are solved in parallel (one per thread), as many rounds as fit
+    t0 = time.perf_counter()
+    P.forward_pairs(s.sigma, kwn, kwnwi, np.zeros((0, 2), np.int32), nthreads=threads)
+    t_setup = time.perf_counter() - t0
+    pairs_all = np.array([(k, l) for k in range(K) for l in range(E)], np.int32)
+    nsample = 2 * threads
+    t_fwd = 0.0
+    solved = 0
+    while t_fwd < target_s * 0.6 and solved < nsys:
+        pick = pairs_all[rng.choice(nsys, size=min(nsample, nsys), replace=False)]
+        t0 = time.perf_counter()
+        P.forward_pairs(s.sigma, kwn, kwnwi, pick, nthreads=threads)
+        t_fwd += time.perf_counter() - t0 - t_setup
+        solved += len(pick)
+    fwd_per_unit = t_setup + t_fwd / solved * nsys
+    # Jacobian: a sample of measurements (timing only; the numbers are those
+    # of the GPU kpot)
+    from titatest_gb300 import formats as F
+    q = max(threads * 4, 64)
+    idx = rng.choice(s.survey.nanz, size=min(q, s.survey.nanz), replace=False)
+    sub = F.Survey(enr=s.survey.enr, strnr=s.survey.strnr[idx], vnr=s.survey.vnr[idx],
+                   strom=s.survey.strom[idx])
+    Ps = O.Problem(s.grid, sub)
+    t0 = time.perf_counter()
+    Ps.bsens(kpot, kwn, kwnwi, s.sigma, None, mode=0, nthreads=threads)
+    t_j = time.perf_counter() - t0
+    sens_per_unit = t_j / len(idx) * s.survey.nanz
+    unit_s = fwd_per_unit + sens_per_unit
+    return {"value": 1.0 / unit_s, "unit": "units/s", "cores": threads, "kind": "port",
+            "sample": (f"{solved} of {nsys} (k,l) systems and {len(idx)} of {s.survey.nanz} Jacobian rows, "
+                       f"scaled to one unit ({t_fwd + t_j:.1f} s of CPU work)"),
+            "seconds_per_unit": unit_s, "forward_s": fwd_per_unit, "sens_s": sens_per_unit}
+
+
+def run_reference(args):
+    rank, world, _ = _dist_env()
+    if rank != 0:
+        return 0
+    from titatest_gb300 import synth
+    from oracle import oracle as O
+    s = synth.make(args.config)
+    P = O.Problem(s.grid, s.survey)
+    kwn, kwnwi = P.rwaven()
+    # potentials for the Jacobian timing: zeros have the same cost
+    kpot = np.zeros((len(kwn), s.survey.eanz, s.grid.sanz), np.complex128)
+    vals = []
+    for it in range(args.warmup + args.steps):
+        cb = cpu_baseline(s, kwn, kwnwi, kpot, target_s=args.ref_seconds)
+        if it >= args.warmup:
+            vals.append(cb["value"])
+    v = statistics.median(vals)
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "units/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"config{args.config}: {s.grid.elanz} elements, {s.grid.sanz} nodes, "
+                                   f"mb={s.grid.mb}, {s.survey.eanz} electrodes, {s.survey.nanz} quadrupoles, "
+                                   f"{len(kwn)} wavenumbers",
+                       "parallelism": f"OpenMP {cb['cores']} threads"},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "units/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+
+    rank, world, local = _dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from titatest_gb300 import MIXED, PLAIN, CRMod, synth
+    from titatest_gb300 import _lib
+
+    s = synth.make(args.config)
+    g, sv = s.grid, s.survey
+    nanz, manz = sv.nanz, g.elanz
+    stream = torch.cuda.current_stream()
+    sig_dev = torch.from_numpy(s.sigma.view(np.float64).copy()).cuda()
+    volt_dev = torch.zeros(2 * nanz, dtype=torch.float64, device="cuda")
+    sens_dev = torch.zeros(2 * nanz * manz, dtype=torch.float64, device="cuda")
+
+    mixed = CRMod(g, sv, precision=MIXED)
+    mixed.set_stream(stream.cuda_stream)
+    mixed.set_refinement(args.refine_maxit, args.refine_tol)
+    K = mixed.kwnanz
+
+    def unit(m):
+        m.forward_device(sig_dev.data_ptr(), volt_dev.data_ptr())
+        m.sens_device(0, sens_dev.data_ptr())
+
+    for _ in range(args.warmup):
+        unit(mixed)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fac_ms, sens_ms, launches, iters = [], [], 0, []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            unit(mixed)
+            st = mixed.stats()
+            fac_ms.append(st["ms_factor"])
+            sens_ms.append(st["ms_sens"])
+            iters.append(st["refine_iterations"])
+            launches += st["kernel_launches"]
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    ms_per_step = elapsed_ms / args.steps
+    value = world * 1e3 / ms_per_step
+    volt_mixed = volt_dev.cpu().numpy().view(np.complex128).copy()
+    sens_mixed = sens_dev.cpu().numpy().view(np.complex128).copy()
+
+    # ---- e2e through the host C ABI with pinned buffers
+    L = _lib.lib()
+    h_sig = torch.from_numpy(s.sigma.view(np.float64).copy()).pin_memory()
+    h_volt = torch.zeros(2 * nanz, dtype=torch.float64).pin_memory()
+    h_sens = torch.zeros(2 * nanz * manz, dtype=torch.float64).pin_memory()
+    import ctypes as C
+
+    def unit_host():
+        rc = L.crgpu_forward(mixed._h, C.c_void_p(h_sig.data_ptr()), None, None, 0, None,
+                             C.c_void_p(h_volt.data_ptr()), None)
+        rc = rc or L.crgpu_sens(mixed._h, 0, C.c_void_p(h_sens.data_ptr()))
+        if rc:
+            raise RuntimeError(f"C ABI error {rc}: {L.crgpu_last_error(mixed._h).decode()}")
+
+    unit_host()
+    torch.cuda.synchronize()
+    e_steps = max(1, min(args.steps, 3))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e_steps):
+        unit_host()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / e_steps
+    h2d = 16 * manz
+    d2h = 16 * nanz + 16 * nanz * manz
+
+    # ---- plain complex128 on the same inputs
+    mixed_stats = mixed.stats()
+    plain = CRMod(g, sv, precision=PLAIN)
+    plain.set_stream(stream.cuda_stream)
+    unit(plain)  # warm-up
+    torch.cuda.synchronize()
+    p_steps = max(1, args.plain_steps)
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for _ in range(p_steps):
+        unit(plain)
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = p0.elapsed_time(p1) / p_steps
+    plain_stats = plain.stats()
+    volt_plain = volt_dev.cpu().numpy().view(np.complex128).copy()
+    sens_plain = sens_dev.cpu().numpy().view(np.complex128).copy()
+    err_v = float(np.abs(volt_mixed - volt_plain).max() / np.abs(volt_plain).max())
+    err_j = float(np.abs(sens_mixed - sens_plain).max() / np.abs(sens_plain).max())
+    plain.close()
+
+    # ---- roofline of the dominant kernel (the mixed band factorisation)
+    n, mb = g.sanz, g.mb
+    nsys = K * sv.eanz
+    flops_factor = nsys * 4.0 * n * mb * mb  # complex LL^T, 8 flops per complex MAC
+    fac_avg_ms = statistics.mean(fac_ms)
+    achieved = flops_factor / (fac_avg_ms * 1e-3) / 1e12
+    peak = fp32_peak_tflops(torch)
+    traffic = read_profile_traffic("k_factor_mixed_cfg2.txt")
+    line = {
+        "metric": METRIC, "value": value, "unit": "units/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64 factor + f64 refinement (c128 assembly, residuals, quadrature, J)",
+        "data": "synthetic (seeded model and survey with the configuration's shapes)",
+        "config": {"workload": f"config{args.config}: {g.elanz} quads, {n} nodes, mb={mb}, {sv.eanz} electrodes, "
+                               f"{nanz} quadrupoles, {K} wavenumbers ({nsys} band systems)",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (band factors of all systems, ~%d GB)" % int(
+                       nsys * n * (mb + 1) * 8 / 1e9),
+                   "refinement": {"maxit": args.refine_maxit, "tol": args.refine_tol,
+                                  "iterations": statistics.mean(iters)}},
+        "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+        "e2e": {"value": 1e3 / e2e_ms, "unit": "units/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "plain": {"value": 1e3 / plain_ms, "unit": "units/s", "ms_per_step": plain_ms,
+                  "ms_factor": plain_stats["ms_factor"], "ms_solve": plain_stats["ms_solve"],
+                  "ms_sens": plain_stats["ms_sens"]},
+        "speedup_mixed_vs_plain": plain_ms / ms_per_step,
+        "mixed_vs_plain_rel_err": {"volt": err_v, "jacobian": err_j},
+        "phases_ms": {"factor": fac_avg_ms, "solve": mixed_stats["ms_solve"],
+                      "forward": mixed_stats["ms_forward"], "sens": statistics.mean(sens_ms)},
+        "roofline": {"kernel": "k_factor_mixed", "bound": "fp32", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": "cuBLAS SGEMM (TF32 off) measured in this run; MEASURED_PEAKS.json "
+                                    "has no FP32 SIMT figure",
+                     "algorithmic": "4*n*mb^2 flops per system (complex LL^T)"},
+    }
+    if rank == 0 and args.cpu_baseline:
+        kpot = mixed.forward(s.sigma, kpot=True)["kpot"]
+        line["cpu_baseline"] = cpu_baseline(s, mixed.kwn, mixed.kwnwi, kpot, target_s=args.ref_seconds)
+    mixed.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", type=int, default=2)
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--refine-maxit", type=int, default=8)
+    ap.add_argument("--refine-tol", type=float, default=1e-8)
+    ap.add_argument("--ref-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -89,8 +89,12 @@ int crgpu_destroy(crgpu_ctx *ctx);
 const char *crgpu_last_error(const crgpu_ctx *ctx);
 
 /* Iterative refinement of the mixed mode: at most maxit corrections, stop a
- * system when max|dx| <= tol * max|x|.  Defaults: 6, 1e-12. */
+ * system when max|dx| <= tol * max|x|.  Defaults: 8, 1e-10. */
 int crgpu_set_refinement(crgpu_ctx *ctx, int32_t maxit, double tol);
+
+/* Stream the context's work is issued on (a cudaStream_t; NULL restores the
+ * context's own stream).  The caller keeps the stream alive. */
+int crgpu_set_stream(crgpu_ctx *ctx, void *stream);
 
 /* Upper bound of device memory for the per-system band factors; systems are
  * processed in batches that fit.  Default: 60% of free device memory. */
@@ -171,13 +175,16 @@ int crgpu_cutmck(int32_t sanz, int32_t typanz, const int32_t *typ, const int32_t
 /* Geometric factors of src/bkfak.f90:7-149 (kfak(nanz)). */
 int crgpu_bkfak(const crgpu_grid *grid, const crgpu_survey *survey, double *kfak);
 
-/* Counters of the last call: kernels launched, and device time (ms) of the
- * forward, factorisation, sensitivity and update phases. */
+/* Counters of the last call: kernels launched, device time (ms) of the
+ * forward, factorisation, solve, sensitivity and update phases, refinement
+ * steps taken and the largest relative correction max|dx|/max|x| of the
+ * last refinement step. */
 typedef struct {
     int64_t kernel_launches;
     double ms_forward, ms_factor, ms_solve, ms_sens, ms_update;
     int32_t refine_iterations;
     int32_t nsystems, nbatches;
+    double refine_last_correction;
 } crgpu_stats;
 int crgpu_get_stats(const crgpu_ctx *ctx, crgpu_stats *stats);
 

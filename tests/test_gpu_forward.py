@@ -38,9 +38,19 @@ def test_plain_forward_matches_oracle(gpu_lib, case):
     with CRMod(g, sv, kwn, kwnwi, swrtr=cfg.swrtr, lsink=cfg.lsink, nsink=cfg.nsink,
                precision=PLAIN) as m:
         out = m.forward(sig, kpot=True, hpot=True)
-    assert relerr(out["kpot"], kp) < PLAIN_TOL
-    assert relerr(out["hpot"], hp) < PLAIN_TOL
-    assert relerr(out["volt"], volt) < PLAIN_TOL
+    gk, gh = out["kpot"], out["hpot"]
+    if cfg.swrtr == 0 and not (g.typ == 11).any():
+        # 2D with no-flow boundaries only: the system is singular and each
+        # potential is fixed only up to a rounding-dependent constant (the
+        # reference's too); compare differences to node 1
+        gk, kp = gk - gk[..., :1], kp - kp[..., :1]
+        gh, hp = gh - gh[..., :1], hp - hp[..., :1]
+        tol = 1e-8
+    else:
+        tol = PLAIN_TOL
+    assert relerr(gk, kp) < tol
+    assert relerr(gh, hp) < tol
+    assert relerr(out["volt"], volt) < tol
 
 
 @pytest.mark.parametrize("case", ["minimal", "testmodinv"])

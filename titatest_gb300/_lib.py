@@ -25,7 +25,7 @@ _lib = None
 
 # every exported entry point of include/crtomo_gb300.h
 EXPORTS = (
-    "crgpu_create", "crgpu_destroy", "crgpu_last_error", "crgpu_set_refinement",
+    "crgpu_create", "crgpu_destroy", "crgpu_last_error", "crgpu_set_refinement", "crgpu_set_stream",
     "crgpu_set_memory_budget", "crgpu_forward", "crgpu_forward_device", "crgpu_sens",
     "crgpu_sens_device", "crgpu_device_buffers", "crgpu_factor_system", "crgpu_update",
     "crgpu_rwaven", "crgpu_cutmck", "crgpu_bkfak", "crgpu_get_stats",
@@ -50,7 +50,8 @@ class CStats(C.Structure):
     _fields_ = [("kernel_launches", C.c_int64), ("ms_forward", C.c_double),
                 ("ms_factor", C.c_double), ("ms_solve", C.c_double), ("ms_sens", C.c_double),
                 ("ms_update", C.c_double), ("refine_iterations", C.c_int32),
-                ("nsystems", C.c_int32), ("nbatches", C.c_int32)]
+                ("nsystems", C.c_int32), ("nbatches", C.c_int32),
+                ("refine_last_correction", C.c_double)]
 
 
 def lib() -> C.CDLL:

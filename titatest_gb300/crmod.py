@@ -126,6 +126,11 @@ class CRMod:
     def set_refinement(self, maxit: int, tol: float):
         _check(self._h, lib().crgpu_set_refinement(self._h, int(maxit), C.c_double(tol)))
 
+    def set_stream(self, stream_handle: int):
+        """Issue the work on a caller-owned cudaStream_t (e.g.
+        torch.cuda.current_stream().cuda_stream); 0 restores the own stream."""
+        _check(self._h, lib().crgpu_set_stream(self._h, C.c_void_p(stream_handle or None)))
+
     def set_memory_budget(self, nbytes: int):
         _check(self._h, lib().crgpu_set_memory_budget(self._h, C.c_int64(int(nbytes))))
 

@@ -59,6 +59,10 @@ __global__ void k_assemble_rows(DevProblem P, DevBatch B, const double2 *__restr
             v = cadd(v, cz(dum * sg.x, dum * sg.y));
         }
         int c = P.col[p];
+        if (c < 0) {
+            as[p] = cz(0.0, 0.0);
+            continue;
+        }
         if (dir_i || P.dirichlet[c]) v = (c == i) ? cz(1.0, 0.0) : cz(0.0, 0.0);
         as[p] = v;
         if (c == i) diag = v;
@@ -78,6 +82,7 @@ __global__ void k_scale(DevProblem P, DevBatch B) {
     int s = (int)(gid / P.nnz), p = (int)(gid % P.nnz);
     double2 *a = B.As + gid;
     int i = P.row[p], c = P.col[p];
+    if (c < 0) return;
     if (i == c) {
         double2 v = *a;
         double dum = cabsd(v);

@@ -21,7 +21,7 @@ struct crgpu_ctx {
     int precision = CRGPU_PLAIN;
     int eanz = 0, nanz = 0, K = 0;
     int swrtr = 1, lsr = 0, lsink = 0, nsink = -1, lsytop = 0;
-    cudaStream_t st = nullptr;
+    cudaStream_t st = nullptr, own_st = nullptr;
     int nsm = 0;
     std::vector<void *> allocs;
     // device state
@@ -35,8 +35,9 @@ struct crgpu_ctx {
     int32_t *d_ks = nullptr, *d_ls = nullptr;
     std::vector<int32_t> sys_k, sys_l;
     // options
-    int refine_maxit = 6;
-    double refine_tol = 1e-12;
+    int refine_maxit = 8;
+    double refine_tol = 1e-10;
+    double last_refine_zmax = 0.0;
     int64_t mem_budget = 0;
     bool have_forward = false;
     std::string last_error;
@@ -86,7 +87,7 @@ int upload(crgpu_ctx *c, const T **dst, const std::vector<T> &v) {
 
 void free_batch(crgpu_ctx *c) {
     void *ptrs[] = {c->Bmax.As, c->Bmax.fak, c->Bmax.b, c->Bmax.x, c->Bmax.r, c->Bmax.L, c->Bmax.y,
-                    c->Bmax.status, c->Bmax.active, c->d_ks, c->d_ls};
+                    c->Bmax.status, c->Bmax.active, (void *)c->Bmax.nactive, c->d_ks, c->d_ls};
     for (void *p : ptrs)
         if (p) {
             cudaFree(p);
@@ -121,6 +122,12 @@ int ensure_batch(crgpu_ctx *c, int want) {
     e = e ? e : dalloc(c, &y, (size_t)want * nr * n * esz);
     e = e ? e : dalloc(c, &B.status, (size_t)want);
     e = e ? e : dalloc(c, &B.active, (size_t)want * nr);
+    {
+        double *cnt = nullptr;  // [0]: int count (+pad), [1]: double zmax
+        e = e ? e : dalloc(c, &cnt, 2);
+        B.nactive = (int *)cnt;
+        B.zmax = cnt + 1;
+    }
     e = e ? e : dalloc(c, &c->d_ks, (size_t)want);
     e = e ? e : dalloc(c, &c->d_ls, (size_t)want);
     if (e) return e;
@@ -214,15 +221,32 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
             // all items active: fill with ones through a tiny memset pattern
             std::vector<int> ones((size_t)ns * nr, 1);
             CUCHECK(c, cudaMemcpyAsync(B.active, ones.data(), sizeof(int) * ones.size(), cudaMemcpyHostToDevice, c->st));
+            B.zmax = nullptr;
+            B.nactive = nullptr;
             launch_accumulate(P, B, nr, true, c->refine_tol, c->st);
+            B = c->Bmax;
+            B.nsys = ns;
+            B.ks = c->d_ks;
+            B.ls = c->d_ls;
             c->stats.kernel_launches += 1;
             for (int it = 0; it < c->refine_maxit; it++) {
+                CUCHECK(c, cudaMemsetAsync(B.nactive, 0, 2 * sizeof(double), c->st));
                 launch_residual(P, B, nr, c->st);
                 launch_forward_solve(P, B, nr, true, B.r, c->st);
                 launch_back_solve(P, B, nr, true, c->st);
                 launch_accumulate(P, B, nr, false, c->refine_tol, c->st);
                 c->stats.kernel_launches += 4;
-                c->stats.refine_iterations = it + 1;
+                c->stats.refine_iterations = std::max(c->stats.refine_iterations, it + 1);
+                struct {
+                    int n;
+                    int pad;
+                    double z;
+                } h{};
+                CUCHECK(c, cudaMemcpyAsync(&h, B.nactive, sizeof(h), cudaMemcpyDeviceToHost, c->st));
+                CUCHECK(c, cudaStreamSynchronize(c->st));
+                c->last_refine_zmax = h.z;
+                c->stats.refine_last_correction = h.z;
+                if (h.n == 0) break;
             }
         } else {
             launch_copy_solution(P, B, nr, c->st);
@@ -301,7 +325,8 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
     c->lsink = sv->lsink;
     c->nsink = sv->lsink ? sv->nsink - 1 : -1;
     c->lsytop = sv->lsytop;
-    cudaError_t ce = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+    cudaError_t ce = cudaStreamCreateWithFlags(&c->own_st, cudaStreamNonBlocking);
+    c->st = c->own_st;
     if (ce != cudaSuccess) {
         c->last_error = cudaGetErrorString(ce);
         *out = c;
@@ -323,6 +348,7 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
     P.K = c->K;
     P.nnz = c->pat.nnz;
     P.nnz_full = c->pat.nnz_full;
+    P.rw = c->pat.rw;
     P.swrtr = c->swrtr;
     P.sytop = sv->lsytop ? host_sytop(grid) : 0.0;
     std::vector<int32_t> enr0(c->eanz), meas((size_t)c->nanz * 4);
@@ -422,7 +448,7 @@ int crgpu_destroy(crgpu_ctx *c) {
     if (!c) return 0;
     for (void *p : c->allocs) cudaFree(p);
     if (c->d_upd) cudaFree(c->d_upd);
-    if (c->st) cudaStreamDestroy(c->st);
+    if (c->own_st) cudaStreamDestroy(c->own_st);
     delete c;
     return 0;
 }
@@ -433,6 +459,12 @@ int crgpu_set_refinement(crgpu_ctx *c, int32_t maxit, double tol) {
     if (!c || maxit < 0 || !(tol >= 0.0)) return ERR_ARG;
     c->refine_maxit = maxit;
     c->refine_tol = tol;
+    return 0;
+}
+
+int crgpu_set_stream(crgpu_ctx *c, void *stream) {
+    if (!c) return ERR_ARG;
+    c->st = stream ? (cudaStream_t)stream : c->own_st;
     return 0;
 }
 
@@ -482,7 +514,8 @@ int crgpu_sens_device(crgpu_ctx *c, int32_t mode, void *sens_device) {
     cudaEventCreate(&a);
     cudaEventCreate(&b);
     cudaEventRecord(a, c->st);
-    launch_bsens(c->P, c->d_kpot, c->d_sigma, c->d_volt, mode, (double2 *)sens_device, c->st);
+    launch_bsens(c->P, c->d_kpot, c->d_sigma, c->d_volt, mode, c->precision == CRGPU_MIXED,
+                 (double2 *)sens_device, c->st);
     cudaEventRecord(b, c->st);
     c->stats.kernel_launches += 1;
     CUCHECK(c, cudaStreamSynchronize(c->st));

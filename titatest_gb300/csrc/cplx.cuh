@@ -16,9 +16,18 @@ __device__ __forceinline__ double2 csub(double2 a, double2 b) { return cz(a.x - 
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
     return cz(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-// s - a*b
+// s - a*b with four fused multiply-adds
 __device__ __forceinline__ double2 cfms(double2 s, double2 a, double2 b) {
-    return cz(s.x - (a.x * b.x - a.y * b.y), s.y - (a.x * b.y + a.y * b.x));
+    double re = fma(-a.x, b.x, s.x);
+    re = fma(a.y, b.y, re);
+    double im = fma(-a.x, b.y, s.y);
+    im = fma(-a.y, b.x, im);
+    return cz(re, im);
+}
+// 1 / d = conj(d) / |d|^2
+__device__ __forceinline__ double2 crecip(double2 d) {
+    double q = 1.0 / (d.x * d.x + d.y * d.y);
+    return cz(d.x * q, -d.y * q);
 }
 __device__ __forceinline__ double2 cscale(double2 a, double s) { return cz(a.x * s, a.y * s); }
 __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
@@ -59,6 +68,10 @@ __device__ __forceinline__ float2 cfmaf(float2 s, float2 a, float2 b) {
     float im = fmaf(a.x, b.y, s.y);
     im = fmaf(a.y, b.x, im);
     return cf(re, im);
+}
+__device__ __forceinline__ float2 crecipf(float2 d) {
+    float q = 1.0f / (d.x * d.x + d.y * d.y);
+    return cf(d.x * q, -d.y * q);
 }
 __device__ __forceinline__ float2 cdivf(float2 a, float2 b) {
     float d = b.x * b.x + b.y * b.y;

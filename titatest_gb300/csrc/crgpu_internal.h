@@ -42,8 +42,8 @@ struct HostGrid {
 // of element contributions of every entry (the summation order of
 // src/kompab.f90:80-138: element order, area elements before boundary ones).
 struct Pattern {
-    int n = 0, nnz = 0, nnz_full = 0;
-    std::vector<int32_t> rowptr, col, row;    // lower incl. diagonal; diagonal last in its row
+    int n = 0, nnz = 0, nnz_full = 0, rw = 1;
+    std::vector<int32_t> rowptr, col, row;    // lower incl. diagonal, rows padded to rw (col -1)
     std::vector<int32_t> dom_ptr, dom_list;   // nnz+1, packed (element << 4) | imn
     std::vector<int32_t> bnd_ptr, bnd_list;   // nnz+1, packed (rel << 4) | imn
     std::vector<int32_t> fptr, fcol, fidx;    // full symmetric CSR -> lower index

@@ -9,6 +9,7 @@ namespace crgpu {
 
 struct DevProblem {
     int n, mb, W, elanz, relanz, eanz, nanz, K, nnz, nnz_full;
+    int rw;               // padded row width of the lower pattern (row i at i*rw)
     int swrtr;
     double sytop;
     // grid (node order, 0-based)
@@ -45,6 +46,8 @@ struct DevBatch {
     void *y;          // [nsys][n]     forward-substitution vector (L's type)
     int *status;      // [nsys]        0 or reference error code
     int *active;      // [nsys]        refinement still running
+    int *nactive;     // count of items still refining after the last correction
+    double *zmax;     // largest relative correction of the last refinement step
 };
 
 }  // namespace crgpu

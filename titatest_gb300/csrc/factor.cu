@@ -20,6 +20,7 @@
 //    r mod W); every thread owns a fixed 4x4 tile of the lower triangle of
 //    slot pairs, so a step needs no data movement: the retiring pivot row's
 //    slot is refilled with the entering row.
+#include "async.cuh"
 #include "device.cuh"
 #include "crgpu_internal.h"
 #include "kernels.h"
@@ -36,7 +37,10 @@ __device__ __forceinline__ void materialize_row_c128(const DevProblem &P, const 
     for (int o = lane; o < W; o += 32) row[o] = cz(0.0, 0.0);
     __syncwarp();
     int p0 = P.rowptr[r], p1 = P.rowptr[r + 1];
-    for (int p = p0 + lane; p < p1; p += 32) row[P.col[p] - r + P.mb] = as[p];
+    for (int p = p0 + lane; p < p1; p += 32) {
+        int c = P.col[p];
+        if (c >= 0) row[c - r + P.mb] = as[p];
+    }
     __syncwarp();
 }
 
@@ -64,20 +68,21 @@ __global__ __launch_bounds__(kPlainThreads) void k_factor_plain(DevProblem P, De
                 if (!(cabsd(a) > 0.0)) bad = 28;  // src/chol.f90:67-71
                 double2 d = csqrtd(a);
                 L[(size_t)j * W + mb] = d;
-                dsh = d;
+                double2 dinv = crecip(d);
+                dsh = dinv;
                 if (fuse) {
-                    double2 yj = cdiv(bv[j], d);
+                    double2 yj = cmul(bv[j], dinv);
                     yv[j] = yj;
                     ysh = yj;
                 }
             }
             __syncthreads();
-            const double2 d = dsh;
+            const double2 dinv = dsh;
             const int R = min(mb, n - 1 - j);
             for (int t = tid; t < R; t += kPlainThreads) {
                 int r = j + 1 + t;
                 size_t idx = (size_t)r * W + (mb - 1 - t);
-                double2 l = cdiv(L[idx], d);
+                double2 l = cmul(L[idx], dinv);
                 L[idx] = l;
                 lcol[t] = l;
                 if (fuse) bv[r] = cfms(bv[r], l, ysh);
@@ -98,40 +103,167 @@ __global__ __launch_bounds__(kPlainThreads) void k_factor_plain(DevProblem P, De
 }
 
 void launch_factor_plain(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st) {
-    int grid = B.nsys < nsm * 4 ? B.nsys : nsm * 4;
+    int grid = B.nsys < nsm * 2 ? B.nsys : nsm * 2;
     size_t smem = sizeof(double2) * (P.mb + 1);
     k_factor_plain<<<grid, kPlainThreads, smem, st>>>(P, B, fuse);
 }
 
 // ---------------------------------------------------------------------------
-// complex64, window in registers
+// complex64, window in registers, 4 columns per step
+//
+// The window holds rows j .. j+WP-1 (WP a multiple of 4, WP >= mb+1).  Row r
+// sits in slot r mod WP; slot s belongs to slot block s/4.  The 4 rows that
+// enter at a block step (they replace the pivot rows, in slot block B) may
+// reach back into the pivot columns when WP < mb+4: their L entries there are
+// computed in the panel step like those of any other window row.  Thread t owns
+// tile (bi, bj), bi >= bj, of the lower triangle of slot-block pairs and keeps
+// its 4x4 complex entries in registers for the whole factorisation.
+//
+// Block step J factors columns j = 4J .. j+3 (pivot slot block B = J mod NB):
+//   1. owners of tiles in block row/column B copy the 4 pivot columns into
+//      the panel (shared memory);
+//   2. one thread per slot computes its 4 entries of L from the 4x4 diagonal
+//      block factor (computed at the end of the previous step by the owner
+//      of that tile) by the same right-looking recurrence as chol; thread 0
+//      does the forward substitution of the 4 right-hand-side entries;
+//   3. every tile applies the rank-4 update; the tiles of block row/column B
+//      first take the values of the 4 entering rows (staged through a
+//      cp.async ring) and then get the same update.
+// Two barriers per 4 columns.
 // ---------------------------------------------------------------------------
 template <int WP>
 struct MixCfg {
     static constexpr int NB = WP / 4;
-    static constexpr int T = NB * (NB + 1) / 2;
-    static constexpr int NT = ((T + 31) / 32) * 32;
+    static constexpr int T = NB * (NB + 1) / 2;      // tiles, one per thread
+    static constexpr int NT = ((T + 31) / 32) * 32 + 32;  // + a staging warp without tiles
 };
 
-// value of the scaled matrix entry (row, col), row >= col, from the pattern
-__device__ __forceinline__ float2 lookup_f(const DevProblem &P, const double2 *as, int row, int col) {
-    for (int p = P.rowptr[row]; p < P.rowptr[row + 1]; p++)
-        if (P.col[p] == col) return to_f(as[p]);
-    return cf(0.f, 0.f);
+constexpr int kStageSteps = 4;  // block steps of look-ahead for entering rows
+
+// issue the cp.async copies of the 4 rows r0..r0+3 (padded pattern values,
+// columns, right-hand side) into ring slot sl; called by the staging warp
+__device__ __forceinline__ void stage_issue4(const DevProblem &P, const double2 *as, const double2 *bv, int r0,
+                                             int ln, int rw, int fuse, double2 (*rv)[32], int (*rc)[32],
+                                             double2 *rb) {
+    const int r = ln >> 3, e0 = ln & 7;
+    const int rr = r0 + r;
+    if (rr < P.n) {
+        for (int e = e0; e < rw; e += 8) {
+            cp_async16(&rv[r][e], as + (size_t)rr * rw + e);
+            cp_async4(&rc[r][e], P.col + (size_t)rr * rw + e);
+        }
+        if (e0 == 7 && fuse) cp_async16(&rb[r], bv + rr);
+    }
+    cp_commit();
+}
+
+// Principal complex square root and reciprocal from the approximate MUFU
+// reciprocal square root / reciprocal (a few ulp): the complex64 factor is a
+// preconditioner for the FP64 refinement.
+__device__ __forceinline__ float2 csqrt_fast(float2 z) {
+    const float r2 = z.x * z.x + z.y * z.y;
+    if (r2 == 0.f) return cf(0.f, 0.f);
+    const float r = r2 * rsqrtf(r2);
+    if (z.x >= 0.f) {
+        const float t2 = 0.5f * (r + z.x);
+        const float it = rsqrtf(t2);
+        return cf(t2 * it, 0.5f * z.y * it);
+    }
+    const float t2 = 0.5f * (r - z.x);
+    const float it = rsqrtf(t2);
+    return cf(0.5f * fabsf(z.y) * it, copysignf(t2 * it, z.y));
+}
+__device__ __forceinline__ float2 crecip_fast(float2 d) {
+    const float q = __fdividef(1.0f, d.x * d.x + d.y * d.y);
+    return cf(d.x * q, -d.y * q);
+}
+
+// In-place L L^T of the 4x4 diagonal tile held in registers (rows j0..j0+3);
+// rows beyond n get a unit pivot.  Publishes L and 1/diag to shared memory.
+__device__ __forceinline__ void factor_diag4(float2 (&w)[4][4], int j0, int n, float2 (*Ld)[4], float2 *dinv,
+                                             int *bad) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        float2 d;
+        if (j0 + q < n) {
+            const float2 v = w[q][q];
+            if (!(cabsf_(v) > 0.f) || !isfinite(v.x) || !isfinite(v.y)) *bad = 28;
+            d = csqrt_fast(v);
+        } else {
+            d = cf(1.f, 0.f);
+        }
+        const float2 di = crecip_fast(d);
+        w[q][q] = d;
+        Ld[q][q] = d;
+        dinv[q] = di;
+#pragma unroll
+        for (int r = q + 1; r < 4; r++) {
+            w[r][q] = cmulf(w[r][q], di);
+            Ld[r][q] = w[r][q];
+        }
+#pragma unroll
+        for (int r = q + 1; r < 4; r++)
+#pragma unroll
+            for (int c = q + 1; c <= r; c++) w[r][c] = cfmsf(w[r][c], w[r][q], w[c][q]);
+    }
+}
+
+// Tile entries from the 4 entering rows staged by slot in nb[4][WP]: a tile
+// of block row B takes row a's slots of its column block, a tile of block
+// column B takes row b's slots of its row block, the diagonal tile takes the
+// rows among themselves.  128-bit shared loads.
+template <int WP>
+__device__ __forceinline__ void refill_tile(float2 (&w)[4][4], const float2 (*nb)[WP], bool rowB, bool colB,
+                                            int sa0, int sb0) {
+    if (rowB && colB) {
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) w[a][b] = nb[a > b ? a : b][sb0 + (a > b ? b : a)];
+    } else if (rowB) {
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            const float4 v0 = *(const float4 *)&nb[a][sb0];
+            const float4 v1 = *(const float4 *)&nb[a][sb0 + 2];
+            w[a][0] = cf(v0.x, v0.y);
+            w[a][1] = cf(v0.z, v0.w);
+            w[a][2] = cf(v1.x, v1.y);
+            w[a][3] = cf(v1.z, v1.w);
+        }
+    } else {
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const float4 v0 = *(const float4 *)&nb[b][sa0];
+            const float4 v1 = *(const float4 *)&nb[b][sa0 + 2];
+            w[0][b] = cf(v0.x, v0.y);
+            w[1][b] = cf(v0.z, v0.w);
+            w[2][b] = cf(v1.x, v1.y);
+            w[3][b] = cf(v1.z, v1.w);
+        }
+    }
 }
 
 template <int WP>
 __global__ __launch_bounds__(MixCfg<WP>::NT, 1) void k_factor_mixed(DevProblem P, DevBatch B, int fuse) {
-    constexpr int T = MixCfg<WP>::T;
-    const int n = P.n, mb = P.mb, W = mb + 1;
+    constexpr int NB = MixCfg<WP>::NB, T = MixCfg<WP>::T;
+    constexpr int D = kStageSteps;
+    const int n = P.n, mb = P.mb, Wb = mb + 1, rw = P.rw;
     const int tid = threadIdx.x;
-    __shared__ float2 lsh[WP];
-    __shared__ float2 nrow[3][WP];
-    __shared__ float2 bsh[WP];
-    __shared__ float2 bnew[3];
-    __shared__ float2 dsh, ysh;
+    const int ln = tid - (int)(blockDim.x - 32);  // lane in the staging warp (< 0 elsewhere)
+    __shared__ __align__(16) float2 panel[4][WP];  // pivot columns: panel[q][s] = a(row of slot s, j+q)
+    // L entries of the step: L(row of slot s, j+q) at lp[q][(s&3)>>1][s>>2][s&1]
+    __shared__ __align__(16) float2 lp[4][2][NB][2];
+    __shared__ __align__(16) float2 nbuf[3][4][WP];  // entering rows by slot, triple buffered
+    __shared__ float2 bsh[WP];              // right-hand side by slot
+    __shared__ float2 bnew[3][4];
+    __shared__ float2 ysh[4];
+    __shared__ float2 Ldsh[4][4];           // factor of the next 4x4 diagonal block (lower)
+    __shared__ float2 dinvsh[4];            // reciprocals of its diagonal
     __shared__ int bad;
-    // tile of this thread: (bi, bj), bi >= bj
+    __shared__ __align__(16) double2 ring_val[D][4][32];
+    __shared__ int ring_col[D][4][32];
+    __shared__ __align__(16) double2 ring_b[D][4];
+    // tile of this thread
     const bool has = tid < T;
     int bi = 0, bj = 0;
     if (has) {
@@ -142,120 +274,207 @@ __global__ __launch_bounds__(MixCfg<WP>::NT, 1) void k_factor_mixed(DevProblem P
         bj = t - bi * (bi + 1) / 2;
     }
     const int sa0 = 4 * bi, sb0 = 4 * bj;
+    const int nblk = (n + 3) / 4;
     for (int s = blockIdx.x; s < B.nsys; s += gridDim.x) {
-        float2 *L = (float2 *)B.L + (size_t)s * n * W;
+        float2 *L = (float2 *)B.L + (size_t)s * n * Wb;
         float2 *yv = (float2 *)B.y + (size_t)s * n;
         const double2 *as = B.As + (size_t)s * P.nnz;
         const double2 *bv = B.b + (size_t)s * n;
+        // ---- initial window: slot q holds row q.  The rows enter 4 at a time
+        // through the refill path (rows only reach back, so block bi's rows
+        // complete every tile of block row bi when they enter).
         float2 w[4][4];
 #pragma unroll
-        for (int q = 0; q < 16; q++) {
-            const int a = q >> 2, b = q & 3;
-            const int sa = sa0 + a, sb = sb0 + b;
-            float2 v = cf(0.f, 0.f);
-            if (has && sa < W && sb < W && sa < n && sb < n) {
-                const int rr = max(sa, sb), cc = min(sa, sb);
-                const int p1 = P.rowptr[rr + 1];
-                for (int pp = P.rowptr[rr]; pp < p1; pp++)
-                    if (P.col[pp] == cc) v = to_f(as[pp]);
-            }
-            w[a][b] = v;
-        }
+        for (int q = 0; q < 16; q++) w[q >> 2][q & 3] = cf(0.f, 0.f);
         for (int q = tid; q < WP; q += blockDim.x) {
-            lsh[q] = cf(0.f, 0.f);
-            bsh[q] = (q < W && q < n && fuse) ? to_f(bv[q]) : cf(0.f, 0.f);
-            nrow[0][q] = nrow[1][q] = nrow[2][q] = cf(0.f, 0.f);
+            bsh[q] = (q < n && fuse) ? to_f(bv[q]) : cf(0.f, 0.f);
+#pragma unroll
+            for (int r = 0; r < 4; r++) nbuf[0][r][q] = nbuf[1][r][q] = nbuf[2][r][q] = cf(0.f, 0.f);
         }
-        if (tid == 0) {
-            bad = 0;
-            bnew[0] = bnew[1] = bnew[2] = cf(0.f, 0.f);
-        }
-        __syncthreads();
-        // stage row W (enters at step 0) in nrow[0]
-        if (tid < 32 && W < n) {
-            int rn = W;
-            for (int p = P.rowptr[rn] + tid; p < P.rowptr[rn + 1]; p += 32) nrow[0][P.col[p] % W] = to_f(as[p]);
-            if (tid == 0 && fuse) bnew[0] = to_f(bv[rn]);
-        }
-        int p = 0;  // slot of row j
-        for (int j = 0; j < n; j++) {
-            const int cur = j % 3;
-            // ---- phase A: pivot
-            if (has && bi == bj && (p >> 2) == bi) {
-                // explicit select: an indexed read would move the tile to local memory
-                const int q3 = p & 3;
-                const float2 v = q3 == 0 ? w[0][0] : (q3 == 1 ? w[1][1] : (q3 == 2 ? w[2][2] : w[3][3]));
-                if (!(cabsf_(v) > 0.f) || !isfinite(v.x) || !isfinite(v.y)) bad = 28;
-                float2 d = csqrtf_(v);
-                dsh = d;
-                L[(size_t)j * W + mb] = d;
+        if (tid < 12) bnew[tid / 4][tid % 4] = cf(0.f, 0.f);
+        if (tid == 0) bad = 0;
+        for (int Jw = 0; Jw < NB; Jw++) {
+            __syncthreads();
+            if (ln >= 0) {
+                const int r = ln >> 3, e0 = ln & 7, rr = 4 * Jw + r;
+                if (rr < n)
+                    for (int e = e0; e < rw; e += 8) {
+                        int c = P.col[(size_t)rr * rw + e];
+                        if (c >= 0) nbuf[0][r][c] = to_f(as[(size_t)rr * rw + e]);
+                    }
             }
             __syncthreads();
-            // ---- phase B: pivot column, refill of the retiring slot
-            const float2 d = dsh;
-            if (has && ((p >> 2) == bi || (p >> 2) == bj)) {
+            if (has && (bi == Jw || bj == Jw)) refill_tile(w, nbuf[0], bi == Jw, bj == Jw, sa0, sb0);
+            __syncthreads();
+            if (tid < WP) {
 #pragma unroll
-                for (int q = 0; q < 16; q++) {
-                    const int a = q >> 2, b = q & 3;
-                    const int sa = sa0 + a, sb = sb0 + b;
-                    const bool ra = sa == p, rb = sb == p;
-                    if (ra && rb) {
-                        w[a][b] = nrow[cur][p];
-                        lsh[p] = cf(0.f, 0.f);
-                    } else if (ra || rb) {
-                        const int other = ra ? sb : sa;
-                        if (other < W) {
-                            float2 l = cdivf(w[a][b], d);
-                            lsh[other] = l;
-                            int dist = other - p;
-                            if (dist < 0) dist += W;
-                            const int r = j + dist;
-                            if (r < n && sa > sb) L[(size_t)r * W + (mb - dist)] = l;
-                        }
-                        w[a][b] = nrow[cur][other];
+                for (int r = 0; r < 4; r++) nbuf[0][r][tid] = cf(0.f, 0.f);
+            }
+        }
+        __syncthreads();
+        if (has && bi == 0 && bj == 0) factor_diag4(w, 0, n, Ldsh, dinvsh, &bad);
+        if (ln >= 0) {
+            // rows WP..WP+3 enter at block step 0: staged directly
+            const int r = ln >> 3, e0 = ln & 7, rr = WP + r;
+            if (rr < n) {
+                for (int e = e0; e < rw; e += 8) {
+                    int c = P.col[(size_t)rr * rw + e];
+                    if (c >= 0) nbuf[0][r][c % WP] = to_f(as[(size_t)rr * rw + e]);
+                }
+                if (e0 == 7 && fuse) bnew[0][r] = to_f(bv[rr]);
+            }
+            // block steps 1..D ahead of time
+            for (int q = 0; q < D; q++) {
+                const int sl = (q + 1) % D;
+                stage_issue4(P, as, bv, WP + 4 * (q + 1), ln, rw, fuse, ring_val[sl], ring_col[sl], ring_b[sl]);
+            }
+        }
+        int Bk = 0;  // pivot slot block of the current step
+        for (int J = 0; J < nblk; J++) {
+            const int j = 4 * J, cur = J % 3;
+            // ---- 1. gather the pivot columns
+            if (has && (bi == Bk) != (bj == Bk)) {
+                if (bi == Bk) {
+#pragma unroll
+                    for (int a = 0; a < 4; a++) {
+                        float4 *d = (float4 *)&panel[a][sb0];
+                        d[0] = make_float4(w[a][0].x, w[a][0].y, w[a][1].x, w[a][1].y);
+                        d[1] = make_float4(w[a][2].x, w[a][2].y, w[a][3].x, w[a][3].y);
+                    }
+                } else {
+#pragma unroll
+                    for (int b = 0; b < 4; b++) {
+                        float4 *d = (float4 *)&panel[b][sa0];
+                        d[0] = make_float4(w[0][b].x, w[0][b].y, w[1][b].x, w[1][b].y);
+                        d[1] = make_float4(w[2][b].x, w[2][b].y, w[3][b].x, w[3][b].y);
                     }
                 }
             }
-            if (fuse && tid == p) {
-                float2 yj = cdivf(bsh[p], d);
-                yv[j] = yj;
-                ysh = yj;
-                bsh[p] = bnew[cur];
+            __syncthreads();
+            // ---- 2. panel: L entries of every window row for columns j..j+3
+            if (tid < WP) {
+                const int sl = tid;
+                const int blk = sl >> 2, b4 = sl & 3;
+                int dist = sl - 4 * Bk;
+                if (dist < 0) dist += WP;
+                const int r_s = j + dist;
+                float2 a[4];
+                int band0;  // first pivot column (0..4) inside the band of this row
+                if (blk == Bk) {
+                    // pivot row j+b4: its row of the diagonal block factor
+                    if (j + b4 < n) {
+                        float2 *row = L + (size_t)(j + b4) * Wb + (mb - b4);  // column j
+                        for (int q = 0; q <= b4; q++) row[q] = Ldsh[b4][q];
+                    }
+                    // the row entering this slot: its entries in the pivot columns
+                    band0 = WP + b4 - mb;  // >= b4 + 1
+#pragma unroll
+                    for (int q = 0; q < 4; q++) a[q] = (q >= band0) ? nbuf[cur][b4][4 * Bk + q] : cf(0.f, 0.f);
+                } else {
+                    band0 = dist - mb;
+#pragma unroll
+                    for (int q = 0; q < 4; q++) a[q] = panel[q][sl];
+                }
+                const int r_l = (blk == Bk) ? j + WP + b4 : r_s;  // row whose L entries these are
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float2 l = cmulf(a[q], dinvsh[q]);
+#pragma unroll
+                    for (int r = q + 1; r < 4; r++) a[r] = cfmsf(a[r], l, Ldsh[r][q]);
+                    a[q] = l;
+                    lp[q][b4 >> 1][blk][b4 & 1] = l;
+                }
+                if (r_l < n && band0 < 4) {
+                    float2 *row = L + (size_t)r_l * Wb + (j - r_l + mb);  // column j
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (q >= band0) row[q] = a[q];
+                }
+            }
+            if (ln == 0 && fuse) {
+                // forward substitution of the 4 pivot entries (staging warp)
+                float2 bb[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) bb[q] = bsh[4 * Bk + q];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float2 yq = cmulf(bb[q], dinvsh[q]);
+                    ysh[q] = yq;
+                    if (j + q < n) yv[j + q] = yq;
+#pragma unroll
+                    for (int r = q + 1; r < 4; r++) bb[r] = cfmsf(bb[r], Ldsh[r][q], yq);
+                }
             }
             __syncthreads();
-            // ---- phase C: rank-1 update of the window
+            // ---- 3. rank-4 update, or refill with the entering rows
             if (has) {
-                float2 la[4], lb[4];
+                if (bi == Bk || bj == Bk) refill_tile(w, nbuf[cur], bi == Bk, bj == Bk, sa0, sb0);
+                // one column at a time: keeps 16 registers of L values live
+#pragma unroll 1
+                for (int q = 0; q < 4; q++) {
+                    float2 la[4], lb[4];
+                    {
+                        const float4 a01 = *(const float4 *)&lp[q][0][bi][0];
+                        const float4 a23 = *(const float4 *)&lp[q][1][bi][0];
+                        const float4 b01 = *(const float4 *)&lp[q][0][bj][0];
+                        const float4 b23 = *(const float4 *)&lp[q][1][bj][0];
+                        la[0] = cf(a01.x, a01.y); la[1] = cf(a01.z, a01.w);
+                        la[2] = cf(a23.x, a23.y); la[3] = cf(a23.z, a23.w);
+                        lb[0] = cf(b01.x, b01.y); lb[1] = cf(b01.z, b01.w);
+                        lb[2] = cf(b23.x, b23.y); lb[3] = cf(b23.z, b23.w);
+                    }
 #pragma unroll
-                for (int a = 0; a < 4; a++) la[a] = lsh[sa0 + a];
+                    for (int a = 0; a < 4; a++)
 #pragma unroll
-                for (int b = 0; b < 4; b++) lb[b] = lsh[sb0 + b];
-#pragma unroll
-                for (int a = 0; a < 4; a++)
-#pragma unroll
-                    for (int b = 0; b < 4; b++) w[a][b] = cfmsf(w[a][b], la[a], lb[b]);
+                        for (int b = 0; b < 4; b++) w[a][b] = cfmsf(w[a][b], la[a], lb[b]);
+                }
+                // the next pivot block: factor it now, off the critical path
+                const int Bn = (Bk + 1 == NB) ? 0 : Bk + 1;
+                if (bi == Bn && bj == Bn) factor_diag4(w, j + 4, n, Ldsh, dinvsh, &bad);
             }
-            if (fuse && tid < W && tid != p) bsh[tid] = cfmsf(bsh[tid], lsh[tid], ysh);
-            // stage row j+1+W for the next step; clear the buffer after it
-            if (tid < W) nrow[(j + 2) % 3][tid] = cf(0.f, 0.f);
-            const int rn = j + 1 + W;
-            if (rn < n && tid >= blockDim.x - 32) {
-                int ln = tid - (blockDim.x - 32);
-                for (int q = P.rowptr[rn] + ln; q < P.rowptr[rn + 1]; q += 32)
-                    nrow[(j + 1) % 3][P.col[q] % W] = to_f(as[q]);
-                if (ln == 0 && fuse) bnew[(j + 1) % 3] = to_f(bv[rn]);
-            } else if (rn >= n && tid == blockDim.x - 1) {
-                bnew[(j + 1) % 3] = cf(0.f, 0.f);
+            if (ln >= 0) {
+                // staging warp: right-hand side update, clearing of the buffer
+                // after next, entering rows of the next step
+                if (fuse)
+                    for (int t = ln; t < WP; t += 32) {
+                        const int blk = t >> 2, b4 = t & 3;
+                        float2 v = (blk == Bk) ? bnew[cur][b4] : bsh[t];
+#pragma unroll
+                        for (int q = 0; q < 4; q++) v = cfmsf(v, lp[q][b4 >> 1][blk][b4 & 1], ysh[q]);
+                        bsh[t] = v;
+                    }
+                for (int t = ln; t < WP; t += 32) {
+#pragma unroll
+                    for (int r = 0; r < 4; r++) nbuf[(J + 2) % 3][r][t] = cf(0.f, 0.f);
+                }
+                __syncwarp();
+                // rows of block step J+1 (issued D steps ago) -> nbuf[(J+1)%3];
+                // then issue the rows of block step J+1+D
+                const int sl = (J + 1) % D, r = ln >> 3, e0 = ln & 7;
+                const int rr = j + 4 + WP + r;
+                cp_wait<D - 1>();
+                if (rr < n) {
+                    for (int e = e0; e < rw; e += 8) {
+                        int c = ring_col[sl][r][e];
+                        if (c >= 0) nbuf[(J + 1) % 3][r][c % WP] = to_f(ring_val[sl][r][e]);
+                    }
+                    if (e0 == 7 && fuse) bnew[(J + 1) % 3][r] = to_f(ring_b[sl][r]);
+                } else if (e0 == 7) {
+                    bnew[(J + 1) % 3][r] = cf(0.f, 0.f);
+                }
+                stage_issue4(P, as, bv, rr - r + 4 * D, ln, rw, fuse, ring_val[sl], ring_col[sl], ring_b[sl]);
             }
-            p = (p + 1 == W) ? 0 : p + 1;
+            Bk = (Bk + 1 == NB) ? 0 : Bk + 1;
         }
+        if (ln >= 0) cp_wait<0>();
         __syncthreads();
         if (tid == 0 && bad) atomicCAS(&B.status[s], 0, bad);
     }
 }
 
-#define CRGPU_MIXED_SIZES(X) X(36) X(64) X(80) X(104) X(124) X(144) X(164) X(176)
+#define CRGPU_MIXED_SIZES(X) X(36) X(64) X(84) X(104) X(124) X(128) X(144) X(160) X(176)
 
+// smallest instantiated window holding W = mb + 1 rows
 int mixed_window_supported(int W) {
 #define X(S) if (W <= S) return S;
     CRGPU_MIXED_SIZES(X)

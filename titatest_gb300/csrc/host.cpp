@@ -183,32 +183,47 @@ int build_pattern(const HostGrid &hg, Pattern &pat, std::string &msg) {
     }
     pat = Pattern();
     pat.n = n;
-    pat.rowptr.assign(n + 1, 0);
+    // rows padded to a fixed width RW (padding entries have col = -1 and no
+    // contributions) so that row i starts at i*RW without an indirection
+    int rw = 1;
     for (int i = 0; i < n; i++) {
         std::sort(rows[i].begin(), rows[i].end(), [](const Ent &a, const Ent &b) { return a.col < b.col; });
-        pat.rowptr[i + 1] = pat.rowptr[i] + (int)rows[i].size();
+        rw = std::max(rw, (int)rows[i].size());
     }
+    if (rw > 31) {
+        msg = "more than 31 lower-pattern entries in one row";
+        return ERR_UNSUPPORTED;
+    }
+    pat.rw = rw;
+    pat.rowptr.assign(n + 1, 0);
+    for (int i = 0; i < n; i++) pat.rowptr[i + 1] = pat.rowptr[i] + rw;
     pat.nnz = pat.rowptr[n];
-    pat.col.resize(pat.nnz);
+    pat.col.assign(pat.nnz, -1);
     pat.row.resize(pat.nnz);
     pat.dom_ptr.assign(pat.nnz + 1, 0);
     pat.bnd_ptr.assign(pat.nnz + 1, 0);
     int p = 0;
     for (int i = 0; i < n; i++)
-        for (auto &e : rows[i]) {
-            pat.col[p] = e.col;
+        for (int q = 0; q < rw; q++, p++) {
             pat.row[p] = i;
-            pat.dom_ptr[p + 1] = pat.dom_ptr[p] + (int)e.dom.size();
-            pat.bnd_ptr[p + 1] = pat.bnd_ptr[p] + (int)e.bnd.size();
-            pat.dom_list.insert(pat.dom_list.end(), e.dom.begin(), e.dom.end());
-            pat.bnd_list.insert(pat.bnd_list.end(), e.bnd.begin(), e.bnd.end());
-            p++;
+            int nd = 0, nb = 0;
+            if (q < (int)rows[i].size()) {
+                const Ent &e = rows[i][q];
+                pat.col[p] = e.col;
+                nd = (int)e.dom.size();
+                nb = (int)e.bnd.size();
+                pat.dom_list.insert(pat.dom_list.end(), e.dom.begin(), e.dom.end());
+                pat.bnd_list.insert(pat.bnd_list.end(), e.bnd.begin(), e.bnd.end());
+            }
+            pat.dom_ptr[p + 1] = pat.dom_ptr[p] + nd;
+            pat.bnd_ptr[p + 1] = pat.bnd_ptr[p] + nb;
         }
     if (pat.dom_list.empty()) pat.dom_list.push_back(0);
     if (pat.bnd_list.empty()) pat.bnd_list.push_back(0);
     // full symmetric CSR
     std::vector<int> cnt(n, 0);
     for (int q = 0; q < pat.nnz; q++) {
+        if (pat.col[q] < 0) continue;
         cnt[pat.row[q]]++;
         if (pat.col[q] != pat.row[q]) cnt[pat.col[q]]++;
     }
@@ -220,6 +235,7 @@ int build_pattern(const HostGrid &hg, Pattern &pat, std::string &msg) {
     std::vector<int> fill(pat.fptr.begin(), pat.fptr.end() - 1);
     for (int q = 0; q < pat.nnz; q++) {
         int r = pat.row[q], c = pat.col[q];
+        if (c < 0) continue;
         pat.fcol[fill[r]] = c;
         pat.fidx[fill[r]++] = q;
         if (r != c) {

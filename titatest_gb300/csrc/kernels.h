@@ -43,7 +43,7 @@ void launch_bvolt(const DevProblem &P, const double2 *hpot, int mode, const doub
 
 // sensitivities (src/bsens.f90, src/bsensi.f90)
 void launch_bsens(const DevProblem &P, const double2 *kpot, const double2 *sigma,
-                  const double2 *volt, int mode, double2 *sens, cudaStream_t st);
+                  const double2 *volt, int mode, bool single, double2 *sens, cudaStream_t st);
 
 // update / CG (src/update.f90, src/cg_mod.f90)
 struct CGArgs {

@@ -78,13 +78,33 @@ void launch_bvolt(const DevProblem &P, const double2 *hpot, int mode, const doub
 constexpr int kSensThreads = 256;
 constexpr int kSensMPT = 4;  // measurements per thread per pass
 
-template <int MODE>
+template <typename R>
+struct SensT;
+template <>
+struct SensT<double> {
+    using C = double2;
+    __device__ static C load(double2 v) { return v; }
+    __device__ static C mk(double a, double b) { return cz(a, b); }
+};
+template <>
+struct SensT<float> {
+    using C = float2;
+    __device__ static C load(double2 v) { return to_f(v); }
+    __device__ static C mk(float a, float b) { return cf(a, b); }
+};
+
+// MODE 0: src/bsens.f90, MODE 1: src/bsensi.f90.  R: arithmetic type of the
+// element contraction (double: the reference arithmetic; float: the mixed
+// mode, with FP64 output).
+template <int MODE, typename R>
 __global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P, const double2 *__restrict__ kpot,
                                                          const double2 *__restrict__ sigma,
                                                          const double2 *__restrict__ volt,
                                                          double2 *__restrict__ sens) {
-    extern __shared__ double2 kp_sh[];  // [4][eanz]
-    __shared__ double kel[10];
+    using C = typename SensT<R>::C;
+    extern __shared__ __align__(16) unsigned char kp_raw[];
+    C *kp_sh = (C *)kp_raw;  // [4][eanz]
+    __shared__ R kel[10];
     const int e = blockIdx.x;
     const int nk = P.etype[e] == 3 ? 3 : 4;
     int nodes[4];
@@ -92,11 +112,11 @@ __global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P, const doub
     for (int q = 0; q < 4; q++) nodes[q] = P.enodes[e * 4 + q];
     const int eanz = P.eanz;
     for (int i0 = 0; i0 < P.nanz; i0 += kSensThreads * kSensMPT) {
-        double2 acc[kSensMPT];
+        C acc[kSensMPT];
         int ee[kSensMPT][4];
 #pragma unroll
         for (int m = 0; m < kSensMPT; m++) {
-            acc[m] = cz(0.0, 0.0);
+            acc[m] = SensT<R>::mk(0, 0);
             int i = i0 + m * kSensThreads + threadIdx.x;
 #pragma unroll
             for (int q = 0; q < 4; q++) ee[m][q] = (i < P.nanz) ? P.meas[i * 4 + q] : -1;
@@ -105,36 +125,36 @@ __global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P, const doub
             __syncthreads();
             for (int t = threadIdx.x; t < nk * eanz; t += kSensThreads) {
                 int q = t / eanz, l = t % eanz;
-                kp_sh[t] = kpot[((size_t)k * eanz + l) * P.n + nodes[q]];
+                kp_sh[t] = SensT<R>::load(kpot[((size_t)k * eanz + l) * P.n + nodes[q]]);
             }
-            if (threadIdx.x < 10) kel[threadIdx.x] = P.elbg[((size_t)k * P.elanz + e) * 10 + threadIdx.x];
+            if (threadIdx.x < 10) kel[threadIdx.x] = (R)P.elbg[((size_t)k * P.elanz + e) * 10 + threadIdx.x];
             __syncthreads();
-            const double w = P.swrtr ? P.kwnwi[k] : 1.0;
+            const R w = P.swrtr ? (R)P.kwnwi[k] : (R)1;
 #pragma unroll
             for (int m = 0; m < kSensMPT; m++) {
                 int i = i0 + m * kSensThreads + threadIdx.x;
                 if (i >= P.nanz) continue;
-                double2 u[4], v[4];
+                C u[4], v[4];
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    double2 s1 = ee[m][0] >= 0 ? kp_sh[q * eanz + ee[m][0]] : cz(0.0, 0.0);
-                    double2 s2 = ee[m][1] >= 0 ? kp_sh[q * eanz + ee[m][1]] : cz(0.0, 0.0);
-                    double2 s3 = ee[m][2] >= 0 ? kp_sh[q * eanz + ee[m][2]] : cz(0.0, 0.0);
-                    double2 s4 = ee[m][3] >= 0 ? kp_sh[q * eanz + ee[m][3]] : cz(0.0, 0.0);
-                    u[q] = csub(s2, s1);
-                    v[q] = csub(s4, s3);
-                    if (q >= nk) { u[q] = cz(0.0, 0.0); v[q] = cz(0.0, 0.0); }
+                    C s1 = ee[m][0] >= 0 ? kp_sh[q * eanz + ee[m][0]] : SensT<R>::mk(0, 0);
+                    C s2 = ee[m][1] >= 0 ? kp_sh[q * eanz + ee[m][1]] : SensT<R>::mk(0, 0);
+                    C s3 = ee[m][2] >= 0 ? kp_sh[q * eanz + ee[m][2]] : SensT<R>::mk(0, 0);
+                    C s4 = ee[m][3] >= 0 ? kp_sh[q * eanz + ee[m][3]] : SensT<R>::mk(0, 0);
+                    u[q] = SensT<R>::mk(s2.x - s1.x, s2.y - s1.y);
+                    v[q] = SensT<R>::mk(s4.x - s3.x, s4.y - s3.y);
+                    if (q >= nk) { u[q] = SensT<R>::mk(0, 0); v[q] = SensT<R>::mk(0, 0); }
                 }
-                double2 hs = cz(0.0, 0.0);
+                C hs = SensT<R>::mk(0, 0);
 #pragma unroll
                 for (int mi = 0; mi < 4; mi++) {
                     if (mi >= nk) continue;
-                    double2 ku = cz(0.0, 0.0);
+                    C ku = SensT<R>::mk(0, 0);
 #pragma unroll
                     for (int mj = 0; mj < 4; mj++) {
                         if (mj >= nk) continue;
                         int imax = mi > mj ? mi : mj, imin = mi < mj ? mi : mj;
-                        double kk = kel[imax * (imax + 1) / 2 + imin];
+                        R kk = kel[imax * (imax + 1) / 2 + imin];
                         ku.x = fma(kk, u[mj].x, ku.x);
                         ku.y = fma(kk, u[mj].y, ku.y);
                     }
@@ -151,7 +171,7 @@ __global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P, const doub
         for (int m = 0; m < kSensMPT; m++) {
             int i = i0 + m * kSensThreads + threadIdx.x;
             if (i >= P.nanz) continue;
-            double2 d = acc[m];
+            double2 d = cz((double)acc[m].x, (double)acc[m].y);
             double2 out;
             if (MODE == 0) {
                 double f = P.swrtr ? P.strom[i] / kPi : P.strom[i];
@@ -166,10 +186,16 @@ __global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P, const doub
 }
 
 void launch_bsens(const DevProblem &P, const double2 *kpot, const double2 *sigma, const double2 *volt, int mode,
-                  double2 *sens, cudaStream_t st) {
-    size_t smem = sizeof(double2) * 4 * P.eanz;
-    if (mode == 0) k_bsens<0><<<P.elanz, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens);
-    else k_bsens<1><<<P.elanz, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens);
+                  bool single, double2 *sens, cudaStream_t st) {
+    if (single) {
+        size_t smem = sizeof(float2) * 4 * P.eanz;
+        if (mode == 0) k_bsens<0, float><<<P.elanz, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens);
+        else k_bsens<1, float><<<P.elanz, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens);
+    } else {
+        size_t smem = sizeof(double2) * 4 * P.eanz;
+        if (mode == 0) k_bsens<0, double><<<P.elanz, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens);
+        else k_bsens<1, double><<<P.elanz, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens);
+    }
 }
 
 }  // namespace crgpu

@@ -1,13 +1,13 @@
 // Band triangular solves (src/vre.f90:5-71), FP64 iterative refinement of the
 // mixed mode, and the unscaling into kpot (src/fem.f90:383-394).
 //
-// One warp solves one right-hand side.  Both sweeps keep a W = mb+1 window of
-// the working vector in shared memory (entry i in slot i mod W):
-//   forward  L y = b : column j of L is gathered from the rows j+1..j+mb
-//                      (addresses step by mb; the same sectors serve the next
-//                      three columns, so L1 absorbs the gather);
-//   backward L^T x = y: row i of L is read contiguously (the vre update
-//                      pot(j) += a(i,j) * pot(i)).
+// One warp solves one right-hand side.  Both sweeps read the band rows of L
+// contiguously, streamed kRing rows ahead into shared memory by cp.async, and
+// keep a W = mb+1 window of the working vector in shared memory (entry i in
+// slot i mod W):
+//   forward  L y = b : row-oriented, a warp-reduced dot product per row;
+//   backward L^T x = y: the column sweep of vre (x_i broadcast, W updates).
+#include "async.cuh"
 #include "device.cuh"
 #include "kernels.h"
 
@@ -23,6 +23,16 @@ struct Ops<double2> {
     __device__ static double2 shfl(double2 a, int src) {
         return cz(__shfl_sync(0xffffffffu, a.x, src), __shfl_sync(0xffffffffu, a.y, src));
     }
+    __device__ static double2 add(double2 a, double2 b) { return cadd(a, b); }
+    __device__ static double2 mul(double2 a, double2 b) { return cmul(a, b); }
+    __device__ static double2 rcp(double2 a) { return crecip(a); }
+    __device__ static double2 reduce(double2 a) {
+        for (int o = 16; o > 0; o >>= 1) {
+            a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
+            a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
+        }
+        return a;
+    }
 };
 template <>
 struct Ops<float2> {
@@ -32,100 +42,200 @@ struct Ops<float2> {
     __device__ static float2 shfl(float2 a, int src) {
         return cf(__shfl_sync(0xffffffffu, a.x, src), __shfl_sync(0xffffffffu, a.y, src));
     }
+    __device__ static float2 add(float2 a, float2 b) { return caddf(a, b); }
+    __device__ static float2 mul(float2 a, float2 b) { return cmulf(a, b); }
+    __device__ static float2 rcp(float2 a) {  // approximate reciprocal: the solves refine in FP64
+        const float q = __fdividef(1.0f, a.x * a.x + a.y * a.y);
+        return cf(a.x * q, -a.y * q);
+    }
+    __device__ static float2 reduce(float2 a) {
+        for (int o = 16; o > 0; o >>= 1) {
+            a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
+            a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
+        }
+        return a;
+    }
 };
 
 constexpr int kSolveWarps = 4;
+constexpr int kRing = 8;  // rows of look-ahead streamed by cp.async
 
-// y = L^{-1} rin (rin FP64, converted to T); items whose active flag is 0 are skipped
+// per-warp shared memory: kRing vector entries, kRing rows, the W window;
+// rounded to 16 bytes so every warp's region keeps cp.async alignment
+template <typename T>
+__host__ __device__ constexpr size_t solve_smem_per_warp(int W) {
+    return (((size_t)kRing * W * sizeof(T) + (size_t)W * sizeof(T) + (size_t)kRing * sizeof(double2)) + 15) & ~(size_t)15;
+}
+
+// issue row rr of L (W entries) and vector entry vv (if >= 0) into ring slot sl
+template <typename T>
+__device__ __forceinline__ void ring_issue(const T *L, int W, int rr, int n, T *slot, const double2 *vsrc,
+                                           double2 *vdst, int lane) {
+    if (rr >= 0 && rr < n) {
+        const T *row = L + (size_t)rr * W;
+        for (int o = lane; o < W; o += 32) cp_async_elem<T>(slot + o, row + o);
+        if (lane == 0 && vsrc) cp_async16(vdst, vsrc);
+    }
+    cp_commit();
+}
+
+// the same with a vector entry of type T (the back sweep's entering y values)
+template <typename T>
+__device__ __forceinline__ void ring_issue_v(const T *L, int W, int rr, int n, T *slot, const T *vsrc, T *vdst,
+                                             int lane) {
+    if (rr >= 0 && rr < n) {
+        const T *row = L + (size_t)rr * W;
+        for (int o = lane; o < W; o += 32) cp_async_elem<T>(slot + o, row + o);
+        if (lane == 0 && vsrc) cp_async_elem<T>(vdst, vsrc);
+    }
+    cp_commit();
+}
+
+// Row-oriented forward substitution y = L^{-1} rin:
+//   y_i = (rin_i - sum_{j=i-mb}^{i-1} L(i,j) y_j) / L(i,i)
+// rows stream through a ring of kRing slots; the last W values of y sit in
+// a shared-memory window (y_j in slot j mod W, tracked incrementally).
+// Items whose active flag is 0 are skipped.
 template <typename T>
 __global__ __launch_bounds__(kSolveWarps * 32) void k_fwd(DevProblem P, DevBatch B, int nrhs,
                                                            const double2 *__restrict__ rin) {
-    extern __shared__ unsigned char sm_raw[];
+    extern __shared__ __align__(16) unsigned char sm_raw[];
     const int n = P.n, mb = P.mb, W = mb + 1;
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    T *pw = (T *)sm_raw + (size_t)wl * W;
-    int item = blockIdx.x * kSolveWarps + wl;
-    int nitems = B.nsys * nrhs;
-    if (item >= nitems) return;
+    unsigned char *base = sm_raw + (size_t)wl * solve_smem_per_warp<T>(W);
+    double2 *rv = (double2 *)base;                       // [kRing]
+    T *ring = (T *)(base + kRing * sizeof(double2));     // [kRing][W]
+    T *pw = ring + (size_t)kRing * W;                    // [W]
+    const int item = blockIdx.x * kSolveWarps + wl;
+    if (item >= B.nsys * nrhs) return;
     if (B.active && !B.active[item]) return;
-    int s = item / nrhs;
+    const int s = item / nrhs;
     const T *L = (const T *)B.L + (size_t)s * n * W;
     const double2 *r = rin + (size_t)item * n;
     T *y = (T *)B.y + (size_t)item * n;
-    for (int q = lane; q < W; q += 32) pw[q] = (q < n) ? Ops<T>::from(r[q]) : T{};
-    __syncwarp();
-    for (int j = 0; j < n; j++) {
-        T v{};
+    for (int q = lane; q < W; q += 32) pw[q] = T{};
+    for (int q = 0; q < kRing; q++) ring_issue<T>(L, W, q, n, ring + (size_t)q * W, r + q, rv + q, lane);
+    int sb = 1;  // slot of column i - mb (== (i - mb) mod W); row i's slot is sb + mb - W or sb - 1
+    int sl = 0;  // ring slot of row i
+    for (int i = 0; i < n; i++) {
+        const T *row = ring + (size_t)sl * W;
+        cp_wait<kRing - 1>();
+        __syncwarp();
+        // read the diagonal and the right-hand side before any lane can
+        // re-issue copies into this ring slot
+        const T dg = row[mb];
+        const double2 rhs = rv[sl];
+        T acc{};
+        const int o0 = i < mb ? mb - i : 0;
+        for (int o = o0 + lane; o < mb; o += 32) {
+            int sw = sb + o;
+            if (sw >= W) sw -= W;
+            acc = Ops<T>::fms(acc, row[o], pw[sw]);
+        }
+        acc = Ops<T>::reduce(acc);  // acc = -sum
+        const int si = sb == 0 ? W - 1 : sb - 1;  // slot of row i == (i - mb - 1) mod W
         if (lane == 0) {
-            v = Ops<T>::div(pw[j % W], L[(size_t)j * W + mb]);
-            y[j] = v;
+            const T v = Ops<T>::mul(Ops<T>::add(Ops<T>::from(rhs), acc), Ops<T>::rcp(dg));
+            pw[si] = v;
+            y[i] = v;
         }
-        v = Ops<T>::shfl(v, 0);
-        const int R = min(mb, n - 1 - j);
-        for (int o = lane; o < R; o += 32) {
-            int rr = j + 1 + o;
-            int sl = rr % W;
-            pw[sl] = Ops<T>::fms(pw[sl], L[(size_t)rr * W + (mb - 1 - o)], v);
-        }
-        __syncwarp();
-        if (lane == 0 && j + W < n) pw[j % W] = Ops<T>::from(r[j + W]);
-        __syncwarp();
+        ring_issue<T>(L, W, i + kRing, n, ring + (size_t)sl * W, i + kRing < n ? r + i + kRing : nullptr,
+                      rv + sl, lane);
+        sb = sb + 1 == W ? 0 : sb + 1;
+        sl = sl + 1 == kRing ? 0 : sl + 1;
     }
+    cp_wait<0>();
 }
 
-// x = L^{-T} y in place (y -> x); items whose active flag is 0 are skipped
+// Backward substitution L^T x = y in place (y -> x), the column sweep of
+// src/vre.f90:58-69: x_i = w_i / L(i,i); w_j -= L(i,j) x_i for j < i.
 template <typename T>
 __global__ __launch_bounds__(kSolveWarps * 32) void k_bwd(DevProblem P, DevBatch B, int nrhs) {
-    extern __shared__ unsigned char sm_raw[];
+    extern __shared__ __align__(16) unsigned char sm_raw[];
     const int n = P.n, mb = P.mb, W = mb + 1;
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    T *pw = (T *)sm_raw + (size_t)wl * W;
-    int item = blockIdx.x * kSolveWarps + wl;
-    int nitems = B.nsys * nrhs;
-    if (item >= nitems) return;
+    unsigned char *base = sm_raw + (size_t)wl * solve_smem_per_warp<T>(W);
+    double2 *rv = (double2 *)base;  // entering entries y[i - W], as raw bytes of T
+    T *ring = (T *)(base + kRing * sizeof(double2));
+    T *pw = ring + (size_t)kRing * W;
+    const int item = blockIdx.x * kSolveWarps + wl;
+    if (item >= B.nsys * nrhs) return;
     if (B.active && !B.active[item]) return;
-    int s = item / nrhs;
+    const int s = item / nrhs;
     const T *L = (const T *)B.L + (size_t)s * n * W;
     T *y = (T *)B.y + (size_t)item * n;
-    int j0 = n - W < 0 ? 0 : n - W;
+    // window slot of entry j is j mod W
+    const int j0 = n - W < 0 ? 0 : n - W;
     for (int q = j0 + lane; q < n; q += 32) pw[q % W] = y[q];
-    __syncwarp();
+    for (int q = 0; q < kRing; q++) {
+        const int rr = n - 1 - q;
+        ring_issue_v<T>(L, W, rr, n, ring + (size_t)q * W, rr - W >= 0 ? y + (rr - W) : nullptr, (T *)(rv + q), lane);
+    }
+    int si = (n - 1) % W;            // slot of row i
+    int sb = si + 1 == W ? 0 : si + 1;  // slot of column i - mb (== (i + 1) mod W)
+    int sl = 0;
     for (int i = n - 1; i >= 0; i--) {
-        const T *row = L + (size_t)i * W;
+        const T *row = ring + (size_t)sl * W;
+        cp_wait<kRing - 1>();
+        __syncwarp();
         T v{};
         if (lane == 0) {
-            v = Ops<T>::div(pw[i % W], row[mb]);
+            v = Ops<T>::mul(pw[si], Ops<T>::rcp(row[mb]));
             y[i] = v;
         }
         v = Ops<T>::shfl(v, 0);
-        int o0 = mb - i;  // first offset with column >= 0
-        if (o0 < 0) o0 = 0;
+        const int o0 = i < mb ? mb - i : 0;
         for (int o = o0 + lane; o < mb; o += 32) {
-            int jj = i - mb + o;
-            int sl = jj % W;
-            pw[sl] = Ops<T>::fms(pw[sl], row[o], v);
+            int sw = sb + o;
+            if (sw >= W) sw -= W;
+            pw[sw] = Ops<T>::fms(pw[sw], row[o], v);
         }
-        __syncwarp();
-        if (lane == 0 && i - W >= 0) pw[i % W] = y[i - W];
-        __syncwarp();
+        if (lane == 0 && i - W >= 0) pw[si] = *(const T *)(rv + sl);
+        const int rr = i - kRing;
+        ring_issue_v<T>(L, W, rr, n, ring + (size_t)sl * W, rr - W >= 0 ? y + (rr - W) : nullptr, (T *)(rv + sl),
+                        lane);
+        si = si == 0 ? W - 1 : si - 1;
+        sb = sb == 0 ? W - 1 : sb - 1;
+        sl = sl + 1 == kRing ? 0 : sl + 1;
     }
+    cp_wait<0>();
+}
+
+template <typename T>
+static void set_solve_smem(int W) {
+    static int done_w = -1;
+    if (done_w == W) return;
+    size_t bytes = kSolveWarps * solve_smem_per_warp<T>(W);
+    cudaFuncSetAttribute(k_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaFuncSetAttribute(k_bwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    done_w = W;
 }
 
 void launch_forward_solve(const DevProblem &P, const DevBatch &B, int nrhs, bool mixed, const double2 *rin,
                           cudaStream_t st) {
     int nitems = B.nsys * nrhs;
     int grid = (nitems + kSolveWarps - 1) / kSolveWarps;
-    size_t W = P.mb + 1;
-    if (mixed) k_fwd<float2><<<grid, kSolveWarps * 32, kSolveWarps * W * sizeof(float2), st>>>(P, B, nrhs, rin);
-    else k_fwd<double2><<<grid, kSolveWarps * 32, kSolveWarps * W * sizeof(double2), st>>>(P, B, nrhs, rin);
+    int W = P.mb + 1;
+    if (mixed) {
+        set_solve_smem<float2>(W);
+        k_fwd<float2><<<grid, kSolveWarps * 32, kSolveWarps * solve_smem_per_warp<float2>(W), st>>>(P, B, nrhs, rin);
+    } else {
+        set_solve_smem<double2>(W);
+        k_fwd<double2><<<grid, kSolveWarps * 32, kSolveWarps * solve_smem_per_warp<double2>(W), st>>>(P, B, nrhs, rin);
+    }
 }
 
 void launch_back_solve(const DevProblem &P, const DevBatch &B, int nrhs, bool mixed, cudaStream_t st) {
     int nitems = B.nsys * nrhs;
     int grid = (nitems + kSolveWarps - 1) / kSolveWarps;
-    size_t W = P.mb + 1;
-    if (mixed) k_bwd<float2><<<grid, kSolveWarps * 32, kSolveWarps * W * sizeof(float2), st>>>(P, B, nrhs);
-    else k_bwd<double2><<<grid, kSolveWarps * 32, kSolveWarps * W * sizeof(double2), st>>>(P, B, nrhs);
+    int W = P.mb + 1;
+    if (mixed) {
+        set_solve_smem<float2>(W);
+        k_bwd<float2><<<grid, kSolveWarps * 32, kSolveWarps * solve_smem_per_warp<float2>(W), st>>>(P, B, nrhs);
+    } else {
+        set_solve_smem<double2>(W);
+        k_bwd<double2><<<grid, kSolveWarps * 32, kSolveWarps * solve_smem_per_warp<double2>(W), st>>>(P, B, nrhs);
+    }
 }
 
 // r = b - A x with the full symmetric pattern (FP64)
@@ -184,6 +294,12 @@ __global__ void k_accumulate(DevProblem P, DevBatch B, int nrhs, int first, doub
         mz = fmax(mz, red[0][0]);
         mx = fmax(mx, red[1][0]);
         if (!first && B.active && !(mz > tol * mx)) B.active[item] = 0;
+        if (B.active && B.active[item] && B.nactive) atomicAdd(B.nactive, 1);
+        if (B.zmax && mx > 0.0) {
+            // relative corrections are non-negative: compare their bit patterns
+            unsigned long long rel = (unsigned long long)__double_as_longlong(mz / mx);
+            atomicMax((unsigned long long *)B.zmax, rel);
+        }
         if (!isfinite(mz) || !isfinite(mx)) {
             atomicCAS(&B.status[item / nrhs], 0, 28);
             if (B.active) B.active[item] = 0;

@@ -1,0 +1,53 @@
+"""Run one forward (and optionally the Jacobian) of a synthetic configuration.
+
+A small driver for profilers (ncu) and quick timing:
+
+    python -m titatest_gb300.profile_case --config 2 --precision mixed \
+        --batch 152 --repeat 1 [--sens]
+
+--batch limits the number of band systems per batch (one factor launch per
+batch), so a profiler can capture a single launch of known size.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+import numpy as np
+
+from . import MIXED, PLAIN, CRMod, synth
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--config", type=int, default=2)
+    ap.add_argument("--precision", choices=["mixed", "plain"], default="mixed")
+    ap.add_argument("--batch", type=int, default=0, help="systems per batch (0: as many as fit)")
+    ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--sens", action="store_true")
+    ap.add_argument("--refine-tol", type=float, default=1e-8)
+    a = ap.parse_args(argv)
+    s = synth.make(a.config)
+    prec = MIXED if a.precision == "mixed" else PLAIN
+    with CRMod(s.grid, s.survey, precision=prec) as m:
+        m.set_refinement(8, a.refine_tol)
+        if a.batch:
+            g = s.grid
+            esz = 8 if prec == MIXED else 16
+            per = g.sanz * (g.mb + 1) * esz + (g.sanz * 12 * 16) + g.sanz * 8 + g.sanz * (3 * 16 + esz) + 64
+            m.set_memory_budget(int(per * a.batch + per // 2))
+        for _ in range(a.repeat):
+            t = time.time()
+            out = m.forward(s.sigma)
+            st = m.stats()
+            msg = f"forward {1e3 * (time.time() - t):.1f} ms, batches {st['nbatches']}, factor {st['ms_factor']:.1f} ms, " \
+                  f"solve {st['ms_solve']:.1f} ms, refinement {st['refine_iterations']}"
+            if a.sens:
+                J = m.sens(0)
+                msg += f", sens {m.stats()['ms_sens']:.1f} ms, |J|max {np.abs(J).max():.3e}"
+            print(msg, flush=True)
+        assert np.all(np.isfinite(out["volt"]))
+
+
+if __name__ == "__main__":
+    main()
