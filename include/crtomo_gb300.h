@@ -138,6 +138,21 @@ int crgpu_device_buffers(crgpu_ctx *ctx, void **kpot_device, void **hpot_device)
 int crgpu_factor_system(crgpu_ctx *ctx, const double *sigma, int32_t k, int32_t l,
                         double *a, double *fak);
 
+/* No counterpart in the reference.  The same band factor and fak as
+ * crgpu_factor_system (plain precision contexts only), for callers that
+ * cannot allocate device memory when they call: code running while a CUDA
+ * graph is captured, or inside a framework that owns all device memory.
+ * sigma_device (elanz complex), a_device (sanz*(mb+1) complex) and
+ * fak_device (sanz) are caller-owned device buffers; stream may be NULL (the
+ * context's stream).  The call allocates nothing: its scratch is one fixed
+ * 8 MiB device array in the library (held on every GPU that loads it until
+ * exit); systems needing more (16 + 32*(nnz + sanz) bytes) are rejected with
+ * an error.  The first call on a device looks the array up and should come
+ * before any stream capture.  Calls share the array: calls that overlap on
+ * the GPU race. */
+int crgpu_factor_system_noalloc(crgpu_ctx *ctx, const void *sigma_device, int32_t k, int32_t l,
+                                void *a_device, void *fak_device, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* inversion update                                                     */
 /* ------------------------------------------------------------------ */

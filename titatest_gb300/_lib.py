@@ -28,7 +28,7 @@ EXPORTS = (
     "crgpu_create", "crgpu_destroy", "crgpu_last_error", "crgpu_set_refinement", "crgpu_set_stream",
     "crgpu_set_memory_budget", "crgpu_forward", "crgpu_forward_device", "crgpu_sens",
     "crgpu_sens_device", "crgpu_device_buffers", "crgpu_factor_system", "crgpu_update",
-    "crgpu_rwaven", "crgpu_cutmck", "crgpu_bkfak", "crgpu_get_stats",
+    "crgpu_rwaven", "crgpu_cutmck", "crgpu_bkfak", "crgpu_get_stats", "crgpu_factor_system_noalloc",
 )
 
 

@@ -9,43 +9,9 @@
 #include <string>
 #include <vector>
 
-#include "crgpu_internal.h"
-#include "kernels.h"
+#include "ctx.h"
 
 using namespace crgpu;
-
-struct crgpu_ctx {
-    HostGrid hg;
-    Pattern pat;
-    DevProblem P{};
-    int precision = CRGPU_PLAIN;
-    int eanz = 0, nanz = 0, K = 0;
-    int swrtr = 1, lsr = 0, lsink = 0, nsink = -1, lsytop = 0;
-    cudaStream_t st = nullptr, own_st = nullptr;
-    int nsm = 0;
-    std::vector<void *> allocs;
-    // device state
-    double2 *d_sigma = nullptr, *d_adom = nullptr, *d_kpot = nullptr, *d_hpot = nullptr;
-    double2 *d_volt = nullptr, *d_sigmaa = nullptr, *d_sens = nullptr;
-    double *d_kfak = nullptr;
-    int *d_err = nullptr;
-    // batch buffers
-    int batch_cap = 0, nrhs = 1;
-    DevBatch Bmax{};
-    int32_t *d_ks = nullptr, *d_ls = nullptr;
-    std::vector<int32_t> sys_k, sys_l;
-    // options
-    int refine_maxit = 8;
-    double refine_tol = 1e-10;
-    double last_refine_zmax = 0.0;
-    int64_t mem_budget = 0;
-    bool have_forward = false;
-    std::string last_error;
-    crgpu_stats stats{};
-    // update work space
-    void *d_upd = nullptr;
-    size_t upd_bytes = 0;
-};
 
 namespace {
 
@@ -334,6 +300,7 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
     }
     int dev = 0;
     cudaGetDevice(&dev);
+    c->device = dev;
     cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev);
     // device problem
     DevProblem &P = c->P;
