@@ -140,3 +140,37 @@ def test_zero_conductivity_raises_reference_error(gpu_lib):
         assert ei.value.errnr == 27
         out = m.forward(sig)  # context still usable
         assert np.all(np.isfinite(out["volt"]))
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_singularity_removal_matches_oracle(gpu_lib, cfg1, prec):
+    """mswitch bit 2: src/refsig.f90 + src/potana.f90 + the lsr branch of
+    src/kompab.f90 and kpot += pota (src/fem.f90:390-391)."""
+    from titatest_gb300 import CRMod
+    s, kwn, kwnwi, *_ = cfg1
+    P = O.Problem(s.grid, s.survey)
+    kp = P.forward(s.sigma, kwn, kwnwi, lsr=True)
+    hp = P.rtrafo(kp, kwnwi)
+    volt, _ = P.bvolt(hp, 0, None)
+    with CRMod(s.grid, s.survey, kwn, kwnwi, precision=prec, lsr=True) as m:
+        out = m.forward(s.sigma, kpot=True)
+    tol = PLAIN_TOL if prec == 0 else MIXED_VOLT_TOL
+    assert relerr(out["kpot"], kp) < (PLAIN_TOL if prec == 0 else 1e-6)
+    assert relerr(out["volt"], volt) < tol
+
+
+def test_singularity_removal_homogeneous_is_analytic(gpu_lib):
+    """With a homogeneous model sigma - sigma0 = 0, the removal right-hand side
+    vanishes and kpot is the analytic half-space field of src/potana.f90."""
+    from titatest_gb300 import PLAIN, CRMod
+    g, sv, sig, cfg, _ = load_case("minimal")
+    sig = np.full_like(sig, 0.01 + 0.001j)
+    P = O.Problem(g, sv)
+    kwn, kwnwi = P.rwaven()
+    with CRMod(g, sv, kwn, kwnwi, precision=PLAIN, lsr=True) as m:
+        out = m.forward(sig, kpot=True)
+    s0 = P.refsig(sig)
+    for k in (0, len(kwn) - 1):
+        for l in (1, sv.eanz):
+            pa = P.potana(l, kwn[k], s0)
+            assert relerr(out["kpot"][k, l - 1], pa) < 1e-12

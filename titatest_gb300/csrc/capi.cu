@@ -53,7 +53,8 @@ int upload(crgpu_ctx *c, const T **dst, const std::vector<T> &v) {
 
 void free_batch(crgpu_ctx *c) {
     void *ptrs[] = {c->Bmax.As, c->Bmax.fak, c->Bmax.b, c->Bmax.x, c->Bmax.r, c->Bmax.L, c->Bmax.y,
-                    c->Bmax.status, c->Bmax.active, (void *)c->Bmax.nactive, c->d_ks, c->d_ls};
+                    c->Bmax.status, c->Bmax.active, (void *)c->Bmax.nactive, c->Bmax.pota,
+                    c->Bmax.potmax, c->d_ks, c->d_ls};
     for (void *p : ptrs)
         if (p) {
             cudaFree(p);
@@ -96,6 +97,10 @@ int ensure_batch(crgpu_ctx *c, int want) {
     }
     e = e ? e : dalloc(c, &c->d_ks, (size_t)want);
     e = e ? e : dalloc(c, &c->d_ls, (size_t)want);
+    if (!e && c->lsr) {
+        e = dalloc(c, &B.pota, (size_t)want * n);
+        e = e ? e : dalloc(c, &B.potmax, (size_t)want);
+    }
     if (e) return e;
     B.L = L;
     B.y = y;
@@ -130,6 +135,10 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
     CUCHECK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
     launch_adom(P, d_sigma, c->d_adom, c->st);
     c->stats.kernel_launches += 1;
+    if (c->lsr) {
+        launch_refsig(P, d_sigma, c->d_sigma0, c->st);
+        c->stats.kernel_launches += 1;
+    }
     const bool mixed = c->precision == CRGPU_MIXED;
     const int nsys_total = (int)c->sys_k.size();
     // batch size from the memory budget
@@ -163,8 +172,13 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
         const int nr = c->nrhs;
         const int fuse = nr == 1 ? 1 : 0;
         launch_assemble(P, B, d_sigma, c->d_adom, c->st);
-        launch_rhs(P, B, nr, c->lsink, c->nsink, c->st);
-        c->stats.kernel_launches += 3;
+        if (c->lsr) {
+            launch_pota_rhs(P, B, d_sigma, c->d_sigma0, c->lsink, c->nsink, c->st);
+            c->stats.kernel_launches += 5;
+        } else {
+            launch_rhs(P, B, nr, c->lsink, c->nsink, c->st);
+            c->stats.kernel_launches += 3;
+        }
         cudaEventRecord(f0, c->st);
         if (mixed) {
             e = launch_factor_mixed(P, B, fuse, c->nsm, c->st);
@@ -274,10 +288,6 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
         e = ERR_ARG;
         c->last_error = "precision";
     }
-    if (!e && sv->lsr) {
-        e = ERR_UNSUPPORTED;
-        c->last_error = "singularity removal (mswitch bit 2) is not supported";
-    }
     if (!e) e = build_pattern(c->hg, c->pat, c->last_error);
     if (e) {
         *out = c;  // keep the message available
@@ -291,6 +301,8 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
     c->lsink = sv->lsink;
     c->nsink = sv->lsink ? sv->nsink - 1 : -1;
     c->lsytop = sv->lsytop;
+    // src/fem.f90:311 (no mixed boundaries: no singularity removal) and 2D
+    c->lsr = (sv->lsr && c->hg.lbeta && sv->swrtr != 0) ? 1 : 0;
     cudaError_t ce = cudaStreamCreateWithFlags(&c->own_st, cudaStreamNonBlocking);
     c->st = c->own_st;
     if (ce != cudaSuccess) {
@@ -317,6 +329,7 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
     P.nnz_full = c->pat.nnz_full;
     P.rw = c->pat.rw;
     P.swrtr = c->swrtr;
+    P.lsr = c->lsr;
     P.sytop = sv->lsytop ? host_sytop(grid) : 0.0;
     std::vector<int32_t> enr0(c->eanz), meas((size_t)c->nanz * 4);
     for (int i = 0; i < c->eanz; i++) {
@@ -366,6 +379,23 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
     if (!e) e = upload(c, &P.strom, strom);
     if (!e) e = upload(c, &P.kwn, kwn);
     if (!e) e = upload(c, &P.kwnwi, kwnwi);
+    {
+        // element areas as src/refsig.f90:38-62 computes them
+        std::vector<double> area(hg.elanz, 0.0);
+        for (int q = 0; q < hg.elanz; q++) {
+            const int *nd = &hg.enodes[(size_t)q * 4];
+            double xk = hg.x[nd[0]], yk = hg.y[nd[0]];
+            double ax = hg.x[nd[1]] - xk, ay = hg.y[nd[1]] - yk, bx = hg.x[nd[2]] - xk, by = hg.y[nd[2]] - yk;
+            if (hg.etype[q] == 3) {
+                area[q] = std::fabs(ax * by - ay * bx) / 2.0;
+            } else {
+                double cx = hg.x[nd[3]] - xk, cy = hg.y[nd[3]] - yk;
+                area[q] = (std::fabs(ax * by - ay * bx) + std::fabs(bx * cy - by * cx)) / 2.0;
+            }
+        }
+        if (!e) e = upload(c, &P.earea, area);
+    }
+    if (!e) e = dalloc(c, &c->d_sigma0, 1);
     if (!e) e = dalloc(c, &P.elbg, (size_t)c->K * hg.elanz * 10);
     if (!e) e = dalloc(c, &P.relbg, (size_t)std::max(hg.relanz, 1) * 3);
     if (!e) e = dalloc(c, &P.kg, (size_t)c->K * c->eanz * std::max(hg.relanz, 1));
@@ -483,6 +513,7 @@ int crgpu_sens_device(crgpu_ctx *c, int32_t mode, void *sens_device) {
     cudaEventRecord(a, c->st);
     launch_bsens(c->P, c->d_kpot, c->d_sigma, c->d_volt, mode, c->precision == CRGPU_MIXED,
                  (double2 *)sens_device, c->st);
+    c->last_sens = (const double2 *)sens_device;
     cudaEventRecord(b, c->st);
     c->stats.kernel_launches += 1;
     CUCHECK(c, cudaStreamSynchronize(c->st));
@@ -504,6 +535,7 @@ int crgpu_sens(crgpu_ctx *c, int32_t mode, double *sens) {
     }
     int e = crgpu_sens_device(c, mode, c->d_sens);
     if (e) return e;
+    c->last_sens = c->d_sens;
     CUCHECK(c, cudaMemcpyAsync(sens, c->d_sens, cnt * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
     CUCHECK(c, cudaStreamSynchronize(c->st));
     return 0;
@@ -624,9 +656,90 @@ int crgpu_update(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, const 
                  int32_t ltri, const double *smatm, int32_t nx, const int32_t *nachbar, double lam, double eps,
                  int32_t ncgmax, double step, double *par, double *dpar, double *cgfac, float *cgres,
                  int32_t *ncg) {
-    (void)wmatd; (void)wdfak; (void)dat; (void)sigmaa; (void)ltri; (void)smatm; (void)nx; (void)nachbar;
-    (void)lam; (void)eps; (void)ncgmax; (void)step; (void)par; (void)dpar; (void)cgfac; (void)cgres; (void)ncg;
-    return fail(c, ERR_UNSUPPORTED, "crgpu_update: not built yet");
+    if (!c || !wmatd || !wdfak || !dat || !sigmaa || !smatm || !par || !dpar || !cgfac || !cgres || !ncg ||
+        ncgmax < 1)
+        return ERR_ARG;
+    if (!c->last_sens) return fail(c, ERR_ARG, "crgpu_update needs the sensitivities (crgpu_sens mode 1) first");
+    if (ltri != 0 && ltri != 1 && ltri != 2)
+        return fail(c, ERR_UNSUPPORTED, "crgpu_update: regularisation types 0, 1 and 2 only");
+    if (ltri != 0 && !nachbar) return ERR_ARG;
+    const int nanz = c->nanz, manz = c->hg.elanz;
+    int maxnk = 0;
+    for (int e = 0; e < manz; e++) maxnk = std::max(maxnk, c->hg.etype[e] == 3 ? 3 : 4);
+    if (ltri == 0 && (nx <= 0 || manz % nx != 0)) return fail(c, ERR_ARG, "nx must divide manz");
+    const int ncol = ltri == 0 ? 3 : maxnk + 1;
+    // device layout of the inputs and outputs, then the CG work space
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off += (bytes + 255) & ~(size_t)255;
+        return o;
+    };
+    const size_t o_w = take(sizeof(double) * nanz), o_wd = take(sizeof(int32_t) * nanz);
+    const size_t o_dat = take(sizeof(double2) * nanz), o_sa = take(sizeof(double2) * nanz);
+    const size_t o_sm = take(sizeof(double) * (size_t)manz * ncol);
+    const size_t o_nb = take(sizeof(int32_t) * (size_t)manz * (maxnk + 1));
+    const size_t o_par = take(sizeof(double2) * manz), o_dpar = take(sizeof(double2) * manz);
+    const size_t o_cg = take(sizeof(double) * manz);
+    const size_t o_work = take(update_work_bytes(nanz, manz));
+    if (c->upd_bytes < off) {
+        if (c->d_upd) cudaFree(c->d_upd);
+        c->d_upd = nullptr;
+        c->upd_bytes = 0;
+        cudaError_t e = cudaMalloc(&c->d_upd, off);
+        if (e != cudaSuccess) return fail(c, 94, std::string("update work space: ") + cudaGetErrorString(e));
+        c->upd_bytes = off;
+    }
+    char *base = (char *)c->d_upd;
+    CUCHECK(c, cudaMemcpyAsync(base + o_w, wmatd, sizeof(double) * nanz, cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemcpyAsync(base + o_wd, wdfak, sizeof(int32_t) * nanz, cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemcpyAsync(base + o_dat, dat, sizeof(double2) * nanz, cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemcpyAsync(base + o_sa, sigmaa, sizeof(double2) * nanz, cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemcpyAsync(base + o_sm, smatm, sizeof(double) * (size_t)manz * ncol, cudaMemcpyHostToDevice, c->st));
+    if (ltri != 0)
+        CUCHECK(c, cudaMemcpyAsync(base + o_nb, nachbar, sizeof(int32_t) * (size_t)manz * (maxnk + 1),
+                                   cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemcpyAsync(base + o_par, par, sizeof(double2) * manz, cudaMemcpyHostToDevice, c->st));
+    CGArgs a{};
+    a.nanz = nanz;
+    a.manz = manz;
+    a.ltri = ltri;
+    a.nx = nx;
+    a.maxnk = maxnk;
+    a.ncgmax = ncgmax;
+    a.lam = lam;
+    a.eps = eps;
+    a.step = step;
+    a.sens = c->last_sens;
+    a.wmatd = (const double *)(base + o_w);
+    a.wdfak = (const int32_t *)(base + o_wd);
+    a.dat = (const double2 *)(base + o_dat);
+    a.sigmaa = (const double2 *)(base + o_sa);
+    a.smatm = (const double *)(base + o_sm);
+    a.nachbar = (const int32_t *)(base + o_nb);
+    a.par = (double2 *)(base + o_par);
+    a.dpar = (double2 *)(base + o_dpar);
+    a.cgfac = (double *)(base + o_cg);
+    a.work = (double2 *)(base + o_work);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, c->st);
+    int n_cg = 0;
+    int rc = run_update(a, c->st, &n_cg, cgres);
+    cudaEventRecord(e1, c->st);
+    if (rc) return fail(c, rc, "update kernels failed");
+    CUCHECK(c, cudaMemcpyAsync(par, a.par, sizeof(double2) * manz, cudaMemcpyDeviceToHost, c->st));
+    CUCHECK(c, cudaMemcpyAsync(dpar, a.dpar, sizeof(double2) * manz, cudaMemcpyDeviceToHost, c->st));
+    CUCHECK(c, cudaMemcpyAsync(cgfac, a.cgfac, sizeof(double) * manz, cudaMemcpyDeviceToHost, c->st));
+    CUCHECK(c, cudaStreamSynchronize(c->st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    c->stats.ms_update = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ncg = n_cg;
+    return 0;
 }
 
 }  // extern "C"

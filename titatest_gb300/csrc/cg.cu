@@ -1,0 +1,276 @@
+// Model update of the Gauss-Newton step: src/update.f90:27-353 with the
+// complex preconditioned CG of src/cg_mod.f90:426-726 (cjggra, bap, bp,
+// bptri, bb).  The Jacobian is column-major (nanz, manz): column j is
+// contiguous, so the column reductions (preconditioner, right-hand side,
+// J^H W (J p)) read coalesced columns, and J p is formed from column chunks
+// with fixed-order partial sums (deterministic, no atomics).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "crgpu_internal.h"
+#include "kernels.h"
+
+namespace crgpu {
+
+namespace {
+
+constexpr int kRowTile = 256;   // rows of J per block in J p
+constexpr int kColChunk = 64;   // columns of J per block in J p
+constexpr int kRedThreads = 256;
+
+// R v (optionally R (w o v)): structured 5-point stencil (ltri 0,
+// src/cg_mod.f90:547-577 / src/update.f90:63-91) or the neighbour stencil
+// (ltri 1, 2: src/cg_mod.f90:579-613 / src/update.f90:99-120)
+__global__ void k_rmul(CGArgs a, const double2 *__restrict__ v, const double *__restrict__ w,
+                       double2 *__restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int manz = a.manz;
+    if (i >= manz) return;
+    auto wv = [&](int j) -> double2 {
+        double2 x = v[j];
+        if (w) {
+            double f = w[j];
+            return cz(x.x * f, x.y * f);
+        }
+        return x;
+    };
+    double2 c = cz(0.0, 0.0);
+    if (a.ltri == 0) {
+        const double *sm1 = a.smatm, *sm2 = a.smatm + manz, *sm3 = a.smatm + 2 * (size_t)manz;
+        const int nx = a.nx;
+        if (i > 0) c = cscale(wv(i - 1), sm2[i - 1]);
+        if (i < manz - 1) c = cadd(c, cscale(wv(i + 1), sm2[i]));
+        if (i >= nx) c = cadd(c, cscale(wv(i - nx), sm3[i - nx]));
+        if (i < manz - nx) c = cadd(c, cscale(wv(i + nx), sm3[i]));
+        out[i] = cadd(c, cscale(wv(i), sm1[i]));
+    } else {
+        for (int q = 0; q < a.maxnk; q++) {
+            int nb = a.nachbar[(size_t)q * manz + i];
+            if (nb != 0) c = cadd(c, cscale(wv(nb - 1), a.smatm[(size_t)q * manz + i]));
+        }
+        out[i] = cadd(c, cscale(wv(i), a.smatm[(size_t)a.maxnk * manz + i]));
+    }
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// One block per column j: g_j = sum_i conj(s_ij) w_i vec_i and (mode 0)
+// diag_j = sum_i |s_ij|^2 w_i (w_i = wmatd_i * wdfak_i).
+// mode 0 (update.f90 RHS): cgfac_j = 1/sqrt(diag_j + lam R_jj),
+//                          out_j = (g_j - lam rm_j) cgfac_j
+// mode 1 (cg_mod.f90 bb):  out_j = (g_j + lam rm_j) cgfac_j
+__global__ __launch_bounds__(kRedThreads) void k_colred(CGArgs a, int mode, const double2 *__restrict__ vec,
+                                                        const double2 *rm, double *cgfac,
+                                                        double2 *out) {  // out may alias rm
+    const int j = blockIdx.x;
+    const double2 *col = a.sens + (size_t)j * a.nanz;
+    double gr = 0.0, gi = 0.0, dg = 0.0;
+    for (int i = threadIdx.x; i < a.nanz; i += kRedThreads) {
+        const double2 s = col[i];
+        const double w = a.wmatd[i] * (double)a.wdfak[i];
+        if (mode == 0) dg = fma(s.x * s.x + s.y * s.y, w, dg);
+        const double2 v = vec[i];
+        // conj(s) * (w v)
+        const double vx = w * v.x, vy = w * v.y;
+        gr = fma(s.x, vx, gr);
+        gr = fma(s.y, vy, gr);
+        gi = fma(s.x, vy, gi);
+        gi = fma(-s.y, vx, gi);
+    }
+    __shared__ double red[3][kRedThreads / 32];
+    gr = warp_sum(gr);
+    gi = warp_sum(gi);
+    dg = warp_sum(dg);
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    if (lane == 0) {
+        red[0][wl] = gr;
+        red[1][wl] = gi;
+        red[2][wl] = dg;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        gr = gi = dg = 0.0;
+        for (int q = 0; q < kRedThreads / 32; q++) {
+            gr += red[0][q];
+            gi += red[1][q];
+            dg += red[2][q];
+        }
+        double diagR = a.ltri == 0 ? a.smatm[j] : a.smatm[(size_t)a.maxnk * a.manz + j];
+        double cf;
+        if (mode == 0) {
+            cf = 1.0 / sqrt(dg + a.lam * diagR);
+            cgfac[j] = cf;
+            out[j] = cz((gr - a.lam * rm[j].x) * cf, (gi - a.lam * rm[j].y) * cf);
+        } else {
+            cf = cgfac[j];
+            out[j] = cz((gr + a.lam * rm[j].x) * cf, (gi + a.lam * rm[j].y) * cf);
+        }
+    }
+}
+
+// partial[chunk][i] = sum_{j in chunk} s_ij (cgfac_j p_j)   (src/cg_mod.f90:520-545)
+__global__ __launch_bounds__(kRowTile) void k_jp_partial(CGArgs a, const double2 *__restrict__ p,
+                                                         double2 *__restrict__ partial) {
+    __shared__ double2 q[kColChunk];
+    const int i = blockIdx.x * kRowTile + threadIdx.x;
+    const int j0 = blockIdx.y * kColChunk;
+    const int j1 = min(j0 + kColChunk, a.manz);
+    for (int t = threadIdx.x; t < j1 - j0; t += kRowTile) {
+        double2 v = p[j0 + t];
+        double f = a.cgfac[j0 + t];
+        q[t] = cz(v.x * f, v.y * f);
+    }
+    __syncthreads();
+    if (i >= a.nanz) return;
+    double ar = 0.0, ai = 0.0;
+    for (int j = j0; j < j1; j++) {
+        const double2 s = a.sens[(size_t)j * a.nanz + i];
+        const double2 v = q[j - j0];
+        ar = fma(s.x, v.x, ar);
+        ar = fma(-s.y, v.y, ar);
+        ai = fma(s.x, v.y, ai);
+        ai = fma(s.y, v.x, ai);
+    }
+    partial[(size_t)blockIdx.y * a.nanz + i] = cz(ar, ai);
+}
+
+__global__ void k_jp_reduce(CGArgs a, int nchunk, const double2 *__restrict__ partial, double2 *__restrict__ ap) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nanz) return;
+    double2 s = cz(0.0, 0.0);
+    for (int c = 0; c < nchunk; c++) s = cadd(s, partial[(size_t)c * a.nanz + i]);
+    ap[i] = s;
+}
+
+// block partial sums of Re(conj(x) y) (x == y: |x|^2), then a second pass
+__global__ __launch_bounds__(kRedThreads) void k_dot_partial(int n, const double2 *__restrict__ x,
+                                                             const double2 *__restrict__ y, double *part) {
+    double s = 0.0;
+    for (int i = blockIdx.x * kRedThreads + threadIdx.x; i < n; i += gridDim.x * kRedThreads) {
+        double2 a = x[i], b = y[i];
+        s = fma(a.x, b.x, s);
+        s = fma(a.y, b.y, s);
+    }
+    __shared__ double red[kRedThreads / 32];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < kRedThreads / 32; q++) t += red[q];
+        part[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_dot_final(int nb, const double *part, double *out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < nb; q++) t += part[q];
+        *out = t;
+    }
+}
+
+// x = y + c z   (elementwise, complex with real c)
+__global__ void k_axpy(int n, double2 *x, const double2 *y, double c, const double2 *z) {  // x may alias y or z
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double2 a = y[i], b = z[i];
+    x[i] = cz(a.x + c * b.x, a.y + c * b.y);
+}
+
+// d = (y - f) for the right-hand side, dpar = 0, ...
+__global__ void k_sub(int n, const double2 *__restrict__ a, const double2 *__restrict__ b, double2 *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = csub(a[i], b[i]);
+}
+
+__global__ void k_final(int n, double2 *dpar, const double *__restrict__ cgfac, double step, double2 *par) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double2 d = dpar[i];
+    double f = cgfac[i];
+    d = cz(d.x * f, d.y * f);
+    dpar[i] = d;
+    double2 p = par[i];
+    par[i] = cz(p.x + step * d.x, p.y + step * d.y);
+}
+
+inline unsigned nblk(int n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+// work layout (double2 units): bvec, rvec, pvec, dpar(out) | ap, dmf (nanz) |
+// partial (nchunk * nanz) | scalars
+size_t update_work_bytes(int nanz, int manz) {
+    int nchunk = (manz + kColChunk - 1) / kColChunk;
+    return sizeof(double2) * ((size_t)3 * manz + 2 * (size_t)nanz + (size_t)nchunk * nanz) + sizeof(double) * 1024;
+}
+
+int run_update(const CGArgs &a, cudaStream_t st, int *ncg_out, float *cgres_host) {
+    const int manz = a.manz, nanz = a.nanz;
+    const int nchunk = (manz + kColChunk - 1) / kColChunk;
+    double2 *bvec = a.work, *rvec = bvec + manz, *pvec = rvec + manz;
+    double2 *ap = pvec + manz, *dmf = ap + nanz, *partial = dmf + nanz;
+    double *scal = (double *)(partial + (size_t)nchunk * nanz);
+    double *dots = scal;          // [0]: result
+    double *dpart = scal + 8;     // block partials
+    const int nbm = 120;
+    auto dot = [&](const double2 *x, const double2 *y) -> double {
+        k_dot_partial<<<nbm, kRedThreads, 0, st>>>(manz, x, y, dpart);
+        k_dot_final<<<1, 32, 0, st>>>(nbm, dpart, dots);
+        double h = 0.0;
+        cudaMemcpyAsync(&h, dots, sizeof(double), cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        return h;
+    };
+    const int T = 256;
+    // bvec = R m ; right-hand side and preconditioner
+    k_rmul<<<nblk(manz, T), T, 0, st>>>(a, a.par, nullptr, bvec);
+    k_sub<<<nblk(nanz, T), T, 0, st>>>(nanz, a.dat, a.sigmaa, dmf);
+    k_colred<<<manz, kRedThreads, 0, st>>>(a, 0, dmf, bvec, a.cgfac, bvec);
+    // cjggra
+    cudaMemsetAsync(a.dpar, 0, sizeof(double2) * manz, st);
+    cudaMemcpyAsync(rvec, bvec, sizeof(double2) * manz, cudaMemcpyDeviceToDevice, st);
+    cudaMemsetAsync(pvec, 0, sizeof(double2) * manz, st);
+    std::vector<float> cgres(a.ncgmax + 2, 0.f);
+    double dr = 0, dr0 = 0, dr1 = 0, beta = 0;
+    int ncg = a.ncgmax, k;
+    for (k = 1; k <= a.ncgmax; k++) {
+        ncg = k - 1;
+        dr = dot(rvec, rvec);
+        if (k == 1) {
+            dr0 = dr * a.eps;
+            beta = 0.0;
+        } else {
+            if (dr <= dr0) break;
+            beta = dr / dr1;
+        }
+        k_axpy<<<nblk(manz, T), T, 0, st>>>(manz, pvec, rvec, beta, pvec);
+        dim3 g1(nblk(nanz, kRowTile), nchunk);
+        k_jp_partial<<<g1, kRowTile, 0, st>>>(a, pvec, partial);
+        k_jp_reduce<<<nblk(nanz, T), T, 0, st>>>(a, nchunk, partial, ap);
+        k_rmul<<<nblk(manz, T), T, 0, st>>>(a, pvec, a.cgfac, bvec);
+        k_colred<<<manz, kRedThreads, 0, st>>>(a, 1, ap, bvec, a.cgfac, bvec);
+        dr1 = dot(pvec, bvec);
+        const double alpha = dr / dr1;
+        k_axpy<<<nblk(manz, T), T, 0, st>>>(manz, a.dpar, a.dpar, alpha, pvec);
+        k_axpy<<<nblk(manz, T), T, 0, st>>>(manz, rvec, rvec, -alpha, bvec);
+        dr1 = dr;
+        cgres[k] = (float)(a.eps * dr / dr0);
+    }
+    if (k > a.ncgmax) ncg = a.ncgmax;
+    cgres[0] = (float)ncg;
+    k_final<<<nblk(manz, T), T, 0, st>>>(manz, a.dpar, a.cgfac, a.step, a.par);
+    for (size_t q = 0; q < cgres.size(); q++) cgres_host[q] = cgres[q];
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    *ncg_out = ncg;
+    return e == cudaSuccess ? 0 : ERR_CUDA;
+}
+
+}  // namespace crgpu

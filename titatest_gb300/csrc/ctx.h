@@ -23,6 +23,7 @@ struct crgpu_ctx {
     double2 *d_sigma = nullptr, *d_adom = nullptr, *d_kpot = nullptr, *d_hpot = nullptr;
     double2 *d_volt = nullptr, *d_sigmaa = nullptr, *d_sens = nullptr;
     double *d_kfak = nullptr;
+    double2 *d_sigma0 = nullptr;  // reference conductivity (singularity removal)
     int *d_err = nullptr;
     // batch buffers
     int batch_cap = 0, nrhs = 1;
@@ -37,8 +38,9 @@ struct crgpu_ctx {
     bool have_forward = false;
     std::string last_error;
     crgpu_stats stats{};
-    // update work space
+    // update work space and the sensitivities it uses
     void *d_upd = nullptr;
     size_t upd_bytes = 0;
+    const double2 *last_sens = nullptr;
 };
 

@@ -11,7 +11,9 @@ struct DevProblem {
     int n, mb, W, elanz, relanz, eanz, nanz, K, nnz, nnz_full;
     int rw;               // padded row width of the lower pattern (row i at i*rw)
     int swrtr;
+    int lsr;              // singularity removal
     double sytop;
+    const double *earea;  // elanz: element areas of src/refsig.f90
     // grid (node order, 0-based)
     const double *x, *y;
     const int32_t *etype, *enodes;          // elanz, elanz*4
@@ -48,6 +50,8 @@ struct DevBatch {
     int *active;      // [nsys]        refinement still running
     int *nactive;     // count of items still refining after the last correction
     double *zmax;     // largest relative correction of the last refinement step
+    double2 *pota;    // [nsys][n] analytic potentials (singularity removal)
+    double *potmax;   // [nsys]
 };
 
 }  // namespace crgpu

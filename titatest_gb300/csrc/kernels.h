@@ -16,6 +16,11 @@ void launch_assemble(const DevProblem &P, const DevBatch &B, const double2 *sigm
 void launch_rhs(const DevProblem &P, const DevBatch &B, int nrhs, int lsink, int nsink,
                 cudaStream_t st);
 
+// singularity removal (src/refsig.f90, src/potana.f90, kompab lsr branch)
+void launch_refsig(const DevProblem &P, const double2 *sigma, double2 *sigma0, cudaStream_t st);
+void launch_pota_rhs(const DevProblem &P, const DevBatch &B, const double2 *sigma, const double2 *sigma0,
+                     int lsink, int nsink, cudaStream_t st);
+
 // factorisation (src/chol.f90) with fused forward substitution when fuse != 0
 void launch_factor_plain(const DevProblem &P, const DevBatch &B, int fuse, int nsm,
                          cudaStream_t st);
@@ -45,7 +50,7 @@ void launch_bvolt(const DevProblem &P, const double2 *hpot, int mode, const doub
 void launch_bsens(const DevProblem &P, const double2 *kpot, const double2 *sigma,
                   const double2 *volt, int mode, bool single, double2 *sens, cudaStream_t st);
 
-// update / CG (src/update.f90, src/cg_mod.f90)
+// update / CG (src/update.f90, src/cg_mod.f90); all pointers device memory
 struct CGArgs {
     int nanz, manz, ltri, nx, maxnk, ncgmax;
     double lam, eps, step;
@@ -55,13 +60,12 @@ struct CGArgs {
     const double2 *dat, *sigmaa;
     const double *smatm;    // column-major (manz, 3) or (manz, maxnk+1)
     const int32_t *nachbar; // column-major (manz, maxnk+1)
-    double2 *par, *dpar;
-    double *cgfac;
-    float *cgres;           // ncgmax+2
-    double2 *work;          // 4*manz + nanz + partials
-    double *scal;           // scalars
-    int nblocks;
+    double2 *par, *dpar;    // in/out model, out update
+    double *cgfac;          // out preconditioner
+    double2 *work;          // update_work_bytes(nanz, manz)
 };
-int run_update(const CGArgs &a, cudaStream_t st, int *ncg_out);
+size_t update_work_bytes(int nanz, int manz);
+// runs update + cjggra; cgres (host, ncgmax+2 floats) receives the CG record
+int run_update(const CGArgs &a, cudaStream_t st, int *ncg_out, float *cgres_host);
 
 }  // namespace crgpu

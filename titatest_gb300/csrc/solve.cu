@@ -337,7 +337,9 @@ __global__ void k_kpot(DevProblem P, DevBatch B, int nrhs, double2 *kpot) {
     int k = B.ks[s], l = (nrhs == 1) ? B.ls[s] : r;
     double f = B.fak[(size_t)s * P.n + i];
     double2 x = B.x[gid];
-    kpot[((size_t)k * P.eanz + l) * P.n + i] = cz(-x.x * f, -x.y * f);
+    double2 v = cz(-x.x * f, -x.y * f);
+    if (P.lsr) v = cadd(v, B.pota[(size_t)s * P.n + i]);  // src/fem.f90:390-391
+    kpot[((size_t)k * P.eanz + l) * P.n + i] = v;
 }
 
 void launch_kpot(const DevProblem &P, const DevBatch &B, int nrhs, double2 *kpot, cudaStream_t st) {
