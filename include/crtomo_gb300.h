@@ -20,7 +20,8 @@
  *    73 duplicate electrodes, 82 zero voltage, 93 zero geometry factor,
  *    94/97 allocation, 101 mixed and Dirichlet boundaries together).
  *    Codes >= 1000 are this library's own (1000 CUDA error, 1001 bad
- *    argument, 1002 unsupported option).  crgpu_last_error() gives the text
+ *    argument, 1002 unsupported option, 1003 a bounded device-side wait
+ *    gave up).  crgpu_last_error() gives the text
  *    (the reference's fetxt).
  *  - One context owns one CUDA stream; calls on one context must not overlap.
  */

@@ -65,10 +65,13 @@ void free_batch(crgpu_ctx *c) {
     c->batch_cap = 0;
 }
 
+// elements between the band factors of consecutive systems (see DevBatch)
+size_t lpitch_of(size_t n, size_t W) { return ((n * W + 1) & ~(size_t)1) + 2; }
+
 size_t bytes_per_system(const crgpu_ctx *c) {
     const size_t n = c->hg.n, W = c->hg.mb + 1, nnz = c->pat.nnz, nr = c->nrhs;
     size_t esz = c->precision == CRGPU_MIXED ? sizeof(float2) : sizeof(double2);
-    return n * W * esz + nnz * sizeof(double2) + n * sizeof(double) +
+    return lpitch_of(n, W) * esz + nnz * sizeof(double2) + n * sizeof(double) +
            nr * n * (3 * sizeof(double2) + esz) + 64;
 }
 
@@ -85,7 +88,7 @@ int ensure_batch(crgpu_ctx *c, int want) {
     e = e ? e : dalloc(c, &B.x, (size_t)want * nr * n);
     e = e ? e : dalloc(c, &B.r, (size_t)want * nr * n);
     char *L = nullptr, *y = nullptr;
-    e = e ? e : dalloc(c, &L, (size_t)want * n * W * esz);
+    e = e ? e : dalloc(c, &L, (size_t)want * lpitch_of(n, W) * esz);
     e = e ? e : dalloc(c, &y, (size_t)want * nr * n * esz);
     e = e ? e : dalloc(c, &B.status, (size_t)want);
     e = e ? e : dalloc(c, &B.active, (size_t)want * nr);
@@ -103,6 +106,7 @@ int ensure_batch(crgpu_ctx *c, int want) {
     }
     if (e) return e;
     B.L = L;
+    B.lpitch = lpitch_of(n, W);
     B.y = y;
     c->batch_cap = want;
     return 0;

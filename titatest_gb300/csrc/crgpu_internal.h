@@ -16,6 +16,7 @@ enum : int {
     ERR_CUDA = 1000,
     ERR_ARG = 1001,
     ERR_UNSUPPORTED = 1002,
+    ERR_TIMEOUT = 1003,  // a bounded device-side wait gave up
 };
 
 // ---------------------------------------------------------------------------

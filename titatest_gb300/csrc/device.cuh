@@ -44,7 +44,10 @@ struct DevBatch {
     double2 *b;       // [nsys][n]     scaled right-hand side (FP64)
     double2 *x;       // [nsys][n]     solution of A x = b (FP64)
     double2 *r;       // [nsys][n]     residual / work (FP64)
-    void *L;          // [nsys][n][mb+1] band factor (complex128 or complex64)
+    void *L;          // [nsys][lpitch] band factor (complex128 or complex64), row i at i*(mb+1)
+    size_t lpitch;    // elements of L's type between systems: n*(mb+1) rounded up to even, + 2,
+                      // so every system starts 16-byte aligned and a block copy rounded up to
+                      // 16 bytes stays inside its own system
     void *y;          // [nsys][n]     forward-substitution vector (L's type)
     int *status;      // [nsys]        0 or reference error code
     int *active;      // [nsys]        refinement still running

@@ -54,7 +54,7 @@ __global__ __launch_bounds__(kPlainThreads) void k_factor_plain(DevProblem P, De
     __shared__ double2 dsh, ysh;
     __shared__ int bad;
     for (int s = blockIdx.x; s < B.nsys; s += gridDim.x) {
-        double2 *L = (double2 *)B.L + (size_t)s * n * W;
+        double2 *L = (double2 *)B.L + (size_t)s * B.lpitch;
         const double2 *as = B.As + (size_t)s * P.nnz;
         double2 *bv = B.b + (size_t)s * n;
         double2 *yv = (double2 *)B.y + (size_t)s * n;
@@ -276,7 +276,7 @@ __global__ __launch_bounds__(MixCfg<WP>::NT, 1) void k_factor_mixed(DevProblem P
     const int sa0 = 4 * bi, sb0 = 4 * bj;
     const int nblk = (n + 3) / 4;
     for (int s = blockIdx.x; s < B.nsys; s += gridDim.x) {
-        float2 *L = (float2 *)B.L + (size_t)s * n * Wb;
+        float2 *L = (float2 *)B.L + (size_t)s * B.lpitch;
         float2 *yv = (float2 *)B.y + (size_t)s * n;
         const double2 *as = B.As + (size_t)s * P.nnz;
         const double2 *bv = B.b + (size_t)s * n;

@@ -87,6 +87,7 @@ extern "C" int crgpu_factor_system_noalloc(crgpu_ctx *c, const void *sigma_devic
     B.b = b;
     B.y = y;
     B.L = a_device;
+    B.lpitch = (size_t)c->hg.n * (c->hg.mb + 1);  // one system
     B.status = ints;
     if (cudaMemsetAsync(P.err, 0, sizeof(int), st) != cudaSuccess) return fail(c, ERR_CUDA, "memset");
     k_noalloc_init<<<1, 1, 0, st>>>(ints, ll);

@@ -1,13 +1,15 @@
 // Band triangular solves (src/vre.f90:5-71), FP64 iterative refinement of the
 // mixed mode, and the unscaling into kpot (src/fem.f90:383-394).
 //
-// One warp solves one right-hand side.  Both sweeps read the band rows of L
-// contiguously, streamed kRing rows ahead into shared memory by cp.async, and
-// keep a W = mb+1 window of the working vector in shared memory (entry i in
-// slot i mod W):
-//   forward  L y = b : row-oriented, a warp-reduced dot product per row;
-//   backward L^T x = y: the column sweep of vre (x_i broadcast, W updates).
+// One warp solves one right-hand side, kRB = 8 band rows at a time.  A
+// block's rows are contiguous in the band layout (8 * (mb+1) entries), so one
+// bulk copy per block brings them into shared memory kStages blocks ahead;
+// the working vector lives in a shared window.  Per block the dependent
+// chain is one warp reduction (forward) and an 8-step triangle of shuffles;
+// the rest is independent multiply-adds over the lanes' columns.
 #include "async.cuh"
+#include "bulk.cuh"
+#include "crgpu_internal.h"
 #include "device.cuh"
 #include "kernels.h"
 
@@ -26,12 +28,8 @@ struct Ops<double2> {
     __device__ static double2 add(double2 a, double2 b) { return cadd(a, b); }
     __device__ static double2 mul(double2 a, double2 b) { return cmul(a, b); }
     __device__ static double2 rcp(double2 a) { return crecip(a); }
-    __device__ static double2 reduce(double2 a) {
-        for (int o = 16; o > 0; o >>= 1) {
-            a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
-            a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
-        }
-        return a;
+    __device__ static double2 shfl_xor(double2 a, int m) {
+        return cz(__shfl_xor_sync(0xffffffffu, a.x, m), __shfl_xor_sync(0xffffffffu, a.y, m));
     }
 };
 template <>
@@ -48,193 +46,282 @@ struct Ops<float2> {
         const float q = __fdividef(1.0f, a.x * a.x + a.y * a.y);
         return cf(a.x * q, -a.y * q);
     }
-    __device__ static float2 reduce(float2 a) {
-        for (int o = 16; o > 0; o >>= 1) {
-            a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
-            a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
-        }
-        return a;
+    __device__ static float2 shfl_xor(float2 a, int m) {
+        return cf(__shfl_xor_sync(0xffffffffu, a.x, m), __shfl_xor_sync(0xffffffffu, a.y, m));
     }
 };
 
-constexpr int kSolveWarps = 4;
-constexpr int kRing = 8;  // rows of look-ahead streamed by cp.async
+constexpr int kRB = 8;      // rows per block of a sweep
+constexpr int kStages = 2;  // blocks of band rows in flight per warp
 
-// per-warp shared memory: kRing vector entries, kRing rows, the W window;
-// rounded to 16 bytes so every warp's region keeps cp.async alignment
+// Per-warp shared memory (byte offsets): stage barriers, the right-hand side
+// of each staged block (forward sweep), the staged band rows, the window of
+// the working vector (entry j in slot j & wmask) and the vector entries that
+// enter the window with each block (backward sweep).
+struct SolveLayout {
+    int bars, rhs, rows, win, ent, total;
+};
 template <typename T>
-__host__ __device__ constexpr size_t solve_smem_per_warp(int W) {
-    return (((size_t)kRing * W * sizeof(T) + (size_t)W * sizeof(T) + (size_t)kRing * sizeof(double2)) + 15) & ~(size_t)15;
+__host__ __device__ inline SolveLayout solve_layout(int W, int WW) {
+    SolveLayout s;
+    s.bars = 0;
+    s.rhs = 64;
+    s.rows = s.rhs + kStages * kRB * (int)sizeof(double2);
+    s.win = s.rows + kStages * kRB * W * (int)sizeof(T);
+    s.ent = s.win + WW * (int)sizeof(T);
+    s.total = (s.ent + kStages * kRB * (int)sizeof(T) + 127) & ~127;
+    return s;
 }
 
-// issue row rr of L (W entries) and vector entry vv (if >= 0) into ring slot sl
+// window size: a power of two holding mb + kRB consecutive entries
+static int solve_window(int mb) {
+    int w = 16;
+    while (w < mb + kRB) w <<= 1;
+    return w;
+}
+
+// Reduce eight per-lane partial sums a[0..7] (one per block row) over the
+// warp; lane l returns the total of row l >> 2.  Halving exchanges: nine
+// complex shuffles instead of eight full butterflies.
 template <typename T>
-__device__ __forceinline__ void ring_issue(const T *L, int W, int rr, int n, T *slot, const double2 *vsrc,
-                                           double2 *vdst, int lane) {
-    if (rr >= 0 && rr < n) {
-        const T *row = L + (size_t)rr * W;
-        for (int o = lane; o < W; o += 32) cp_async_elem<T>(slot + o, row + o);
-        if (lane == 0 && vsrc) cp_async16(vdst, vsrc);
+__device__ __forceinline__ T reduce_rows8(const T (&a)[kRB], int lane) {
+    const bool h16 = lane & 16, h8 = lane & 8, h4 = lane & 4;
+    T b[4], c[2];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const T send = h16 ? a[k] : a[k + 4];
+        const T keep = h16 ? a[k + 4] : a[k];
+        b[k] = Ops<T>::add(keep, Ops<T>::shfl_xor(send, 16));
     }
-    cp_commit();
-}
-
-// the same with a vector entry of type T (the back sweep's entering y values)
-template <typename T>
-__device__ __forceinline__ void ring_issue_v(const T *L, int W, int rr, int n, T *slot, const T *vsrc, T *vdst,
-                                             int lane) {
-    if (rr >= 0 && rr < n) {
-        const T *row = L + (size_t)rr * W;
-        for (int o = lane; o < W; o += 32) cp_async_elem<T>(slot + o, row + o);
-        if (lane == 0 && vsrc) cp_async_elem<T>(vdst, vsrc);
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const T send = h8 ? b[k] : b[k + 2];
+        const T keep = h8 ? b[k + 2] : b[k];
+        c[k] = Ops<T>::add(keep, Ops<T>::shfl_xor(send, 8));
     }
-    cp_commit();
+    const T send = h4 ? c[0] : c[1];
+    const T keep = h4 ? c[1] : c[0];
+    T d = Ops<T>::add(keep, Ops<T>::shfl_xor(send, 4));
+    d = Ops<T>::add(d, Ops<T>::shfl_xor(d, 2));
+    d = Ops<T>::add(d, Ops<T>::shfl_xor(d, 1));
+    return d;
 }
 
-// Row-oriented forward substitution y = L^{-1} rin:
-//   y_i = (rin_i - sum_{j=i-mb}^{i-1} L(i,j) y_j) / L(i,i)
-// rows stream through a ring of kRing slots; the last W values of y sit in
-// a shared-memory window (y_j in slot j mod W, tracked incrementally).
-// Items whose active flag is 0 are skipped.
+__device__ __forceinline__ void solve_timeout(const DevProblem &P, uint64_t *bar, int next_use, int last_use) {
+    // report, then let the copies still in flight land before the block exits
+    if ((threadIdx.x & 31) == 0) atomicCAS(P.err, 0, ERR_TIMEOUT);
+    for (int u = next_use; u <= last_use; u++) mbar_wait(&bar[u % kStages], (u / kStages) & 1);
+    cp_wait<0>();
+}
+
+// Forward substitution y = L^{-1} rin, one warp per right-hand side, in
+// blocks of kRB rows.  For block rows i0..i0+7:
+//   (1) t_r = rin_r - sum_{j < i0} L(r, j) y_j   lanes own columns, 8 sums
+//   (2) warp reduction of the 8 sums
+//   (3) the 8x8 triangle, y_q broadcast from the lanes of row q
+// The block's band rows (contiguous, 8 W entries) and right-hand side arrive
+// by bulk copy kStages blocks ahead.
 template <typename T>
-__global__ __launch_bounds__(kSolveWarps * 32) void k_fwd(DevProblem P, DevBatch B, int nrhs,
-                                                           const double2 *__restrict__ rin) {
-    extern __shared__ __align__(16) unsigned char sm_raw[];
-    const int n = P.n, mb = P.mb, W = mb + 1;
-    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    unsigned char *base = sm_raw + (size_t)wl * solve_smem_per_warp<T>(W);
-    double2 *rv = (double2 *)base;                       // [kRing]
-    T *ring = (T *)(base + kRing * sizeof(double2));     // [kRing][W]
-    T *pw = ring + (size_t)kRing * W;                    // [W]
-    const int item = blockIdx.x * kSolveWarps + wl;
+__global__ __launch_bounds__(32) void k_fwd(DevProblem P, DevBatch B, int nrhs, const double2 *__restrict__ rin,
+                                             int wmask) {
+    extern __shared__ __align__(128) unsigned char sm_raw[];
+    const int n = P.n, mb = P.mb, W = mb + 1, lane = threadIdx.x;
+    const int item = blockIdx.x;
     if (item >= B.nsys * nrhs) return;
     if (B.active && !B.active[item]) return;
-    const int s = item / nrhs;
-    const T *L = (const T *)B.L + (size_t)s * n * W;
+    const SolveLayout lay = solve_layout<T>(W, wmask + 1);
+    uint64_t *bar = (uint64_t *)(sm_raw + lay.bars);
+    double2 *rv = (double2 *)(sm_raw + lay.rhs);
+    T *rows = (T *)(sm_raw + lay.rows);
+    T *win = (T *)(sm_raw + lay.win);
+    const T *L = (const T *)B.L + (size_t)(item / nrhs) * B.lpitch;
     const double2 *r = rin + (size_t)item * n;
     T *y = (T *)B.y + (size_t)item * n;
-    for (int q = lane; q < W; q += 32) pw[q] = T{};
-    for (int q = 0; q < kRing; q++) ring_issue<T>(L, W, q, n, ring + (size_t)q * W, r + q, rv + q, lane);
-    int sb = 1;  // slot of column i - mb (== (i - mb) mod W); row i's slot is sb + mb - W or sb - 1
-    int sl = 0;  // ring slot of row i
-    for (int i = 0; i < n; i++) {
-        const T *row = ring + (size_t)sl * W;
-        cp_wait<kRing - 1>();
-        __syncwarp();
-        // read the diagonal and the right-hand side before any lane can
-        // re-issue copies into this ring slot
-        const T dg = row[mb];
-        const double2 rhs = rv[sl];
-        T acc{};
-        const int o0 = i < mb ? mb - i : 0;
-        for (int o = o0 + lane; o < mb; o += 32) {
-            int sw = sb + o;
-            if (sw >= W) sw -= W;
-            acc = Ops<T>::fms(acc, row[o], pw[sw]);
-        }
-        acc = Ops<T>::reduce(acc);  // acc = -sum
-        const int si = sb == 0 ? W - 1 : sb - 1;  // slot of row i == (i - mb - 1) mod W
-        if (lane == 0) {
-            const T v = Ops<T>::mul(Ops<T>::add(Ops<T>::from(rhs), acc), Ops<T>::rcp(dg));
-            pw[si] = v;
-            y[i] = v;
-        }
-        ring_issue<T>(L, W, i + kRing, n, ring + (size_t)sl * W, i + kRing < n ? r + i + kRing : nullptr,
-                      rv + sl, lane);
-        sb = sb + 1 == W ? 0 : sb + 1;
-        sl = sl + 1 == kRing ? 0 : sl + 1;
+    const int nblk = (n + kRB - 1) / kRB;
+    auto issue = [&](int t) {
+        if (t >= nblk) return;
+        const int st = t % kStages, i0 = t * kRB, nr = min(kRB, n - i0);
+        const uint32_t bl = ((uint32_t)(nr * W * (int)sizeof(T)) + 15u) & ~15u;
+        const uint32_t br = (uint32_t)nr * (uint32_t)sizeof(double2);
+        mbar_expect_tx(&bar[st], bl + br);
+        bulk_g2s(rows + (size_t)st * kRB * W, L + (size_t)i0 * W, bl, &bar[st]);
+        bulk_g2s(rv + st * kRB, r + i0, br, &bar[st]);
+    };
+    if (lane == 0) {
+        for (int q = 0; q < kStages; q++) mbar_init(&bar[q], 1);
+        mbar_init_fence();
+        for (int t = 0; t < kStages; t++) issue(t);
     }
-    cp_wait<0>();
+    __syncwarp();
+    const int myr = lane >> 2;
+    for (int t = 0; t < nblk; t++) {
+        const int st = t % kStages, i0 = t * kRB, nr = min(kRB, n - i0);
+        const bool ok = mbar_wait(&bar[st], (t / kStages) & 1);
+        if (!__all_sync(0xffffffffu, ok)) {
+            solve_timeout(P, bar, t, min(nblk - 1, t + kStages - 1));
+            return;
+        }
+        const T *Lb = rows + (size_t)st * kRB * W;
+        T acc[kRB];
+#pragma unroll
+        for (int q = 0; q < kRB; q++) acc[q] = T{};
+        for (int c = lane; c < mb; c += 32) {
+            const int j = i0 - mb + c;
+            if (j < 0) continue;
+            const T yv = win[j & wmask];
+#pragma unroll
+            for (int q = 0; q < kRB; q++)
+                if (c >= q) acc[q] = Ops<T>::fms(acc[q], Lb[q * W + c - q], yv);
+        }
+        T tv = Ops<T>::add(Ops<T>::from(rv[st * kRB + myr]), reduce_rows8<T>(acc, lane));
+        const T rinv = Ops<T>::rcp(Lb[myr * W + mb]);
+        T lt[kRB];
+#pragma unroll
+        for (int q = 0; q < kRB; q++) {
+            const int off = mb - myr + q;  // column i0 + q of row i0 + myr
+            lt[q] = (q < myr && off >= 0) ? Lb[myr * W + off] : T{};
+        }
+#pragma unroll
+        for (int q = 0; q < kRB - 1; q++) {
+            const T yq = Ops<T>::shfl(Ops<T>::mul(tv, rinv), 4 * q);
+            if (q < myr) tv = Ops<T>::fms(tv, lt[q], yq);
+        }
+        const T ymine = Ops<T>::mul(tv, rinv);
+        if ((lane & 3) == 0 && myr < nr) {
+            win[(i0 + myr) & wmask] = ymine;
+            y[i0 + myr] = ymine;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            fence_proxy_async();
+            issue(t + kStages);
+        }
+    }
 }
 
 // Backward substitution L^T x = y in place (y -> x), the column sweep of
-// src/vre.f90:58-69: x_i = w_i / L(i,i); w_j -= L(i,j) x_i for j < i.
+// src/vre.f90:58-69 in blocks of kRB rows from the bottom:
+//   (1) the 8x8 triangle: x_q = w_q / L(q,q), w_r -= L(q,r) x_q (r < q)
+//   (2) w_j -= sum_r L(r, j) x_r for the columns j < i0, lanes own columns
+// w lives in the shared window; entries enter it (w_j = y_j) when the first
+// block that touches column j is processed.
 template <typename T>
-__global__ __launch_bounds__(kSolveWarps * 32) void k_bwd(DevProblem P, DevBatch B, int nrhs) {
-    extern __shared__ __align__(16) unsigned char sm_raw[];
-    const int n = P.n, mb = P.mb, W = mb + 1;
-    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    unsigned char *base = sm_raw + (size_t)wl * solve_smem_per_warp<T>(W);
-    double2 *rv = (double2 *)base;  // entering entries y[i - W], as raw bytes of T
-    T *ring = (T *)(base + kRing * sizeof(double2));
-    T *pw = ring + (size_t)kRing * W;
-    const int item = blockIdx.x * kSolveWarps + wl;
+__global__ __launch_bounds__(32) void k_bwd(DevProblem P, DevBatch B, int nrhs, int wmask) {
+    extern __shared__ __align__(128) unsigned char sm_raw[];
+    const int n = P.n, mb = P.mb, W = mb + 1, lane = threadIdx.x;
+    const int item = blockIdx.x;
     if (item >= B.nsys * nrhs) return;
     if (B.active && !B.active[item]) return;
-    const int s = item / nrhs;
-    const T *L = (const T *)B.L + (size_t)s * n * W;
+    const SolveLayout lay = solve_layout<T>(W, wmask + 1);
+    uint64_t *bar = (uint64_t *)(sm_raw + lay.bars);
+    T *rows = (T *)(sm_raw + lay.rows);
+    T *win = (T *)(sm_raw + lay.win);
+    T *ent = (T *)(sm_raw + lay.ent);
+    const T *L = (const T *)B.L + (size_t)(item / nrhs) * B.lpitch;
     T *y = (T *)B.y + (size_t)item * n;
-    // window slot of entry j is j mod W
-    const int j0 = n - W < 0 ? 0 : n - W;
-    for (int q = j0 + lane; q < n; q += 32) pw[q % W] = y[q];
-    for (int q = 0; q < kRing; q++) {
-        const int rr = n - 1 - q;
-        ring_issue_v<T>(L, W, rr, n, ring + (size_t)q * W, rr - W >= 0 ? y + (rr - W) : nullptr, (T *)(rv + q), lane);
+    const int nblk = (n + kRB - 1) / kRB;
+    // use u = 0, 1, ... processes block t = nblk - 1 - u
+    auto issue = [&](int u) {
+        const int t = nblk - 1 - u;
+        if (t >= 0) {
+            const int st = u % kStages, i0 = t * kRB;
+            if (lane == 0) {
+                const int nr = min(kRB, n - i0);
+                const uint32_t bl = ((uint32_t)(nr * W * (int)sizeof(T)) + 15u) & ~15u;
+                mbar_expect_tx(&bar[st], bl);
+                bulk_g2s(rows + (size_t)st * kRB * W, L + (size_t)i0 * W, bl, &bar[st]);
+            }
+            const int j = i0 - mb + lane;  // entering column (not for the last block)
+            if (u > 0 && lane < kRB && j >= 0) cp_async_elem<T>(ent + st * kRB + lane, y + j);
+        }
+        cp_commit();
+    };
+    const int i0l = (nblk - 1) * kRB;
+    for (int j = max(0, i0l - mb) + lane; j < n; j += 32) win[j & wmask] = y[j];
+    if (lane == 0) {
+        for (int q = 0; q < kStages; q++) mbar_init(&bar[q], 1);
+        mbar_init_fence();
     }
-    int si = (n - 1) % W;            // slot of row i
-    int sb = si + 1 == W ? 0 : si + 1;  // slot of column i - mb (== (i + 1) mod W)
-    int sl = 0;
-    for (int i = n - 1; i >= 0; i--) {
-        const T *row = ring + (size_t)sl * W;
-        cp_wait<kRing - 1>();
+    __syncwarp();
+    for (int u = 0; u < kStages; u++) issue(u);
+    const int myr = lane >> 2;
+    for (int u = 0; u < nblk; u++) {
+        const int t = nblk - 1 - u, st = u % kStages, i0 = t * kRB, nr = min(kRB, n - i0);
+        const bool ok = mbar_wait(&bar[st], (u / kStages) & 1);
+        cp_wait<kStages - 1>();
+        if (!__all_sync(0xffffffffu, ok)) {
+            solve_timeout(P, bar, u, min(nblk - 1, u + kStages - 1));
+            return;
+        }
+        {
+            const int j = i0 - mb + lane;
+            if (u > 0 && lane < kRB && j >= 0) win[j & wmask] = ent[st * kRB + lane];
+        }
         __syncwarp();
-        T v{};
-        if (lane == 0) {
-            v = Ops<T>::mul(pw[si], Ops<T>::rcp(row[mb]));
-            y[i] = v;
+        const T *Lb = rows + (size_t)st * kRB * W;
+        T wv = win[(i0 + myr) & wmask];
+        const T rinv = Ops<T>::rcp(Lb[myr * W + mb]);
+        T lt[kRB];
+#pragma unroll
+        for (int q = 0; q < kRB; q++) {
+            const int off = mb - q + myr;  // column i0 + myr of row i0 + q
+            lt[q] = (myr < q && q < nr && off >= 0) ? Lb[q * W + off] : T{};
         }
-        v = Ops<T>::shfl(v, 0);
-        const int o0 = i < mb ? mb - i : 0;
-        for (int o = o0 + lane; o < mb; o += 32) {
-            int sw = sb + o;
-            if (sw >= W) sw -= W;
-            pw[sw] = Ops<T>::fms(pw[sw], row[o], v);
+        T xq[kRB];
+#pragma unroll
+        for (int q = kRB - 1; q >= 0; q--) {
+            xq[q] = Ops<T>::shfl(Ops<T>::mul(wv, rinv), 4 * q);
+            if (myr < q && q < nr) wv = Ops<T>::fms(wv, lt[q], xq[q]);
         }
-        if (lane == 0 && i - W >= 0) pw[si] = *(const T *)(rv + sl);
-        const int rr = i - kRing;
-        ring_issue_v<T>(L, W, rr, n, ring + (size_t)sl * W, rr - W >= 0 ? y + (rr - W) : nullptr, (T *)(rv + sl),
-                        lane);
-        si = si == 0 ? W - 1 : si - 1;
-        sb = sb == 0 ? W - 1 : sb - 1;
-        sl = sl + 1 == kRing ? 0 : sl + 1;
+        if ((lane & 3) == 0 && myr < nr) y[i0 + myr] = Ops<T>::mul(wv, rinv);
+        for (int c = lane; c < mb; c += 32) {
+            const int j = i0 - mb + c;
+            if (j < 0) continue;
+            T w2 = win[j & wmask];
+#pragma unroll
+            for (int q = 0; q < kRB; q++)
+                if (q < nr && c >= q) w2 = Ops<T>::fms(w2, Lb[q * W + c - q], xq[q]);
+            win[j & wmask] = w2;
+        }
+        __syncwarp();
+        if (lane == 0) fence_proxy_async();
+        issue(u + kStages);
     }
     cp_wait<0>();
 }
 
 template <typename T>
-static void set_solve_smem(int W) {
-    static int done_w = -1;
-    if (done_w == W) return;
-    size_t bytes = kSolveWarps * solve_smem_per_warp<T>(W);
-    cudaFuncSetAttribute(k_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    cudaFuncSetAttribute(k_bwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    done_w = W;
+static int set_solve_smem(int W, int WW) {
+    static int done = -1;
+    const int bytes = solve_layout<T>(W, WW).total;
+    if (done != bytes) {
+        cudaFuncSetAttribute(k_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        cudaFuncSetAttribute(k_bwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        done = bytes;
+    }
+    return bytes;
 }
 
 void launch_forward_solve(const DevProblem &P, const DevBatch &B, int nrhs, bool mixed, const double2 *rin,
                           cudaStream_t st) {
-    int nitems = B.nsys * nrhs;
-    int grid = (nitems + kSolveWarps - 1) / kSolveWarps;
-    int W = P.mb + 1;
+    const int nitems = B.nsys * nrhs, W = P.mb + 1, WW = solve_window(P.mb);
     if (mixed) {
-        set_solve_smem<float2>(W);
-        k_fwd<float2><<<grid, kSolveWarps * 32, kSolveWarps * solve_smem_per_warp<float2>(W), st>>>(P, B, nrhs, rin);
+        const int bytes = set_solve_smem<float2>(W, WW);
+        k_fwd<float2><<<nitems, 32, bytes, st>>>(P, B, nrhs, rin, WW - 1);
     } else {
-        set_solve_smem<double2>(W);
-        k_fwd<double2><<<grid, kSolveWarps * 32, kSolveWarps * solve_smem_per_warp<double2>(W), st>>>(P, B, nrhs, rin);
+        const int bytes = set_solve_smem<double2>(W, WW);
+        k_fwd<double2><<<nitems, 32, bytes, st>>>(P, B, nrhs, rin, WW - 1);
     }
 }
 
 void launch_back_solve(const DevProblem &P, const DevBatch &B, int nrhs, bool mixed, cudaStream_t st) {
-    int nitems = B.nsys * nrhs;
-    int grid = (nitems + kSolveWarps - 1) / kSolveWarps;
-    int W = P.mb + 1;
+    const int nitems = B.nsys * nrhs, W = P.mb + 1, WW = solve_window(P.mb);
     if (mixed) {
-        set_solve_smem<float2>(W);
-        k_bwd<float2><<<grid, kSolveWarps * 32, kSolveWarps * solve_smem_per_warp<float2>(W), st>>>(P, B, nrhs);
+        const int bytes = set_solve_smem<float2>(W, WW);
+        k_bwd<float2><<<nitems, 32, bytes, st>>>(P, B, nrhs, WW - 1);
     } else {
-        set_solve_smem<double2>(W);
-        k_bwd<double2><<<grid, kSolveWarps * 32, kSolveWarps * solve_smem_per_warp<double2>(W), st>>>(P, B, nrhs);
+        const int bytes = set_solve_smem<double2>(W, WW);
+        k_bwd<double2><<<nitems, 32, bytes, st>>>(P, B, nrhs, WW - 1);
     }
 }
 
