@@ -368,7 +368,7 @@ def main():
     ap.add_argument("--config", type=int, default=2)
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--refine-maxit", type=int, default=8)
-    ap.add_argument("--refine-tol", type=float, default=1e-8)
+    ap.add_argument("--refine-tol", type=float, default=1e-6)
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     args = ap.parse_args()

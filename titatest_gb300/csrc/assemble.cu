@@ -35,39 +35,38 @@ void launch_adom(const DevProblem &P, const double2 *sigma, double2 *adom, cudaS
     k_adom<<<(unsigned)((tot + nt - 1) / nt), nt, 0, st>>>(P, sigma, adom);
 }
 
-// One thread per (system, row): raw values of the row (area part + mixed
-// boundary part), Dirichlet rows and columns, and fak of the row.
-__global__ void k_assemble_rows(DevProblem P, DevBatch B, const double2 *__restrict__ sigma,
-                                const double2 *__restrict__ adom) {
-    size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (size_t)B.nsys * P.n) return;
-    int s = (int)(gid / P.n), i = (int)(gid % P.n);
-    int k = B.ks[s], l = B.ls[s];
-    const double2 *ad = adom + (size_t)k * P.nnz;
-    double2 *as = B.As + (size_t)s * P.nnz;
-    const double *kgl = P.kg + ((size_t)k * P.eanz + l) * P.relanz;
-    bool dir_i = P.dirichlet[i] != 0;
-    int p0 = P.rowptr[i], p1 = P.rowptr[i + 1];
-    double2 diag = cz(0.0, 0.0);
-    for (int p = p0; p < p1; p++) {
-        double2 v = ad[p];
-        for (int q = P.bnd_ptr[p]; q < P.bnd_ptr[p + 1]; q++) {
-            int code = P.bnd_list[q];
-            int rb = code >> 4, imn = code & 15;
-            double dum = P.relbg[rb * 3 + imn] * kgl[rb];
-            double2 sg = sigma[P.brnr[rb]];
-            v = cadd(v, cz(dum * sg.x, dum * sg.y));
-        }
-        int c = P.col[p];
-        if (c < 0) {
-            as[p] = cz(0.0, 0.0);
-            continue;
-        }
-        if (dir_i || P.dirichlet[c]) v = (c == i) ? cz(1.0, 0.0) : cz(0.0, 0.0);
-        as[p] = v;
-        if (c == i) diag = v;
+// Value of lower-pattern entry p of system (k, l) before scaling: area part
+// plus the mixed-boundary terms, with Dirichlet rows and columns replaced.
+__device__ __forceinline__ double2 entry_value(const DevProblem &P, const double2 *__restrict__ ad,
+                                               const double *__restrict__ kgl, const double2 *__restrict__ sigma,
+                                               int p, int i, int c, bool dir_i) {
+    double2 v = ad[p];
+    for (int q = P.bnd_ptr[p]; q < P.bnd_ptr[p + 1]; q++) {
+        const int code = P.bnd_list[q];
+        const int rb = code >> 4, imn = code & 15;
+        const double dum = P.relbg[rb * 3 + imn] * kgl[rb];
+        const double2 sg = sigma[P.brnr[rb]];
+        v = cadd(v, cz(dum * sg.x, dum * sg.y));
     }
-    double dum = cabsd(diag);
+    if (dir_i || P.dirichlet[c]) v = (c == i) ? cz(1.0, 0.0) : cz(0.0, 0.0);
+    return v;
+}
+
+// fak of every row (src/scalab.f90:50-64): grid (row blocks, systems).  The
+// rows of the lower pattern are sorted by column, so the diagonal is the
+// last entry that is not padding.
+__global__ void k_fak(DevProblem P, DevBatch B, const double2 *__restrict__ sigma,
+                      const double2 *__restrict__ adom) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
+    if (i >= P.n) return;
+    const int k = B.ks[s], l = B.ls[s];
+    const double2 *ad = adom + (size_t)k * P.nnz;
+    const double *kgl = P.kg + ((size_t)k * P.eanz + l) * P.relanz;
+    int pd = -1;
+    for (int p = P.rowptr[i]; p < P.rowptr[i + 1]; p++)
+        if (P.col[p] == i) pd = p;
+    double dum = 0.0;
+    if (pd >= 0) dum = cabsd(entry_value(P, ad, kgl, sigma, pd, i, i, P.dirichlet[i] != 0));
     if (!(dum > 0.0)) {  // src/scalab.f90:57-61
         atomicCAS(&B.status[s], 0, 27);
         dum = 1.0;
@@ -75,33 +74,43 @@ __global__ void k_assemble_rows(DevProblem P, DevBatch B, const double2 *__restr
     B.fak[(size_t)s * P.n + i] = 1.0 / sqrt(dum);
 }
 
-// scaling of every entry with the factors of its row and column
-__global__ void k_scale(DevProblem P, DevBatch B) {
-    size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (size_t)B.nsys * P.nnz) return;
-    int s = (int)(gid / P.nnz), p = (int)(gid % P.nnz);
-    double2 *a = B.As + gid;
-    int i = P.row[p], c = P.col[p];
-    if (c < 0) return;
-    if (i == c) {
-        double2 v = *a;
-        double dum = cabsd(v);
-        if (dum > 0.0) *a = cdiv(v, cz(dum, 0.0));
-    } else {
-        const double *f = B.fak + (size_t)s * P.n;
-        double fk = f[i] * f[c];
-        double2 v = *a;
-        *a = cz(v.x * fk, v.y * fk);
+// Scaled values of row i (src/kompab.f90 + src/scalab.f90:63-80): the
+// diagonal becomes a_ii / |a_ii|, the others a_ij * fak_i * fak_j.
+__global__ void k_assemble_rows(DevProblem P, DevBatch B, const double2 *__restrict__ sigma,
+                                const double2 *__restrict__ adom) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
+    if (i >= P.n) return;
+    const int k = B.ks[s], l = B.ls[s];
+    const double2 *ad = adom + (size_t)k * P.nnz;
+    double2 *as = B.As + (size_t)s * P.nnz;
+    const double *kgl = P.kg + ((size_t)k * P.eanz + l) * P.relanz;
+    const double *f = B.fak + (size_t)s * P.n;
+    const bool dir_i = P.dirichlet[i] != 0;
+    const double fi = f[i];
+    for (int p = P.rowptr[i]; p < P.rowptr[i + 1]; p++) {
+        const int c = P.col[p];
+        if (c < 0) {
+            as[p] = cz(0.0, 0.0);
+            continue;
+        }
+        double2 v = entry_value(P, ad, kgl, sigma, p, i, c, dir_i);
+        if (c == i) {
+            const double dum = cabsd(v);
+            if (dum > 0.0) v = cdiv(v, cz(dum, 0.0));
+        } else {
+            const double fk = fi * f[c];
+            v = cz(v.x * fk, v.y * fk);
+        }
+        as[p] = v;
     }
 }
 
 void launch_assemble(const DevProblem &P, const DevBatch &B, const double2 *sigma, const double2 *adom,
                      cudaStream_t st) {
-    int nt = 256;
-    size_t t1 = (size_t)B.nsys * P.n;
-    k_assemble_rows<<<(unsigned)((t1 + nt - 1) / nt), nt, 0, st>>>(P, B, sigma, adom);
-    size_t t2 = (size_t)B.nsys * P.nnz;
-    k_scale<<<(unsigned)((t2 + nt - 1) / nt), nt, 0, st>>>(P, B);
+    const int nt = 128;
+    const dim3 grid((P.n + nt - 1) / nt, B.nsys);
+    k_fak<<<grid, nt, 0, st>>>(P, B, sigma, adom);
+    k_assemble_rows<<<grid, nt, 0, st>>>(P, B, sigma, adom);
 }
 
 // Right-hand sides.  nrhs == 1: one system per (k, l), b of kompab (unit

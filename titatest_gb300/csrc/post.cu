@@ -76,7 +76,7 @@ void launch_bvolt(const DevProblem &P, const double2 *hpot, int mode, const doub
 // measurements and keep their k-sums in registers.
 // ---------------------------------------------------------------------------
 constexpr int kSensThreads = 256;
-constexpr int kSensMPT = 4;  // measurements per thread per pass
+constexpr int kSensMPT = 16;  // measurements per thread per pass (4096 per pass)
 
 template <typename R>
 struct SensT;
@@ -111,16 +111,11 @@ __global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P, const doub
 #pragma unroll
     for (int q = 0; q < 4; q++) nodes[q] = P.enodes[e * 4 + q];
     const int eanz = P.eanz;
+    const int4 *meas4 = (const int4 *)P.meas;
     for (int i0 = 0; i0 < P.nanz; i0 += kSensThreads * kSensMPT) {
         C acc[kSensMPT];
-        int ee[kSensMPT][4];
 #pragma unroll
-        for (int m = 0; m < kSensMPT; m++) {
-            acc[m] = SensT<R>::mk(0, 0);
-            int i = i0 + m * kSensThreads + threadIdx.x;
-#pragma unroll
-            for (int q = 0; q < 4; q++) ee[m][q] = (i < P.nanz) ? P.meas[i * 4 + q] : -1;
-        }
+        for (int m = 0; m < kSensMPT; m++) acc[m] = SensT<R>::mk(0, 0);
         for (int k = 0; k < P.K; k++) {
             __syncthreads();
             for (int t = threadIdx.x; t < nk * eanz; t += kSensThreads) {
@@ -134,13 +129,14 @@ __global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P, const doub
             for (int m = 0; m < kSensMPT; m++) {
                 int i = i0 + m * kSensThreads + threadIdx.x;
                 if (i >= P.nanz) continue;
+                const int4 ee = meas4[i];  // electrodes e1..e4 (-1: none), L1-resident
                 C u[4], v[4];
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    C s1 = ee[m][0] >= 0 ? kp_sh[q * eanz + ee[m][0]] : SensT<R>::mk(0, 0);
-                    C s2 = ee[m][1] >= 0 ? kp_sh[q * eanz + ee[m][1]] : SensT<R>::mk(0, 0);
-                    C s3 = ee[m][2] >= 0 ? kp_sh[q * eanz + ee[m][2]] : SensT<R>::mk(0, 0);
-                    C s4 = ee[m][3] >= 0 ? kp_sh[q * eanz + ee[m][3]] : SensT<R>::mk(0, 0);
+                    C s1 = ee.x >= 0 ? kp_sh[q * eanz + ee.x] : SensT<R>::mk(0, 0);
+                    C s2 = ee.y >= 0 ? kp_sh[q * eanz + ee.y] : SensT<R>::mk(0, 0);
+                    C s3 = ee.z >= 0 ? kp_sh[q * eanz + ee.z] : SensT<R>::mk(0, 0);
+                    C s4 = ee.w >= 0 ? kp_sh[q * eanz + ee.w] : SensT<R>::mk(0, 0);
                     u[q] = SensT<R>::mk(s2.x - s1.x, s2.y - s1.y);
                     v[q] = SensT<R>::mk(s4.x - s3.x, s4.y - s3.y);
                     if (q >= nk) { u[q] = SensT<R>::mk(0, 0); v[q] = SensT<R>::mk(0, 0); }
