@@ -67,4 +67,56 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     return false;
 }
 
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s: far above any legitimate wait
+
+// try_wait that lets the thread sleep (up to `ns`) until the phase completes,
+// so waiting warps leave the issue slots to the warps doing the work
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t parity, uint32_t ns) {
+    uint32_t ok;
+    asm volatile(
+        "{\n"
+        " .reg .pred p;\n"
+        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+        " selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+        : "memory");
+    return ok != 0;
+}
+
+// mbar_wait for kernels whose roles wait on one another: gives up when
+// another thread has raised *abort, or after kWaitNs (then raises it).
+// sleep_ns > 0 lets the waiting thread sleep between polls (for waits off
+// the critical path); 0 polls without sleeping.
+__device__ __forceinline__ bool mbar_wait_abort(uint64_t *bar, uint32_t parity, volatile int *abort,
+                                                uint32_t sleep_ns = 20000u) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t it = 1;; it++) {
+        if (sleep_ns ? mbar_try_wait_sleep(bar, parity, sleep_ns) : mbar_try_wait(bar, parity)) return true;
+        if ((it & 15u) == 0u) {
+            if (*abort) return false;
+            if (globaltimer_ns() - t0 > kWaitNs) {
+                *abort = 1;
+                return false;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_inval(uint64_t *bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+
 }  // namespace crgpu

@@ -15,15 +15,18 @@
 //  * k_factor_plain (complex128): the window is updated in place in the band
 //    buffer (global memory; the active ~(mb+1)^2 * 16 B stays in L2).  On
 //    GB300 the FP64 pipe, not memory, bounds this kernel.
-//  * k_factor_mixed<WP> (complex64): the (mb+1) x (mb+1) window lives in
-//    registers.  Window rows rotate through W = mb+1 slots (row r in slot
-//    r mod W); every thread owns a fixed 4x4 tile of the lower triangle of
-//    slot pairs, so a step needs no data movement: the retiring pivot row's
-//    slot is refilled with the entering row.
+//  * complex64, mb <= 124: k_factor_tc (tc_factor.cu) keeps the window in
+//    tensor memory and applies the trailing updates with tcgen05.mma.
+//  * complex64, larger mb: k_factor_mixed<WP>: the (mb+1) x (mb+1) window
+//    lives in registers.  Window rows rotate through W = mb+1 slots (row r in
+//    slot r mod W); every thread owns a fixed 4x4 tile of the lower triangle
+//    of slot pairs, so a step needs no data movement: the retiring pivot
+//    row's slot is refilled with the entering row.
 #include "async.cuh"
 #include "device.cuh"
 #include "crgpu_internal.h"
 #include "kernels.h"
+#include "mixed_common.cuh"
 
 namespace crgpu {
 
@@ -138,46 +141,6 @@ struct MixCfg {
     static constexpr int NT = ((T + 31) / 32) * 32 + 32;  // + a staging warp without tiles
 };
 
-constexpr int kStageSteps = 4;  // block steps of look-ahead for entering rows
-
-// issue the cp.async copies of the 4 rows r0..r0+3 (padded pattern values,
-// columns, right-hand side) into ring slot sl; called by the staging warp
-__device__ __forceinline__ void stage_issue4(const DevProblem &P, const double2 *as, const double2 *bv, int r0,
-                                             int ln, int rw, int fuse, double2 (*rv)[32], int (*rc)[32],
-                                             double2 *rb) {
-    const int r = ln >> 3, e0 = ln & 7;
-    const int rr = r0 + r;
-    if (rr < P.n) {
-        for (int e = e0; e < rw; e += 8) {
-            cp_async16(&rv[r][e], as + (size_t)rr * rw + e);
-            cp_async4(&rc[r][e], P.col + (size_t)rr * rw + e);
-        }
-        if (e0 == 7 && fuse) cp_async16(&rb[r], bv + rr);
-    }
-    cp_commit();
-}
-
-// Principal complex square root and reciprocal from the approximate MUFU
-// reciprocal square root / reciprocal (a few ulp): the complex64 factor is a
-// preconditioner for the FP64 refinement.
-__device__ __forceinline__ float2 csqrt_fast(float2 z) {
-    const float r2 = z.x * z.x + z.y * z.y;
-    if (r2 == 0.f) return cf(0.f, 0.f);
-    const float r = r2 * rsqrtf(r2);
-    if (z.x >= 0.f) {
-        const float t2 = 0.5f * (r + z.x);
-        const float it = rsqrtf(t2);
-        return cf(t2 * it, 0.5f * z.y * it);
-    }
-    const float t2 = 0.5f * (r - z.x);
-    const float it = rsqrtf(t2);
-    return cf(0.5f * fabsf(z.y) * it, copysignf(t2 * it, z.y));
-}
-__device__ __forceinline__ float2 crecip_fast(float2 d) {
-    const float q = __fdividef(1.0f, d.x * d.x + d.y * d.y);
-    return cf(d.x * q, -d.y * q);
-}
-
 // In-place L L^T of the 4x4 diagonal tile held in registers (rows j0..j0+3);
 // rows beyond n get a unit pivot.  Publishes L and 1/diag to shared memory.
 __device__ __forceinline__ void factor_diag4(float2 (&w)[4][4], int j0, int n, float2 (*Ld)[4], float2 *dinv,
@@ -205,41 +168,6 @@ __device__ __forceinline__ void factor_diag4(float2 (&w)[4][4], int j0, int n, f
         for (int r = q + 1; r < 4; r++)
 #pragma unroll
             for (int c = q + 1; c <= r; c++) w[r][c] = cfmsf(w[r][c], w[r][q], w[c][q]);
-    }
-}
-
-// Tile entries from the 4 entering rows staged by slot in nb[4][WP]: a tile
-// of block row B takes row a's slots of its column block, a tile of block
-// column B takes row b's slots of its row block, the diagonal tile takes the
-// rows among themselves.  128-bit shared loads.
-template <int WP>
-__device__ __forceinline__ void refill_tile(float2 (&w)[4][4], const float2 (*nb)[WP], bool rowB, bool colB,
-                                            int sa0, int sb0) {
-    if (rowB && colB) {
-#pragma unroll
-        for (int a = 0; a < 4; a++)
-#pragma unroll
-            for (int b = 0; b < 4; b++) w[a][b] = nb[a > b ? a : b][sb0 + (a > b ? b : a)];
-    } else if (rowB) {
-#pragma unroll
-        for (int a = 0; a < 4; a++) {
-            const float4 v0 = *(const float4 *)&nb[a][sb0];
-            const float4 v1 = *(const float4 *)&nb[a][sb0 + 2];
-            w[a][0] = cf(v0.x, v0.y);
-            w[a][1] = cf(v0.z, v0.w);
-            w[a][2] = cf(v1.x, v1.y);
-            w[a][3] = cf(v1.z, v1.w);
-        }
-    } else {
-#pragma unroll
-        for (int b = 0; b < 4; b++) {
-            const float4 v0 = *(const float4 *)&nb[b][sa0];
-            const float4 v1 = *(const float4 *)&nb[b][sa0 + 2];
-            w[0][b] = cf(v0.x, v0.y);
-            w[1][b] = cf(v0.z, v0.w);
-            w[2][b] = cf(v1.x, v1.y);
-            w[3][b] = cf(v1.z, v1.w);
-        }
     }
 }
 
@@ -484,6 +412,7 @@ int mixed_window_supported(int W) {
 
 int launch_factor_mixed(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st) {
     int W = P.mb + 1;
+    if (P.mb + 4 <= 128) return launch_factor_tc(P, B, fuse, nsm, st);
     int grid = B.nsys < nsm ? B.nsys : nsm;
 #define X(S)                                                                   \
     if (W <= S) {                                                              \

@@ -27,6 +27,8 @@ void launch_factor_plain(const DevProblem &P, const DevBatch &B, int fuse, int n
 int launch_factor_mixed(const DevProblem &P, const DevBatch &B, int fuse, int nsm,
                         cudaStream_t st);
 int mixed_window_supported(int W);
+// tensor-core variant (tc_factor.cu) for band widths mb <= 124
+int launch_factor_tc(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st);
 
 // triangular solves (src/vre.f90); item = system * nrhs + rhs
 void launch_forward_solve(const DevProblem &P, const DevBatch &B, int nrhs, bool mixed,

@@ -1,0 +1,596 @@
+// Complex64 band factorisation on the 5th-generation tensor cores
+// (src/chol.f90:7-88, with the forward substitution of src/vre.f90:45-56
+// fused in), for band widths mb <= 124.
+//
+// The active window (rows j .. j+127 of the band, row r in slot r mod 128)
+// lives in tensor memory as FP32: TMEM lane s = slot s, columns 2c / 2c+1 =
+// real / imaginary part of the entry with the row of slot c.  One step
+// eliminates the 4 pivot columns j..j+3 (pivot slot block Bk = J mod 32):
+//
+//   1. tcgen05.ld of the 8 pivot columns: every thread (= slot) gets its
+//      row's 4 entries A(r, j..j+3);
+//   2. SIMT panel: 4x4 factor of the diagonal block, the slot's L entries
+//      l_r = A(r, j..j+3) Ld^{-T}, the band rows of L to global memory and
+//      the fused forward substitution;
+//   3. one elected thread issues, into the TMEM window,
+//        D += A . B^T  (M=128, N=256, K=8, kind::tf32)
+//      with A row r = [Re l_r | Im l_r] and B rows 2c, 2c+1 =
+//      [-Re l_c | Im l_c], [-Im l_c | -Re l_c]: D -= l l^T in complex
+//      arithmetic.  Three products (hi.hi + hi.lo + lo.hi of the tf32
+//      splits of l) keep FP32 accuracy; pivot rows contribute zero.
+//   4. the 4 rows entering at this step take over the pivot slots.  Their
+//      row part D(p, :) is set by a fourth MMA whose A is one-hot on the
+//      pivot lanes and whose B holds new value - old value (hi + lo); the
+//      old value of D(p, c) is, by symmetry, the pivot column entry that
+//      thread c read in step 1.  Their column part D(:, p) is written by
+//      tcgen05.st once the MMAs of the step have completed.
+// Entering rows never reach back into eliminated columns because the window
+// has 128 >= mb + 4 rows, so they need no update of earlier steps.
+//
+// The MMAs of a step are issued in two parts: (a) the 16 columns holding the
+// next step's pivot block, then (b) the other 240.  The next panel starts
+// as soon as (a) has landed and overlaps (b); operands are double buffered.
+//
+// Roles: warps 0-3 (128 threads, thread t <-> TMEM lane t) run the panel;
+// warp 4 stages the entering rows from the scaled sparse values (cp.async
+// ring, kStageSteps ahead); warp 5 issues the MMAs when the panel hands over
+// a step's operands (named barrier 2).  Every mbarrier wait is bounded in
+// time and failures are agreed on by a barrier reduction, so all roles leave
+// together.
+#include "bulk.cuh"
+#include "crgpu_internal.h"
+#include "device.cuh"
+#include "kernels.h"
+#include "mixed_common.cuh"
+
+namespace crgpu {
+
+namespace {
+
+constexpr int kTcWP = 128;     // window slots = TMEM lanes = MMA M
+constexpr int kTcCols = 256;   // TMEM columns = MMA N
+constexpr int kTcNB = kTcWP / 4;
+constexpr int kTcThreads = 192;
+constexpr int kTcNNB = 4;      // buffers of entering rows
+constexpr int kTcSmemRequest = 110 * 1024;  // at most two blocks (2 x 256 TMEM columns) per SM
+
+struct TcOperands {
+    // K-major canonical layout without swizzle: 8-row x 16-byte core
+    // matrices, K-adjacent cores 128 B apart, row groups 256 B apart.
+    float a_hi[kTcWP * 8], a_lo[kTcWP * 8], a_e[kTcWP * 8];
+    float b_hi[kTcCols * 8], b_lo[kTcCols * 8], b_e[kTcCols * 8];
+};
+
+struct TcSmem {
+    TcOperands op[2];               // double buffered by step parity
+    float2 nbuf[kTcNNB][4][kTcWP];  // entering rows by slot of column
+    float2 bnew[kTcNNB][4];         // their right-hand sides
+    double2 ring_val[kStageSteps][4][32];
+    double2 ring_b[kStageSteps][4];
+    int ring_col[kStageSteps][4][32];
+    float2 dm[2][4][4];  // diagonal block of the step
+    float2 bp[2][4];     // right-hand side of the pivot rows
+    uint64_t bar_a, bar_b;  // MMA parts (a) and (b) of a step completed
+    uint64_t bar_nbF[kTcNNB], bar_nbE[kTcNNB];
+    uint32_t tmem_base;
+    int bad;
+    int abort_flag;
+    int panel_fail;
+    int stop_issue;
+};
+
+// float index of element (row, k) of a [rows x 8] K-major operand
+__device__ __forceinline__ int kmaj(int row, int k) { return ((row >> 3) * 2 + (k >> 2)) * 32 + (row & 7) * 4 + (k & 3); }
+
+__device__ __forceinline__ uint64_t smem_desc(const void *p) {
+    const uint64_t addr = smem_u32(p);
+    uint64_t d = (addr >> 4) & 0x3FFFull;   // start address
+    d |= (uint64_t)(128 >> 4) << 16;        // leading (K) byte offset between core matrices
+    d |= (uint64_t)(256 >> 4) << 32;        // stride (M/N) byte offset between 8-row groups
+    d |= 1ull << 46;                        // descriptor version of sm_100
+    return d;                               // base offset 0, no swizzle
+}
+
+// kind::tf32 instruction descriptor: D f32, A/B tf32, both K-major, N, M
+__host__ __device__ constexpr uint32_t tf32_idesc(int M, int N) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+
+__device__ __forceinline__ void tc_mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc) {
+    asm volatile(
+        "{\n"
+        " .reg .pred p;\n"
+        " setp.ne.b32 p, 1, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n"
+        "}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+    uint32_t r0, r1, r2, r3, r4, r5, r6, r7;
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3), "=r"(r4), "=r"(r5), "=r"(r6), "=r"(r7)
+        : "r"(taddr)
+        : "memory");
+    v[0] = __uint_as_float(r0);
+    v[1] = __uint_as_float(r1);
+    v[2] = __uint_as_float(r2);
+    v[3] = __uint_as_float(r3);
+    v[4] = __uint_as_float(r4);
+    v[5] = __uint_as_float(r5);
+    v[6] = __uint_as_float(r6);
+    v[7] = __uint_as_float(r7);
+}
+
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};\n"
+        "tcgen05.wait::st.sync.aligned;\n" ::"r"(taddr),
+        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+        "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+        : "memory");
+}
+
+// tf32 split x = hi + lo: hi is x rounded to the nearest tf32 (10 mantissa
+// bits), so |lo| <= 2^-11 |x| and the tensor core's truncation of lo to tf32
+// costs at most ~2^-22 |x|; the dropped lo.lo product is below 2^-22 too.
+__device__ __forceinline__ float tf32_hi(float x) {
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
+// barrier of the 128 panel threads that also returns the OR of `fail`
+__device__ __forceinline__ bool panel_bar_or(bool fail) {
+    uint32_t r;
+    asm volatile(
+        "{\n"
+        " .reg .pred pi, po;\n"
+        " setp.ne.u32 pi, %1, 0;\n"
+        " bar.red.or.pred po, 1, 128, pi;\n"
+        " selp.u32 %0, 1, 0, po;\n"
+        "}\n"
+        : "=r"(r)
+        : "r"((uint32_t)fail)
+        : "memory");
+    return r != 0;
+}
+
+// entry between entering rows a and b of pivot block Bk: the scatter stores
+// each row's lower pattern, so it sits in the row with the larger index
+__device__ __forceinline__ float2 entering_pair(const float2 (*nb)[kTcWP], int Bk, int a, int b) {
+    return a >= b ? nb[a][4 * Bk + b] : nb[b][4 * Bk + a];
+}
+
+__device__ __forceinline__ void put_row8(float *op, int row, const float (&v)[8]) {
+    *(float4 *)&op[kmaj(row, 0)] = make_float4(v[0], v[1], v[2], v[3]);
+    *(float4 *)&op[kmaj(row, 4)] = make_float4(v[4], v[5], v[6], v[7]);
+}
+
+
+// named barrier 2: the panel threads hand a step's operands to the MMA warp
+__device__ __forceinline__ void handoff_arrive() { asm volatile("bar.arrive 2, 160;\n" ::: "memory"); }
+__device__ __forceinline__ void handoff_sync() { asm volatile("bar.sync 2, 160;\n" ::: "memory"); }
+
+// 4x4 complex-symmetric L L^T of the diagonal block (rows j..j+3; rows
+// beyond n get a unit pivot).  Returns the lower factor and 1/diag in
+// registers; *bad = 28 on a zero or non-finite pivot.
+__device__ __forceinline__ void diag_factor4(const float2 (&d0)[4][4], int j, int n, float2 (&Ld)[4][4],
+                                             float2 (&dinv)[4], int &bad) {
+    float2 dm[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) dm[r][q] = d0[r][q];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        float2 d;
+        if (j + q < n) {
+            const float2 v = dm[q][q];
+            const float r2 = v.x * v.x + v.y * v.y;
+            if (!(r2 > 0.f) || !isfinite(r2)) bad = 28;
+            d = csqrt_fast(v);
+        } else {
+            d = cf(1.f, 0.f);
+        }
+        const float2 di = crecip_fast(d);
+        Ld[q][q] = d;
+        dinv[q] = di;
+#pragma unroll
+        for (int r = q + 1; r < 4; r++) {
+            dm[r][q] = cmulf(dm[r][q], di);
+            Ld[r][q] = dm[r][q];
+        }
+#pragma unroll
+        for (int r = q + 1; r < 4; r++)
+#pragma unroll
+            for (int c = q + 1; c <= r; c++) dm[r][c] = cfmsf(dm[r][c], dm[r][q], dm[c][q]);
+#pragma unroll
+        for (int c = q + 1; c < 4; c++) Ld[q][c] = cf(0.f, 0.f);
+    }
+}
+
+// MMAs of one step over TMEM columns [c0, c0 + N): the rank-4 update as
+// three tf32 products and the injection of the entering rows
+__device__ __forceinline__ void issue_range(uint32_t tbase, const TcOperands &o, int c0, int N) {
+    const uint32_t idesc = tf32_idesc(kTcWP, N);
+    const uint32_t d = tbase + (uint32_t)c0;
+    const int boff = c0 * 8;  // floats: 8-row groups of 256 B
+    const uint64_t ah = smem_desc(o.a_hi), al = smem_desc(o.a_lo), ae = smem_desc(o.a_e);
+    const uint64_t bh = smem_desc(o.b_hi + boff), bl = smem_desc(o.b_lo + boff), be = smem_desc(o.b_e + boff);
+    tc_mma_tf32(d, ah, bh, idesc);
+    tc_mma_tf32(d, ah, bl, idesc);
+    tc_mma_tf32(d, al, bh, idesc);
+    tc_mma_tf32(d, ae, be, idesc);
+}
+
+}  // namespace
+
+__global__ __launch_bounds__(kTcThreads, 1) void k_factor_tc(DevProblem P, DevBatch B, int fuse) {
+    extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+    TcSmem &S = *reinterpret_cast<TcSmem *>(tc_smem_raw);
+    volatile int *abort_flag = &S.abort_flag;
+    const int n = P.n, mb = P.mb, Wb = mb + 1, rw = P.rw;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const bool is_panel = warp < 4, is_stage = warp == 4, is_mma = warp == 5;
+    const int nblk = (n + 3) / 4;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&S.tmem_base)),
+                     "r"(kTcCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = S.tmem_base;
+    const uint32_t tlane = tbase + ((uint32_t)(32 * (warp & 3)) << 16);  // this warp's lanes
+
+    bool stop = false;
+    for (int s = blockIdx.x; s < B.nsys && !stop; s += gridDim.x) {
+        float2 *L = (float2 *)B.L + (size_t)s * B.lpitch;
+        float2 *yv = (float2 *)B.y + (size_t)s * n;
+        const double2 *as = B.As + (size_t)s * P.nnz;
+        const double2 *bv = B.b + (size_t)s * n;
+        __syncthreads();
+        if (tid == 0) {
+            mbar_init(&S.bar_a, 1);
+            mbar_init(&S.bar_b, 1);
+            for (int q = 0; q < kTcNNB; q++) {
+                mbar_init(&S.bar_nbF[q], 1);
+                mbar_init(&S.bar_nbE[q], 4);
+            }
+            mbar_init_fence();
+            S.bad = 0;
+            S.abort_flag = 0;
+            S.panel_fail = 0;
+            S.stop_issue = 0;
+        }
+        for (int q = tid; q < kTcNNB * 4 * kTcWP; q += blockDim.x) (&S.nbuf[0][0][0])[q] = cf(0.f, 0.f);
+        if (tid < 4 * kTcNNB) S.bnew[tid / 4][tid % 4] = cf(0.f, 0.f);
+        __syncthreads();
+        // ---- initial window (rows 0..127) from the full symmetric pattern;
+        //      entering rows of steps 0..kTcNNB-1
+        float2 bsh = cf(0.f, 0.f);
+        if (is_panel) {
+            const int r = tid;
+            if (r < n && fuse) bsh = to_f(bv[r]);
+            const int f0 = r < n ? P.fptr[r] : 0, f1 = r < n ? P.fptr[r + 1] : 0;
+            for (int cb = 0; cb < kTcNB; cb++) {  // 4 slots = 8 columns per store
+                float v[8];
+#pragma unroll
+                for (int q = 0; q < 8; q++) v[q] = 0.f;
+                for (int f = f0; f < f1; f++) {
+                    const int c = P.fcol[f];
+                    if ((c >> 2) != cb) continue;
+                    const float2 a = to_f(as[P.fidx[f]]);
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if ((c & 3) == q) {
+                            v[2 * q] = a.x;
+                            v[2 * q + 1] = a.y;
+                        }
+                }
+                tmem_st8(tlane + 8 * cb, v);
+            }
+        } else if (is_stage) {
+            const int ln = lane;
+            for (int m = 0; m < kTcNNB; m++) {
+                const int r = ln >> 3, e0 = ln & 7, rr = 4 * m + kTcWP + r;
+                if (rr < n) {
+                    for (int e = e0; e < rw; e += 8) {
+                        const int c = P.col[(size_t)rr * rw + e];
+                        if (c >= 0) S.nbuf[m][r][c % kTcWP] = to_f(as[(size_t)rr * rw + e]);
+                    }
+                    if (e0 == 7 && fuse) S.bnew[m][r] = to_f(bv[rr]);
+                }
+            }
+            for (int q = 0; q < kStageSteps; q++) {
+                const int m = kTcNNB + q;
+                stage_issue4(P, as, bv, 4 * m + kTcWP, ln, rw, fuse, S.ring_val[m % kStageSteps],
+                             S.ring_col[m % kStageSteps], S.ring_b[m % kStageSteps]);
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+
+        if (is_panel) {
+            // ================= panel warps: one thread per slot =================
+            const int t = tid, b4 = t & 3, blk = t >> 2;
+            int Bk = 0, Bp = kTcNB - 1;
+            int issued = 0;  // steps handed to the MMA warp
+            int bad = 0;
+            for (int J = 0; J < nblk; J++) {
+                const int j = 4 * J, cn = J % kTcNNB, ob = J & 1;
+                bool ok = true;
+                if (J >= 1) {
+                    ok = __all_sync(0xffffffffu, mbar_wait_abort(&S.bar_a, (J - 1) & 1, abort_flag, 0u));
+                    tc_fence_after();
+                }
+                if (J >= kTcNNB)
+                    ok = __all_sync(0xffffffffu,
+                                    ok && mbar_wait_abort(&S.bar_nbF[cn], ((J - kTcNNB) / kTcNNB) & 1, abort_flag, 0u));
+                // pivot columns of this step (part (a) of the last step has landed)
+                float2 a[4], a0[4];
+                {
+                    float v[8];
+                    tmem_ld8(tlane + 8 * Bk, v);
+#pragma unroll
+                    for (int q = 0; q < 4; q++) a[q] = a0[q] = cf(v[2 * q], v[2 * q + 1]);
+                }
+                if (blk == Bk) {
+#pragma unroll
+                    for (int q = 0; q < 4; q++) S.dm[ob][b4][q] = a[q];
+                    S.bp[ob][b4] = bsh;
+                }
+                tc_fence_before();
+                if (panel_bar_or(!ok)) {  // the same decision in every panel thread
+                    if (t == 0) {
+                        S.panel_fail = 1;
+                        S.stop_issue = 1;
+                    }
+                    handoff_arrive();  // release the MMA warp, which then stops
+                    break;
+                }
+                // ---- 4x4 factor of the diagonal block (every thread, in registers)
+                float2 Ld[4][4], dinv[4];
+                {
+                    float2 d0[4][4];
+#pragma unroll
+                    for (int r = 0; r < 4; r++)
+#pragma unroll
+                        for (int q = 0; q < 4; q++) d0[r][q] = S.dm[ob][r][q];
+                    diag_factor4(d0, j, n, Ld, dinv, bad);
+                }
+                float2 ysh[4];
+                if (fuse) {  // forward substitution of the pivot rows' right-hand side
+                    float2 bb[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) bb[q] = S.bp[ob][q];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        ysh[q] = cmulf(bb[q], dinv[q]);
+#pragma unroll
+                        for (int r = q + 1; r < 4; r++) bb[r] = cfmsf(bb[r], Ld[r][q], ysh[q]);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (t == q && j + q < n) yv[j + q] = ysh[q];
+                }
+                // ---- L entries of this slot's row
+                float2 l[4];
+                if (blk == Bk) {
+                    if (j + b4 < n) {  // row j+b4 of the diagonal block factor
+                        float2 *row = L + (size_t)(j + b4) * Wb + (mb - b4);
+#pragma unroll
+                        for (int r = 0; r < 4; r++)
+                            if (r == b4) {
+#pragma unroll
+                                for (int q = 0; q <= r; q++)
+                                    if (mb - r + q >= 0) row[q] = Ld[r][q];
+                            }
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; q++) l[q] = cf(0.f, 0.f);
+                    bsh = fuse ? S.bnew[cn][b4] : cf(0.f, 0.f);  // the entering row's right-hand side
+                } else {
+                    int dist = t - 4 * Bk;
+                    if (dist < 0) dist += kTcWP;
+                    const int r_l = j + dist, band0 = dist - mb;
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const float2 x = cmulf(a[q], dinv[q]);
+#pragma unroll
+                        for (int r = q + 1; r < 4; r++) a[r] = cfmsf(a[r], x, Ld[r][q]);
+                        l[q] = x;
+                    }
+                    if (r_l < n && band0 < 4) {
+                        float2 *row = L + (size_t)r_l * Wb + (j - r_l + mb);  // column j
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            if (q >= band0) row[q] = l[q];
+                    }
+                    if (fuse) {
+#pragma unroll
+                        for (int q = 0; q < 4; q++) bsh = cfmsf(bsh, l[q], ysh[q]);
+                    }
+                }
+                // ---- MMA operands of this step (buffer ob)
+                {
+                    TcOperands &o = S.op[ob];
+                    float ah[8], al[8], bh0[8], bl0[8], bh1[8], bl1[8], ae[8], be0[8], be1[8];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const float re = l[q].x, im = l[q].y;
+                        const float reh = tf32_hi(re), imh = tf32_hi(im);
+                        ah[q] = reh;
+                        ah[4 + q] = imh;
+                        al[q] = re - reh;
+                        al[4 + q] = im - imh;
+                        bh0[q] = -reh;
+                        bh0[4 + q] = imh;
+                        bl0[q] = -(re - reh);
+                        bl0[4 + q] = im - imh;
+                        bh1[q] = -imh;
+                        bh1[4 + q] = -reh;
+                        bl1[q] = -(im - imh);
+                        bl1[4 + q] = -(re - reh);
+                        ae[q] = (blk == Bk && b4 == q) ? 1.f : 0.f;
+                        ae[4 + q] = ae[q];
+                        // new - old value of entering row q at this slot's column; the old
+                        // value D(pivot q, t) equals this thread's pivot entry a0[q] by symmetry
+                        const float2 nv = (blk == Bk) ? entering_pair(S.nbuf[cn], Bk, q, b4) : S.nbuf[cn][q][t];
+                        const float dr = nv.x - a0[q].x, di = nv.y - a0[q].y;
+                        const float drh = tf32_hi(dr), dih = tf32_hi(di);
+                        be0[q] = drh;
+                        be0[4 + q] = dr - drh;
+                        be1[q] = dih;
+                        be1[4 + q] = di - dih;
+                    }
+                    put_row8(o.a_hi, t, ah);
+                    put_row8(o.a_lo, t, al);
+                    put_row8(o.b_hi, 2 * t, bh0);
+                    put_row8(o.b_lo, 2 * t, bl0);
+                    put_row8(o.b_hi, 2 * t + 1, bh1);
+                    put_row8(o.b_lo, 2 * t + 1, bl1);
+                    put_row8(o.a_e, t, ae);
+                    put_row8(o.b_e, 2 * t, be0);
+                    put_row8(o.b_e, 2 * t + 1, be1);
+                }
+                // ---- the last step's MMAs have all landed: column part of the rows
+                //      that entered then (they are read by this step's MMAs)
+                if (J >= 1) {
+                    ok = __all_sync(0xffffffffu, mbar_wait_abort(&S.bar_b, (J - 1) & 1, abort_flag, 0u));
+                    tc_fence_after();
+                    if (ok) {
+                        const int cp = (J - 1) % kTcNNB;
+                        float v[8];
+#pragma unroll
+                        for (int b = 0; b < 4; b++) {
+                            // entries among the entering rows sit in the later row's pattern
+                            const float2 x = (blk == Bp) ? entering_pair(S.nbuf[cp], Bp, b, b4) : S.nbuf[cp][b][t];
+                            v[2 * b] = x.x;
+                            v[2 * b + 1] = x.y;
+                        }
+                        tmem_st8(tlane + 8 * Bp, v);
+                    }
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&S.bar_nbE[(J - 1) % kTcNNB]);
+                }
+                if (!ok) {
+                    if (t == 0) S.panel_fail = 1;
+                }
+                fence_proxy_async();
+                tc_fence_before();
+                handoff_arrive();
+                issued = J + 1;
+                Bp = Bk;
+                Bk = (Bk + 1 == kTcNB) ? 0 : Bk + 1;
+            }
+            // the MMAs issued last must land before the next system or the dealloc
+            if (issued > 0) {
+                mbar_wait(&S.bar_b, (issued - 1) & 1);
+                tc_fence_after();
+            }
+            if (issued == nblk) {
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&S.bar_nbE[(nblk - 1) % kTcNNB]);
+            }
+            if (bad) S.bad = bad;
+        } else if (is_stage) {
+            // ================= staging warp =================
+            const int ln = lane;
+            for (int J = 0; J < nblk; J++) {
+                const int cn = J % kTcNNB, m = J + kTcNNB;  // refill buffer cn with step m
+                const bool ok = mbar_wait_abort(&S.bar_nbE[cn], (J / kTcNNB) & 1, abort_flag);
+                if (!__all_sync(0xffffffffu, ok)) break;
+                for (int q = ln; q < kTcWP; q += 32) {
+#pragma unroll
+                    for (int r = 0; r < 4; r++) S.nbuf[cn][r][q] = cf(0.f, 0.f);
+                }
+                if (ln < 4) S.bnew[cn][ln] = cf(0.f, 0.f);
+                __syncwarp();
+                const int sl = m % kStageSteps, r = ln >> 3, e0 = ln & 7;
+                const int rr = 4 * m + kTcWP + r;
+                cp_wait<kStageSteps - 1>();
+                __syncwarp();
+                if (rr < n) {
+                    for (int e = e0; e < rw; e += 8) {
+                        const int c = S.ring_col[sl][r][e];
+                        if (c >= 0) S.nbuf[cn][r][c % kTcWP] = to_f(S.ring_val[sl][r][e]);
+                    }
+                    if (e0 == 7 && fuse) S.bnew[cn][r] = to_f(S.ring_b[sl][r]);
+                }
+                __syncwarp();
+                stage_issue4(P, as, bv, 4 * (m + kStageSteps) + kTcWP, ln, rw, fuse, S.ring_val[sl], S.ring_col[sl],
+                             S.ring_b[sl]);
+                if (ln == 0) mbar_arrive(&S.bar_nbF[cn]);
+            }
+            cp_wait<0>();
+        } else if (is_mma) {
+            // ================= MMA warp =================
+            int Bn = 1 % kTcNB;
+            for (int J = 0; J < nblk; J++) {
+                handoff_sync();
+                if (S.stop_issue) break;
+                tc_fence_after();
+                if (lane == 0) {
+                    const TcOperands &o = S.op[J & 1];
+                    const int c0 = 16 * (Bn >> 1);  // 16 columns holding the next pivot block
+                    issue_range(tbase, o, c0, 16);
+                    tc_commit(&S.bar_a);
+                    if (c0 > 0) issue_range(tbase, o, 0, c0);
+                    if (c0 + 16 < kTcCols) issue_range(tbase, o, c0 + 16, kTcCols - c0 - 16);
+                    tc_commit(&S.bar_b);
+                }
+                __syncwarp();
+                Bn = (Bn + 1 == kTcNB) ? 0 : Bn + 1;
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            if (S.abort_flag || S.panel_fail) atomicCAS(&B.status[s], 0, ERR_TIMEOUT);
+            else if (S.bad) atomicCAS(&B.status[s], 0, S.bad);
+            mbar_inval(&S.bar_a);
+            mbar_inval(&S.bar_b);
+            for (int q = 0; q < kTcNNB; q++) {
+                mbar_inval(&S.bar_nbF[q]);
+                mbar_inval(&S.bar_nbE[q]);
+            }
+        }
+        stop = S.abort_flag || S.panel_fail;
+        __syncthreads();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tbase), "r"(kTcCols) : "memory");
+}
+
+int launch_factor_tc(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st) {
+    if (P.mb + 4 > kTcWP) return ERR_UNSUPPORTED;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_factor_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemRequest);
+        attr = true;
+    }
+    static_assert(sizeof(TcSmem) <= kTcSmemRequest, "shared memory layout exceeds the request");
+    const int grid = B.nsys < 2 * nsm ? B.nsys : 2 * nsm;
+    k_factor_tc<<<grid, kTcThreads, kTcSmemRequest, st>>>(P, B, fuse);
+    return 0;
+}
+
+}  // namespace crgpu
