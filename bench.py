@@ -91,28 +91,16 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def fp32_peak_tflops(torch):
-    """FP32 (SIMT) peak measured here with cuBLAS SGEMM, TF32 disabled."""
-    old = torch.backends.cuda.matmul.allow_tf32
-    torch.backends.cuda.matmul.allow_tf32 = False
-    n = 8192
-    a = torch.randn(n, n, device="cuda", dtype=torch.float32)
-    b = torch.randn(n, n, device="cuda", dtype=torch.float32)
-    for _ in range(2):
-        torch.matmul(a, b)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    best = 0.0
-    for _ in range(5):
-        e0.record()
-        torch.matmul(a, b)
-        e1.record()
-        torch.cuda.synchronize()
-        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
-    torch.backends.cuda.matmul.allow_tf32 = old
-    del a, b
-    torch.cuda.empty_cache()
-    return best
+def tensor_peak_tflops():
+    """Dense tensor peak for a kernel timed inside a long step: the sustained
+    bf16 figure of MEASURED_PEAKS.json (measured on this machine), else
+    the fallback measurement of 1.7 PFLOP/s."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["bf16_tflops_sustained"]), "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"
+    except (OSError, KeyError, ValueError):
+        return 1700.0, "fallback 1.7 PFLOP/s sustained bf16 (of fallback)"
 
 
 def read_profile_traffic(name: str):
@@ -312,14 +300,15 @@ def run_gpu(args):
     err_j = float(np.abs(sens_mixed - sens_plain).max() / np.abs(sens_plain).max())
     plain.close()
 
-    # ---- roofline of the dominant kernel (the mixed band factorisation)
+    # ---- roofline of the dominant kernel (the complex64 band factorisation on
+    #      the tensor cores); algorithmic work = complex L L^T of every system
     n, mb = g.sanz, g.mb
     nsys = K * sv.eanz
-    flops_factor = nsys * 4.0 * n * mb * mb  # complex LL^T, 8 flops per complex MAC
+    flops_factor = nsys * 4.0 * n * mb * mb  # 8 flops per complex multiply-add, n*mb^2/2 of them
     fac_avg_ms = statistics.mean(fac_ms)
     achieved = flops_factor / (fac_avg_ms * 1e-3) / 1e12
-    peak = fp32_peak_tflops(torch)
-    traffic = read_profile_traffic("k_factor_mixed_cfg2.txt")
+    peak, peak_source = tensor_peak_tflops()
+    traffic = read_profile_traffic("k_factor_tc_cfg2.txt")
     line = {
         "metric": METRIC, "value": value, "unit": "units/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -342,11 +331,12 @@ def run_gpu(args):
         "mixed_vs_plain_rel_err": {"volt": err_v, "jacobian": err_j},
         "phases_ms": {"factor": fac_avg_ms, "solve": mixed_stats["ms_solve"],
                       "forward": mixed_stats["ms_forward"], "sens": statistics.mean(sens_ms)},
-        "roofline": {"kernel": "k_factor_mixed", "bound": "fp32", "achieved": achieved, "peak": peak,
+        "roofline": {"kernel": "k_factor_tc", "bound": "tensor", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
-                     "peak_source": "cuBLAS SGEMM (TF32 off) measured in this run; MEASURED_PEAKS.json "
-                                    "has no FP32 SIMT figure",
-                     "algorithmic": "4*n*mb^2 flops per system (complex LL^T)"},
+                     "peak_source": peak_source,
+                     "algorithmic": "4*n*mb^2 flops per band system (complex L L^T), all systems of one forward",
+                     "note": "latency-bound band factor: each 4-column step is a serial panel plus 4 tf32 MMAs "
+                             "(3 hi/lo products + row injection) on a 128x128 complex window"},
     }
     if rank == 0 and args.cpu_baseline:
         kpot = mixed.forward(s.sigma, kpot=True)["kpot"]
