@@ -154,6 +154,19 @@ int crgpu_factor_system(crgpu_ctx *ctx, const double *sigma, int32_t k, int32_t 
 int crgpu_factor_system_noalloc(crgpu_ctx *ctx, const void *sigma_device, int32_t k, int32_t l,
                                 void *a_device, void *fak_device, void *stream);
 
+/* No single counterpart in the reference, which forms the Jacobian with
+ * src/bsensi.f90 (reciprocity, no mixed-boundary term) and applies J^H in
+ * src/update.f90.  The exact derivative of L = sum_i g_i V_i, the voltages
+ * of the last crgpu_forward (V of src/bvolt.f90, before kfak or log), with
+ * respect to sigma: one adjoint solve per (k, l) system that reuses the
+ * forward's band factors (refactored batch by batch when the systems did not
+ * fit in one batch) and an element-wise contraction with the element and
+ * mixed-boundary matrices.  V is holomorphic in sigma, so grad_e =
+ * sum_i g_i dV_i/dsigma_e.  Not available with singularity removal (1002).
+ *   g    : nanz complex;  grad : elanz complex */
+int crgpu_adjoint(crgpu_ctx *ctx, const double *g, double *grad);
+int crgpu_adjoint_device(crgpu_ctx *ctx, const void *g_device, void *grad_device);
+
 /* ------------------------------------------------------------------ */
 /* inversion update                                                     */
 /* ------------------------------------------------------------------ */
@@ -201,6 +214,7 @@ typedef struct {
     int32_t refine_iterations;
     int32_t nsystems, nbatches;
     double refine_last_correction;
+    double ms_adjoint;
 } crgpu_stats;
 int crgpu_get_stats(const crgpu_ctx *ctx, crgpu_stats *stats);
 

@@ -29,6 +29,7 @@ EXPORTS = (
     "crgpu_set_memory_budget", "crgpu_forward", "crgpu_forward_device", "crgpu_sens",
     "crgpu_sens_device", "crgpu_device_buffers", "crgpu_factor_system", "crgpu_update",
     "crgpu_rwaven", "crgpu_cutmck", "crgpu_bkfak", "crgpu_get_stats", "crgpu_factor_system_noalloc",
+    "crgpu_adjoint", "crgpu_adjoint_device",
 )
 
 
@@ -51,7 +52,7 @@ class CStats(C.Structure):
                 ("ms_factor", C.c_double), ("ms_solve", C.c_double), ("ms_sens", C.c_double),
                 ("ms_update", C.c_double), ("refine_iterations", C.c_int32),
                 ("nsystems", C.c_int32), ("nbatches", C.c_int32),
-                ("refine_last_correction", C.c_double)]
+                ("refine_last_correction", C.c_double), ("ms_adjoint", C.c_double)]
 
 
 def lib() -> C.CDLL:

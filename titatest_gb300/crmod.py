@@ -184,6 +184,21 @@ class CRMod:
     def bsensi(self) -> np.ndarray:
         return self.sens(1)
 
+    def adjoint(self, g) -> np.ndarray:
+        """Exact dL/dsigma (elanz complex128) of L = sum_i g_i V_i, V the
+        voltages of the last forward, by adjoint solves that reuse the
+        forward's band factors (crgpu_adjoint)."""
+        gg = np.ascontiguousarray(g, np.complex128)
+        if gg.shape != (self.survey.nanz,):
+            raise ValueError(f"g must have shape ({self.survey.nanz},)")
+        out = np.zeros(self.grid.elanz, np.complex128)
+        _check(self._h, lib().crgpu_adjoint(self._h, ptr(gg, f64p), ptr(out, f64p)))
+        return out
+
+    def adjoint_device(self, g_ptr: int, grad_ptr: int):
+        """crgpu_adjoint_device on device pointers (nanz and elanz complex128)."""
+        _check(self._h, lib().crgpu_adjoint_device(self._h, C.c_void_p(g_ptr), C.c_void_p(grad_ptr)))
+
     def sens_device(self, mode: int, sens_ptr: int):
         _check(self._h, lib().crgpu_sens_device(self._h, int(mode), C.c_void_p(sens_ptr)))
 

@@ -128,24 +128,9 @@ int check_device_errors(crgpu_ctx *c, const int *d_status, int nsys) {
     return 0;
 }
 
-// the forward block on device-resident sigma
-int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const double *d_kfak, double2 *d_volt,
-                double2 *d_sigmaa) {
-    DevProblem &P = c->P;
-    c->stats = crgpu_stats{};
-    cudaEvent_t ev[4];
-    for (auto &e : ev) cudaEventCreate(&e);
-    cudaEventRecord(ev[0], c->st);
-    CUCHECK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
-    launch_adom(P, d_sigma, c->d_adom, c->st);
-    c->stats.kernel_launches += 1;
-    if (c->lsr) {
-        launch_refsig(P, d_sigma, c->d_sigma0, c->st);
-        c->stats.kernel_launches += 1;
-    }
-    const bool mixed = c->precision == CRGPU_MIXED;
+// systems per batch under the memory budget (at least one)
+int batch_size(crgpu_ctx *c) {
     const int nsys_total = (int)c->sys_k.size();
-    // batch size from the memory budget
     size_t per = bytes_per_system(c);
     int64_t budget = c->mem_budget;
     if (budget <= 0) {
@@ -155,6 +140,121 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
     }
     int bs = (int)std::max<int64_t>(1, std::min<int64_t>(nsys_total, budget / (int64_t)per));
     if (c->batch_cap > 0 && c->batch_cap < bs && c->batch_cap >= nsys_total) bs = c->batch_cap;
+    return bs;
+}
+
+// the batch of systems s0 .. s0+ns-1
+DevBatch batch_view(crgpu_ctx *c, int ns) {
+    DevBatch B = c->Bmax;
+    B.nsys = ns;
+    B.ks = c->d_ks;
+    B.ls = c->d_ls;
+    return B;
+}
+
+int load_batch(crgpu_ctx *c, int s0, int ns) {
+    CUCHECK(c, cudaMemcpyAsync(c->d_ks, c->sys_k.data() + s0, sizeof(int32_t) * ns, cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemcpyAsync(c->d_ls, c->sys_l.data() + s0, sizeof(int32_t) * ns, cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemsetAsync(c->Bmax.status, 0, sizeof(int) * ns, c->st));
+    return 0;
+}
+
+// Solves the ns systems of the current batch, whose band factors are in
+// B.L, for the right-hand sides in B.b (src/vre.f90); the forward sweep was
+// already done inside the factorisation when fused.  Mixed precision adds the
+// FP64 refinement.  The FP64 solution ends in B.x.
+int solve_batch(crgpu_ctx *c, int ns, bool fused) {
+    DevProblem &P = c->P;
+    const bool mixed = c->precision == CRGPU_MIXED;
+    const int nr = c->nrhs;
+    DevBatch B = batch_view(c, ns);
+    DevBatch Bs = B;
+    Bs.active = nullptr;
+    if (!fused) {
+        launch_forward_solve(P, Bs, nr, mixed, B.b, c->st);
+        c->stats.kernel_launches += 1;
+    }
+    launch_back_solve(P, Bs, nr, mixed, c->st);
+    c->stats.kernel_launches += 1;
+    if (!mixed) {
+        launch_copy_solution(P, B, nr, c->st);
+        c->stats.kernel_launches += 1;
+        return 0;
+    }
+    // all items active: a host array of ones (a memset cannot write int 1)
+    std::vector<int> ones((size_t)ns * nr, 1);
+    CUCHECK(c, cudaMemcpyAsync(B.active, ones.data(), sizeof(int) * ones.size(), cudaMemcpyHostToDevice, c->st));
+    DevBatch B0 = B;
+    B0.zmax = nullptr;
+    B0.nactive = nullptr;
+    launch_accumulate(P, B0, nr, true, c->refine_tol, c->st);
+    c->stats.kernel_launches += 1;
+    for (int it = 0; it < c->refine_maxit; it++) {
+        CUCHECK(c, cudaMemsetAsync(B.nactive, 0, 2 * sizeof(double), c->st));
+        launch_residual(P, B, nr, c->st);
+        launch_forward_solve(P, B, nr, true, B.r, c->st);
+        launch_back_solve(P, B, nr, true, c->st);
+        launch_accumulate(P, B, nr, false, c->refine_tol, c->st);
+        c->stats.kernel_launches += 4;
+        c->stats.refine_iterations = std::max(c->stats.refine_iterations, it + 1);
+        struct {
+            int n;
+            int pad;
+            double z;
+        } h{};
+        CUCHECK(c, cudaMemcpyAsync(&h, B.nactive, sizeof(h), cudaMemcpyDeviceToHost, c->st));
+        CUCHECK(c, cudaStreamSynchronize(c->st));
+        c->last_refine_zmax = h.z;
+        c->stats.refine_last_correction = h.z;
+        if (h.n == 0) break;
+    }
+    return 0;
+}
+
+// assembly and scaling (src/kompab.f90, src/scalab.f90) of the current batch
+int assemble_batch(crgpu_ctx *c, const double2 *d_sigma, int ns) {
+    DevProblem &P = c->P;
+    DevBatch B = batch_view(c, ns);
+    launch_assemble(P, B, d_sigma, c->d_adom, c->st);
+    c->stats.kernel_launches += 2;
+    return 0;
+}
+
+// band factorisation of the current batch (src/chol.f90); with fuse the
+// forward sweep of the right-hand sides in B.b runs inside the factor
+int run_factor(crgpu_ctx *c, int ns, int fuse) {
+    DevBatch B = batch_view(c, ns);
+    if (c->precision == CRGPU_MIXED) {
+        int e = launch_factor_mixed(c->P, B, fuse, c->nsm, c->st);
+        if (e) return fail(c, e, "mixed precision: band width beyond the supported window");
+    } else {
+        launch_factor_plain(c->P, B, fuse, c->nsm, c->st);
+    }
+    c->stats.kernel_launches += 1;
+    return 0;
+}
+
+// the forward block on device-resident sigma
+int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const double *d_kfak, double2 *d_volt,
+                double2 *d_sigmaa) {
+    DevProblem &P = c->P;
+    c->stats = crgpu_stats{};
+    c->factors_resident = false;
+    cudaEvent_t ev[4];
+    for (auto &e : ev) cudaEventCreate(&e);
+    cudaEventRecord(ev[0], c->st);
+    CUCHECK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+    if (d_sigma != c->d_sigma)  // keep the model of this forward (adjoint, refactorisation)
+        CUCHECK(c, cudaMemcpyAsync(c->d_sigma, d_sigma, sizeof(double2) * c->hg.elanz, cudaMemcpyDeviceToDevice, c->st));
+    d_sigma = c->d_sigma;
+    launch_adom(P, d_sigma, c->d_adom, c->st);
+    c->stats.kernel_launches += 1;
+    if (c->lsr) {
+        launch_refsig(P, d_sigma, c->d_sigma0, c->st);
+        c->stats.kernel_launches += 1;
+    }
+    const int nsys_total = (int)c->sys_k.size();
+    const int bs = batch_size(c);
     int e = ensure_batch(c, bs);
     if (e) return e;
     c->stats.nsystems = nsys_total;
@@ -165,77 +265,26 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
     cudaEventCreate(&f2);
     int worst = 0;
     for (int s0 = 0; s0 < nsys_total; s0 += bs) {
-        int ns = std::min(bs, nsys_total - s0);
-        DevBatch B = c->Bmax;
-        B.nsys = ns;
-        B.ks = c->d_ks;
-        B.ls = c->d_ls;
-        CUCHECK(c, cudaMemcpyAsync(c->d_ks, c->sys_k.data() + s0, sizeof(int32_t) * ns, cudaMemcpyHostToDevice, c->st));
-        CUCHECK(c, cudaMemcpyAsync(c->d_ls, c->sys_l.data() + s0, sizeof(int32_t) * ns, cudaMemcpyHostToDevice, c->st));
-        CUCHECK(c, cudaMemsetAsync(B.status, 0, sizeof(int) * ns, c->st));
+        const int ns = std::min(bs, nsys_total - s0);
         const int nr = c->nrhs;
         const int fuse = nr == 1 ? 1 : 0;
-        launch_assemble(P, B, d_sigma, c->d_adom, c->st);
+        DevBatch B = batch_view(c, ns);
+        e = load_batch(c, s0, ns);
+        if (!e) e = assemble_batch(c, d_sigma, ns);
+        if (e) return e;
         if (c->lsr) {
             launch_pota_rhs(P, B, d_sigma, c->d_sigma0, c->lsink, c->nsink, c->st);
-            c->stats.kernel_launches += 5;
+            c->stats.kernel_launches += 3;
         } else {
             launch_rhs(P, B, nr, c->lsink, c->nsink, c->st);
-            c->stats.kernel_launches += 3;
+            c->stats.kernel_launches += 1;
         }
         cudaEventRecord(f0, c->st);
-        if (mixed) {
-            e = launch_factor_mixed(P, B, fuse, c->nsm, c->st);
-            if (e) return fail(c, e, "mixed precision: band width beyond the supported window");
-        } else {
-            launch_factor_plain(P, B, fuse, c->nsm, c->st);
-        }
-        c->stats.kernel_launches += 1;
+        e = run_factor(c, ns, fuse);
+        if (e) return e;
         cudaEventRecord(f1, c->st);
-        DevBatch Bs = B;
-        Bs.active = nullptr;
-        if (!fuse) {
-            launch_forward_solve(P, Bs, nr, mixed, B.b, c->st);
-            c->stats.kernel_launches += 1;
-        }
-        launch_back_solve(P, Bs, nr, mixed, c->st);
-        c->stats.kernel_launches += 1;
-        if (mixed) {
-            CUCHECK(c, cudaMemsetAsync(B.active, 0, sizeof(int) * ns * nr, c->st));
-            // all items active: fill with ones through a tiny memset pattern
-            std::vector<int> ones((size_t)ns * nr, 1);
-            CUCHECK(c, cudaMemcpyAsync(B.active, ones.data(), sizeof(int) * ones.size(), cudaMemcpyHostToDevice, c->st));
-            B.zmax = nullptr;
-            B.nactive = nullptr;
-            launch_accumulate(P, B, nr, true, c->refine_tol, c->st);
-            B = c->Bmax;
-            B.nsys = ns;
-            B.ks = c->d_ks;
-            B.ls = c->d_ls;
-            c->stats.kernel_launches += 1;
-            for (int it = 0; it < c->refine_maxit; it++) {
-                CUCHECK(c, cudaMemsetAsync(B.nactive, 0, 2 * sizeof(double), c->st));
-                launch_residual(P, B, nr, c->st);
-                launch_forward_solve(P, B, nr, true, B.r, c->st);
-                launch_back_solve(P, B, nr, true, c->st);
-                launch_accumulate(P, B, nr, false, c->refine_tol, c->st);
-                c->stats.kernel_launches += 4;
-                c->stats.refine_iterations = std::max(c->stats.refine_iterations, it + 1);
-                struct {
-                    int n;
-                    int pad;
-                    double z;
-                } h{};
-                CUCHECK(c, cudaMemcpyAsync(&h, B.nactive, sizeof(h), cudaMemcpyDeviceToHost, c->st));
-                CUCHECK(c, cudaStreamSynchronize(c->st));
-                c->last_refine_zmax = h.z;
-                c->stats.refine_last_correction = h.z;
-                if (h.n == 0) break;
-            }
-        } else {
-            launch_copy_solution(P, B, nr, c->st);
-            c->stats.kernel_launches += 1;
-        }
+        e = solve_batch(c, ns, fuse != 0);
+        if (e) return e;
         launch_kpot(P, B, nr, c->d_kpot, c->st);
         c->stats.kernel_launches += 1;
         cudaEventRecord(f2, c->st);
@@ -272,7 +321,73 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
     CUCHECK(c, cudaGetLastError());
     if (ce) return ce;
     c->have_forward = true;
+    c->factors_resident = c->stats.nbatches == 1;
     return 0;
+}
+
+// Exact derivative of L = sum_i g_i V_i (the voltages of the last forward)
+// with respect to sigma: lambda_(k,l) = A_(k,l)^{-1} c_l with the adjoint
+// sources c_l of the measurements, solved with the forward's band factors
+// (refactored batch by batch when the forward needed several batches), then
+// grad_e = -sum_(k,l) w_k/pi lambda^T (dA/dsigma_e) kpot.
+int run_adjoint(crgpu_ctx *c, const double2 *d_g, double2 *d_grad) {
+    DevProblem &P = c->P;
+    if (!c->have_forward) return fail(c, ERR_ARG, "adjoint before a forward");
+    if (c->lsr) return fail(c, ERR_UNSUPPORTED, "adjoint with singularity removal");
+    if (!c->d_lambda) {
+        int e = dalloc(c, &c->d_lambda, (size_t)c->K * c->eanz * c->hg.n);
+        if (!e) e = dalloc(c, &c->d_adjsrc, (size_t)c->eanz * c->hg.n);
+        if (e) return e;
+    }
+    cudaEvent_t a0, a1;
+    cudaEventCreate(&a0);
+    cudaEventCreate(&a1);
+    cudaEventRecord(a0, c->st);
+    CUCHECK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+    launch_adjoint_sources(P, d_g, c->d_adjsrc, c->lsink, c->nsink, c->st);
+    c->stats.kernel_launches += 2;
+    const int nsys_total = (int)c->sys_k.size();
+    const int nr = c->nrhs;
+    int e = 0;
+    if (c->factors_resident) {
+        DevBatch B = batch_view(c, nsys_total);
+        launch_adjoint_rhs(P, B, nr, c->d_adjsrc, c->st);
+        e = solve_batch(c, nsys_total, false);
+        if (e) return e;
+        launch_adjoint_lambda(P, B, nr, c->d_lambda, c->st);
+        c->stats.kernel_launches += 2;
+        e = check_device_errors(c, B.status, nsys_total);
+        if (e) return e;
+    } else {
+        const int bs = c->batch_cap;
+        for (int s0 = 0; s0 < nsys_total; s0 += bs) {
+            const int ns = std::min(bs, nsys_total - s0);
+            DevBatch B = batch_view(c, ns);
+            e = load_batch(c, s0, ns);
+            if (!e) e = assemble_batch(c, c->d_sigma, ns);
+            if (e) return e;
+            launch_adjoint_rhs(P, B, nr, c->d_adjsrc, c->st);
+            e = run_factor(c, ns, 0);
+            if (!e) e = solve_batch(c, ns, false);
+            if (e) return e;
+            launch_adjoint_lambda(P, B, nr, c->d_lambda, c->st);
+            c->stats.kernel_launches += 2;
+            e = check_device_errors(c, B.status, ns);
+            if (e) return e;
+        }
+        c->factors_resident = nsys_total <= bs;
+    }
+    launch_adjoint_grad(P, c->d_kpot, c->d_lambda, c->d_ebnd_ptr, c->d_ebnd_list, d_grad, c->st);
+    c->stats.kernel_launches += 1;
+    cudaEventRecord(a1, c->st);
+    e = check_device_errors(c, nullptr, 0);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a0, a1);
+    c->stats.ms_adjoint = ms;
+    cudaEventDestroy(a0);
+    cudaEventDestroy(a1);
+    CUCHECK(c, cudaGetLastError());
+    return e;
 }
 
 }  // namespace
@@ -398,6 +513,19 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
             }
         }
         if (!e) e = upload(c, &P.earea, area);
+    }
+    {
+        // mixed boundary elements (type 11) carried by each area element, for the adjoint
+        std::vector<int32_t> ptr(hg.elanz + 1, 0), lst;
+        for (int rb = 0; rb < hg.relanz; rb++)
+            if (hg.btype[rb] == 11) ptr[hg.brnr[rb] + 1]++;
+        for (int q = 0; q < hg.elanz; q++) ptr[q + 1] += ptr[q];
+        lst.assign(std::max(ptr[hg.elanz], 1), 0);
+        std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
+        for (int rb = 0; rb < hg.relanz; rb++)
+            if (hg.btype[rb] == 11) lst[fill[hg.brnr[rb]]++] = rb;
+        if (!e) e = upload(c, &c->d_ebnd_ptr, ptr);
+        if (!e) e = upload(c, &c->d_ebnd_list, lst);
     }
     if (!e) e = dalloc(c, &c->d_sigma0, 1);
     if (!e) e = dalloc(c, &P.elbg, (size_t)c->K * hg.elanz * 10);
@@ -545,6 +673,26 @@ int crgpu_sens(crgpu_ctx *c, int32_t mode, double *sens) {
     return 0;
 }
 
+int crgpu_adjoint_device(crgpu_ctx *c, const void *g_device, void *grad_device) {
+    if (!c || !g_device || !grad_device) return ERR_ARG;
+    return run_adjoint(c, (const double2 *)g_device, (double2 *)grad_device);
+}
+
+int crgpu_adjoint(crgpu_ctx *c, const double *g, double *grad) {
+    if (!c || !g || !grad) return ERR_ARG;
+    if (!c->d_adjg) {
+        int e = dalloc(c, &c->d_adjg, (size_t)std::max(c->nanz, 1));
+        if (!e) e = dalloc(c, &c->d_adjgrad, (size_t)std::max(c->hg.elanz, 1));
+        if (e) return e;
+    }
+    CUCHECK(c, cudaMemcpyAsync(c->d_adjg, g, sizeof(double2) * c->nanz, cudaMemcpyHostToDevice, c->st));
+    int e = run_adjoint(c, c->d_adjg, c->d_adjgrad);
+    if (e) return e;
+    CUCHECK(c, cudaMemcpyAsync(grad, c->d_adjgrad, sizeof(double2) * c->hg.elanz, cudaMemcpyDeviceToHost, c->st));
+    CUCHECK(c, cudaStreamSynchronize(c->st));
+    return 0;
+}
+
 int crgpu_device_buffers(crgpu_ctx *c, void **kpot_device, void **hpot_device) {
     if (!c) return ERR_ARG;
     if (kpot_device) *kpot_device = c->d_kpot;
@@ -554,6 +702,7 @@ int crgpu_device_buffers(crgpu_ctx *c, void **kpot_device, void **hpot_device) {
 
 int crgpu_factor_system(crgpu_ctx *c, const double *sigma, int32_t k, int32_t l, double *a, double *fak) {
     if (!c || !sigma || k < 1 || k > c->K || l < 1 || l > c->eanz) return ERR_ARG;
+    c->factors_resident = false;  // system 0's factor is overwritten below
     const int n = c->hg.n, W = c->hg.mb + 1;
     CUCHECK(c, cudaMemcpyAsync(c->d_sigma, sigma, c->hg.elanz * sizeof(double2), cudaMemcpyHostToDevice, c->st));
     CUCHECK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));

@@ -36,6 +36,10 @@ struct crgpu_ctx {
     double last_refine_zmax = 0.0;
     int64_t mem_budget = 0;
     bool have_forward = false;
+    bool factors_resident = false;  // band factors of every system still in Bmax (one batch)
+    // adjoint
+    double2 *d_lambda = nullptr, *d_adjsrc = nullptr, *d_adjg = nullptr, *d_adjgrad = nullptr;
+    const int32_t *d_ebnd_ptr = nullptr, *d_ebnd_list = nullptr;  // element -> mixed boundary elements
     std::string last_error;
     crgpu_stats stats{};
     // update work space and the sensitivities it uses

@@ -52,6 +52,14 @@ void launch_bvolt(const DevProblem &P, const double2 *hpot, int mode, const doub
 void launch_bsens(const DevProblem &P, const double2 *kpot, const double2 *sigma,
                   const double2 *volt, int mode, bool single, double2 *sens, cudaStream_t st);
 
+// adjoint of the forward block (adjoint.cu)
+void launch_adjoint_sources(const DevProblem &P, const double2 *g, double2 *src, int lsink, int nsink,
+                            cudaStream_t st);
+void launch_adjoint_rhs(const DevProblem &P, const DevBatch &B, int nrhs, const double2 *src, cudaStream_t st);
+void launch_adjoint_lambda(const DevProblem &P, const DevBatch &B, int nrhs, double2 *lambda, cudaStream_t st);
+void launch_adjoint_grad(const DevProblem &P, const double2 *kpot, const double2 *lambda, const int32_t *ebnd_ptr,
+                         const int32_t *ebnd_list, double2 *grad, cudaStream_t st);
+
 // update / CG (src/update.f90, src/cg_mod.f90); all pointers device memory
 struct CGArgs {
     int nanz, manz, ltri, nx, maxnk, ncgmax;
