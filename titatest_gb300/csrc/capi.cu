@@ -31,7 +31,9 @@ template <typename T>
 int dalloc(crgpu_ctx *c, T **p, size_t count) {
     void *q = nullptr;
     if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+    // stream-ordered: no device-wide synchronisation on free, so contexts on
+    // different streams (ensembles) do not serialise each other
+    cudaError_t e = cudaMallocAsync(&q, count * sizeof(T), c->st);
     if (e != cudaSuccess) return fail(c, 94, std::string("device allocation: ") + cudaGetErrorString(e));
     c->allocs.push_back(q);
     *p = (T *)q;
@@ -57,7 +59,7 @@ void free_batch(crgpu_ctx *c) {
                     c->Bmax.potmax, c->d_ks, c->d_ls};
     for (void *p : ptrs)
         if (p) {
-            cudaFree(p);
+            cudaFreeAsync(p, c->st);
             c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), p), c->allocs.end());
         }
     c->Bmax = DevBatch{};
@@ -575,8 +577,8 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
 
 int crgpu_destroy(crgpu_ctx *c) {
     if (!c) return 0;
-    for (void *p : c->allocs) cudaFree(p);
-    if (c->d_upd) cudaFree(c->d_upd);
+    for (void *p : c->allocs) cudaFreeAsync(p, c->st);
+    if (c->d_upd) cudaFreeAsync(c->d_upd, c->st);
     if (c->own_st) cudaStreamDestroy(c->own_st);
     delete c;
     return 0;
@@ -836,10 +838,10 @@ int crgpu_update(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, const 
     const size_t o_cg = take(sizeof(double) * manz);
     const size_t o_work = take(update_work_bytes(nanz, manz));
     if (c->upd_bytes < off) {
-        if (c->d_upd) cudaFree(c->d_upd);
+        if (c->d_upd) cudaFreeAsync(c->d_upd, c->st);
         c->d_upd = nullptr;
         c->upd_bytes = 0;
-        cudaError_t e = cudaMalloc(&c->d_upd, off);
+        cudaError_t e = cudaMallocAsync(&c->d_upd, off, c->st);
         if (e != cudaSuccess) return fail(c, 94, std::string("update work space: ") + cudaGetErrorString(e));
         c->upd_bytes = off;
     }

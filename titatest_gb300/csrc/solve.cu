@@ -7,6 +7,8 @@
 // the working vector lives in a shared window.  Per block the dependent
 // chain is one warp reduction (forward) and an 8-step triangle of shuffles;
 // the rest is independent multiply-adds over the lanes' columns.
+#include <mutex>
+
 #include "async.cuh"
 #include "bulk.cuh"
 #include "crgpu_internal.h"
@@ -290,16 +292,20 @@ __global__ __launch_bounds__(32) void k_bwd(DevProblem P, DevBatch B, int nrhs, 
     cp_wait<0>();
 }
 
+// The kernels' dynamic shared memory depends on the band width; contexts of
+// different widths may launch concurrently from several host threads, so the
+// limit is raised once to the device's opt-in maximum instead of per width.
 template <typename T>
 static int set_solve_smem(int W, int WW) {
-    static int done = -1;
-    const int bytes = solve_layout<T>(W, WW).total;
-    if (done != bytes) {
-        cudaFuncSetAttribute(k_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        cudaFuncSetAttribute(k_bwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        done = bytes;
-    }
-    return bytes;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0, optin = 48 * 1024;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaFuncSetAttribute(k_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_bwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    });
+    return solve_layout<T>(W, WW).total;
 }
 
 void launch_forward_solve(const DevProblem &P, const DevBatch &B, int nrhs, bool mixed, const double2 *rin,

@@ -37,6 +37,8 @@
 // a step's operands (named barrier 2).  Every mbarrier wait is bounded in
 // time and failures are agreed on by a barrier reduction, so all roles leave
 // together.
+#include <mutex>
+
 #include "bulk.cuh"
 #include "crgpu_internal.h"
 #include "device.cuh"
@@ -582,11 +584,10 @@ __global__ __launch_bounds__(kTcThreads, 1) void k_factor_tc(DevProblem P, DevBa
 
 int launch_factor_tc(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st) {
     if (P.mb + 4 > kTcWP) return ERR_UNSUPPORTED;
-    static bool attr = false;
-    if (!attr) {
+    static std::once_flag once;
+    std::call_once(once, [] {
         cudaFuncSetAttribute(k_factor_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemRequest);
-        attr = true;
-    }
+    });
     static_assert(sizeof(TcSmem) <= kTcSmemRequest, "shared memory layout exceeds the request");
     const int grid = B.nsys < 2 * nsm ? B.nsys : 2 * nsm;
     k_factor_tc<<<grid, kTcThreads, kTcSmemRequest, st>>>(P, B, fuse);
