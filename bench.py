@@ -398,7 +398,8 @@ def main():
     ap.add_argument("--config", type=int, default=2)
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--refine-maxit", type=int, default=8)
-    ap.add_argument("--refine-tol", type=float, default=1e-6)
+    ap.add_argument("--refine-tol", type=float, default=1e-3,
+                    help="mixed refinement stop: max|dx| <= tol max|x| (1e-3 keeps volt within ~1e-8 of complex128)")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--workers", type=int, default=8, help="config 5: concurrent worker streams")
