@@ -160,6 +160,14 @@ def cpu_baseline(s, kwn, kwnwi, kpot, target_s=12.0, threads=None):
             "seconds_per_unit": unit_s, "forward_s": fwd_per_unit, "sens_s": sens_per_unit}
 
 
+def workload_string(cfg: int, s, K: int) -> str:
+    g, sv = s.grid, s.survey
+    kind = "triangles" if getattr(s, "triangles", False) else "quads"
+    nsys = K * sv.eanz
+    return (f"config{cfg}: {g.elanz} {kind}, {g.sanz} nodes, mb={g.mb}, {sv.eanz} electrodes, "
+            f"{sv.nanz} quadrupoles, {K} wavenumbers ({nsys} band systems)")
+
+
 def run_reference(args):
     rank, world, _ = _dist_env()
     if rank != 0:
@@ -182,9 +190,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
             "data": "synthetic (seeded)",
-            "config": {"workload": f"config{args.config}: {s.grid.elanz} elements, {s.grid.sanz} nodes, "
-                                   f"mb={s.grid.mb}, {s.survey.eanz} electrodes, {s.survey.nanz} quadrupoles, "
-                                   f"{len(kwn)} wavenumbers",
+            "config": {"workload": workload_string(args.config, s, len(kwn)),
                        "parallelism": f"OpenMP {cb['cores']} threads"},
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "units/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -314,8 +320,7 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64 factor + f64 refinement (c128 assembly, residuals, quadrature, J)",
         "data": "synthetic (seeded model and survey with the configuration's shapes)",
-        "config": {"workload": f"config{args.config}: {g.elanz} quads, {n} nodes, mb={mb}, {sv.eanz} electrodes, "
-                               f"{nanz} quadrupoles, {K} wavenumbers ({nsys} band systems)",
+        "config": {"workload": workload_string(args.config, s, K),
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (band factors of all systems, ~%d GB)" % int(
                        nsys * n * (mb + 1) * 8 / 1e9),
