@@ -183,41 +183,35 @@ __device__ __forceinline__ void put_row8(float *op, int row, const float (&v)[8]
 __device__ __forceinline__ void handoff_arrive() { asm volatile("bar.arrive 2, 160;\n" ::: "memory"); }
 __device__ __forceinline__ void handoff_sync() { asm volatile("bar.sync 2, 160;\n" ::: "memory"); }
 
-// 4x4 complex-symmetric L L^T of the diagonal block (rows j..j+3; rows
-// beyond n get a unit pivot).  Returns the lower factor and 1/diag in
-// registers; *bad = 28 on a zero or non-finite pivot.
-__device__ __forceinline__ void diag_factor4(const float2 (&d0)[4][4], int j, int n, float2 (&Ld)[4][4],
-                                             float2 (&dinv)[4], int &bad) {
+// L D L^T of the 4x4 pivot block (rows j..j+3, complex symmetric; rows
+// beyond n get a unit pivot): unit lower Lu, d and 1/d.  The only
+// operations on the step's critical path; the square roots for the stored
+// Cholesky factor Lc = Lu D^{1/2} come after the MMAs are issued.
+__device__ __forceinline__ void pivot_ldlt(const float2 (&a)[4][4], int j, int n, float2 (&Lu)[4][4],
+                                           float2 (&dv)[4], float2 (&dinv)[4], int &bad) {
     float2 dm[4][4];
 #pragma unroll
     for (int r = 0; r < 4; r++)
 #pragma unroll
-        for (int q = 0; q < 4; q++) dm[r][q] = d0[r][q];
+        for (int q = 0; q < 4; q++) dm[r][q] = a[r][q];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-        float2 d;
-        if (j + q < n) {
-            const float2 v = dm[q][q];
-            const float r2 = v.x * v.x + v.y * v.y;
-            if (!(r2 > 0.f) || !isfinite(r2)) bad = 28;
-            d = csqrt_fast(v);
-        } else {
+        float2 d = dm[q][q];
+        if (j + q >= n) {
             d = cf(1.f, 0.f);
+        } else {
+            const float r2 = d.x * d.x + d.y * d.y;
+            if (!(r2 > 0.f) || !isfinite(r2)) bad = 28;
         }
         const float2 di = crecip_fast(d);
-        Ld[q][q] = d;
+        dv[q] = d;
         dinv[q] = di;
 #pragma unroll
-        for (int r = q + 1; r < 4; r++) {
-            dm[r][q] = cmulf(dm[r][q], di);
-            Ld[r][q] = dm[r][q];
-        }
+        for (int r = q + 1; r < 4; r++) Lu[r][q] = cmulf(dm[r][q], di);
 #pragma unroll
         for (int r = q + 1; r < 4; r++)
 #pragma unroll
-            for (int c = q + 1; c <= r; c++) dm[r][c] = cfmsf(dm[r][c], dm[r][q], dm[c][q]);
-#pragma unroll
-        for (int c = q + 1; c < 4; c++) Ld[q][c] = cf(0.f, 0.f);
+            for (int c = q + 1; c <= r; c++) dm[r][c] = cfmsf(dm[r][c], Lu[r][q], dm[c][q]);
     }
 }
 
@@ -237,7 +231,7 @@ __device__ __forceinline__ void issue_range(uint32_t tbase, const TcOperands &o,
 
 }  // namespace
 
-__global__ __launch_bounds__(kTcThreads, 1) void k_factor_tc(DevProblem P, DevBatch B, int fuse) {
+__global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBatch B, int fuse) {
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
     TcSmem &S = *reinterpret_cast<TcSmem *>(tc_smem_raw);
     volatile int *abort_flag = &S.abort_flag;
@@ -365,67 +359,34 @@ __global__ __launch_bounds__(kTcThreads, 1) void k_factor_tc(DevProblem P, DevBa
                     handoff_arrive();  // release the MMA warp, which then stops
                     break;
                 }
-                // ---- 4x4 factor of the diagonal block (every thread, in registers)
-                float2 Ld[4][4], dinv[4];
+                // ---- L D L^T of the pivot block (every thread, in registers)
+                float2 Lu[4][4], dv[4], dinv[4];
                 {
                     float2 d0[4][4];
 #pragma unroll
                     for (int r = 0; r < 4; r++)
 #pragma unroll
                         for (int q = 0; q < 4; q++) d0[r][q] = S.dm[ob][r][q];
-                    diag_factor4(d0, j, n, Ld, dinv, bad);
+                    pivot_ldlt(d0, j, n, Lu, dv, dinv, bad);
                 }
-                float2 ysh[4];
-                if (fuse) {  // forward substitution of the pivot rows' right-hand side
-                    float2 bb[4];
+                float2 bpiv[4];
 #pragma unroll
-                    for (int q = 0; q < 4; q++) bb[q] = S.bp[ob][q];
-#pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        ysh[q] = cmulf(bb[q], dinv[q]);
-#pragma unroll
-                        for (int r = q + 1; r < 4; r++) bb[r] = cfmsf(bb[r], Ld[r][q], ysh[q]);
-                    }
-#pragma unroll
-                    for (int q = 0; q < 4; q++)
-                        if (t == q && j + q < n) yv[j + q] = ysh[q];
-                }
-                // ---- L entries of this slot's row
-                float2 l[4];
+                for (int q = 0; q < 4; q++) bpiv[q] = S.bp[ob][q];
+                // ---- m = a Lu^{-T} and l = m D^{-1} of this slot's row (zero for the pivot rows)
+                float2 m[4], l[4];
+                int dist = t - 4 * Bk;
+                if (dist < 0) dist += kTcWP;
                 if (blk == Bk) {
-                    if (j + b4 < n) {  // row j+b4 of the diagonal block factor
-                        float2 *row = L + (size_t)(j + b4) * Wb + (mb - b4);
 #pragma unroll
-                        for (int r = 0; r < 4; r++)
-                            if (r == b4) {
-#pragma unroll
-                                for (int q = 0; q <= r; q++)
-                                    if (mb - r + q >= 0) row[q] = Ld[r][q];
-                            }
-                    }
-#pragma unroll
-                    for (int q = 0; q < 4; q++) l[q] = cf(0.f, 0.f);
-                    bsh = fuse ? S.bnew[cn][b4] : cf(0.f, 0.f);  // the entering row's right-hand side
+                    for (int q = 0; q < 4; q++) m[q] = l[q] = cf(0.f, 0.f);
                 } else {
-                    int dist = t - 4 * Bk;
-                    if (dist < 0) dist += kTcWP;
-                    const int r_l = j + dist, band0 = dist - mb;
 #pragma unroll
                     for (int q = 0; q < 4; q++) {
-                        const float2 x = cmulf(a[q], dinv[q]);
+                        float2 x = a[q];
 #pragma unroll
-                        for (int r = q + 1; r < 4; r++) a[r] = cfmsf(a[r], x, Ld[r][q]);
-                        l[q] = x;
-                    }
-                    if (r_l < n && band0 < 4) {
-                        float2 *row = L + (size_t)r_l * Wb + (j - r_l + mb);  // column j
-#pragma unroll
-                        for (int q = 0; q < 4; q++)
-                            if (q >= band0) row[q] = l[q];
-                    }
-                    if (fuse) {
-#pragma unroll
-                        for (int q = 0; q < 4; q++) bsh = cfmsf(bsh, l[q], ysh[q]);
+                        for (int p = 0; p < q; p++) x = cfmsf(x, m[p], Lu[q][p]);
+                        m[q] = x;
+                        l[q] = cmulf(x, dinv[q]);
                     }
                 }
                 // ---- MMA operands of this step (buffer ob)
@@ -434,12 +395,13 @@ __global__ __launch_bounds__(kTcThreads, 1) void k_factor_tc(DevProblem P, DevBa
                     float ah[8], al[8], bh0[8], bl0[8], bh1[8], bl1[8], ae[8], be0[8], be1[8];
 #pragma unroll
                     for (int q = 0; q < 4; q++) {
-                        const float re = l[q].x, im = l[q].y;
+                        const float mr = m[q].x, mi = m[q].y, re = l[q].x, im = l[q].y;
+                        const float mrh = tf32_hi(mr), mih = tf32_hi(mi);
                         const float reh = tf32_hi(re), imh = tf32_hi(im);
-                        ah[q] = reh;
-                        ah[4 + q] = imh;
-                        al[q] = re - reh;
-                        al[4 + q] = im - imh;
+                        ah[q] = mrh;
+                        ah[4 + q] = mih;
+                        al[q] = mr - mrh;
+                        al[4 + q] = mi - mih;
                         bh0[q] = -reh;
                         bh0[4 + q] = imh;
                         bl0[q] = -(re - reh);
@@ -497,6 +459,60 @@ __global__ __launch_bounds__(kTcThreads, 1) void k_factor_tc(DevProblem P, DevBa
                 tc_fence_before();
                 handoff_arrive();
                 issued = J + 1;
+                // ---- while the MMAs run: the Cholesky factor Lc = Lu D^{1/2} of the
+                //      step (as src/chol.f90 stores it), the fused forward substitution
+                //      and the rows of L in the band
+                {
+                    float2 sq[4], isq[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        sq[q] = csqrt_fast(dv[q]);
+                        isq[q] = cmulf(sq[q], dinv[q]);  // 1/sqrt(d) = sqrt(d)/d
+                    }
+                    float2 ysh[4];
+                    if (fuse) {
+                        float2 bb[4];
+#pragma unroll
+                        for (int q = 0; q < 4; q++) bb[q] = bpiv[q];
+#pragma unroll
+                        for (int q = 0; q < 4; q++) {
+                            ysh[q] = cmulf(bb[q], isq[q]);
+#pragma unroll
+                            for (int r = q + 1; r < 4; r++) bb[r] = cfmsf(bb[r], cmulf(Lu[r][q], sq[q]), ysh[q]);
+                        }
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            if (t == q && j + q < n) yv[j + q] = ysh[q];
+                    }
+                    if (blk == Bk) {
+                        if (j + b4 < n) {  // row j+b4 of the pivot block's Cholesky factor
+                            float2 *row = L + (size_t)(j + b4) * Wb + (mb - b4);
+#pragma unroll
+                            for (int r = 0; r < 4; r++)
+                                if (r == b4) {
+#pragma unroll
+                                    for (int q = 0; q <= r; q++)
+                                        if (mb - r + q >= 0) row[q] = (q == r) ? sq[q] : cmulf(Lu[r][q], sq[q]);
+                                }
+                        }
+                        bsh = fuse ? S.bnew[cn][b4] : cf(0.f, 0.f);  // the entering row's right-hand side
+                    } else {
+                        const int r_l = j + dist, band0 = dist - mb;
+                        float2 lc[4];
+#pragma unroll
+                        for (int q = 0; q < 4; q++) lc[q] = cmulf(m[q], isq[q]);  // = l sqrt(d)
+                        if (r_l < n && band0 < 4) {
+                            float2 *row = L + (size_t)r_l * Wb + (j - r_l + mb);  // column j
+#pragma unroll
+                            for (int q = 0; q < 4; q++)
+                                if (q >= band0) row[q] = lc[q];
+                        }
+                        if (fuse) {
+#pragma unroll
+                            for (int q = 0; q < 4; q++) bsh = cfmsf(bsh, lc[q], ysh[q]);
+                        }
+                    }
+                }
                 Bp = Bk;
                 Bk = (Bk + 1 == kTcNB) ? 0 : Bk + 1;
             }
