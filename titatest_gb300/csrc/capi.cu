@@ -580,6 +580,7 @@ int crgpu_destroy(crgpu_ctx *c) {
     for (void *p : c->allocs) cudaFreeAsync(p, c->st);
     if (c->d_upd) cudaFreeAsync(c->d_upd, c->st);
     if (c->own_st) cudaStreamDestroy(c->own_st);
+    if (c->copy_st) cudaStreamDestroy(c->copy_st);
     delete c;
     return 0;
 }
@@ -660,18 +661,47 @@ int crgpu_sens_device(crgpu_ctx *c, int32_t mode, void *sens_device) {
     return 0;
 }
 
+// The Jacobian to host memory: computed in chunks of elements, each chunk's
+// columns (contiguous in sens(nanz, manz)) copied by a second stream while
+// the next chunk is computed.
 int crgpu_sens(crgpu_ctx *c, int32_t mode, double *sens) {
-    if (!c || !sens) return ERR_ARG;
-    size_t cnt = (size_t)c->nanz * c->hg.elanz;
+    if (!c || !sens || (mode != 0 && mode != 1)) return ERR_ARG;
+    if (!c->have_forward) return fail(c, ERR_ARG, "crgpu_sens before crgpu_forward");
+    const size_t nanz = c->nanz, manz = c->hg.elanz, cnt = nanz * manz;
     if (!c->d_sens) {
         int e = dalloc(c, &c->d_sens, cnt);
         if (e) return e;
     }
-    int e = crgpu_sens_device(c, mode, c->d_sens);
-    if (e) return e;
-    c->last_sens = c->d_sens;
-    CUCHECK(c, cudaMemcpyAsync(sens, c->d_sens, cnt * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+    if (!c->copy_st) CUCHECK(c, cudaStreamCreateWithFlags(&c->copy_st, cudaStreamNonBlocking));
+    constexpr int kChunks = 8;
+    cudaEvent_t a, b, done[kChunks];
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    for (auto &d : done) cudaEventCreateWithFlags(&d, cudaEventDisableTiming);
+    cudaEventRecord(a, c->st);
+    const int per = (int)((manz + kChunks - 1) / kChunks);
+    for (int q = 0; q < kChunks; q++) {
+        const int e0 = q * per, ne = std::min<int>(per, (int)manz - e0);
+        if (ne <= 0) break;
+        launch_bsens(c->P, c->d_kpot, c->d_sigma, c->d_volt, mode, c->precision == CRGPU_MIXED, c->d_sens, c->st, e0,
+                     ne);
+        c->stats.kernel_launches += 1;
+        CUCHECK(c, cudaEventRecord(done[q], c->st));
+        CUCHECK(c, cudaStreamWaitEvent(c->copy_st, done[q], 0));
+        CUCHECK(c, cudaMemcpyAsync(sens + 2 * (size_t)e0 * nanz, c->d_sens + (size_t)e0 * nanz,
+                                   (size_t)ne * nanz * sizeof(double2), cudaMemcpyDeviceToHost, c->copy_st));
+    }
+    cudaEventRecord(b, c->st);
+    CUCHECK(c, cudaStreamSynchronize(c->copy_st));
     CUCHECK(c, cudaStreamSynchronize(c->st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    c->stats.ms_sens = ms;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    for (auto &d : done) cudaEventDestroy(d);
+    c->last_sens = c->d_sens;
+    CUCHECK(c, cudaGetLastError());
     return 0;
 }
 

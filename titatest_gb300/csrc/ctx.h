@@ -17,6 +17,7 @@ struct crgpu_ctx {
     int eanz = 0, nanz = 0, K = 0;
     int swrtr = 1, lsr = 0, lsink = 0, nsink = -1, lsytop = 0;
     cudaStream_t st = nullptr, own_st = nullptr;
+    cudaStream_t copy_st = nullptr;  // device -> host copies overlapped with compute
     int nsm = 0, device = 0;
     std::vector<void *> allocs;
     // device state

@@ -49,8 +49,10 @@ void launch_bvolt(const DevProblem &P, const double2 *hpot, int mode, const doub
                   double2 *volt, double2 *sigmaa, cudaStream_t st);
 
 // sensitivities (src/bsens.f90, src/bsensi.f90)
+// elements e_first .. e_first + e_count - 1 (e_count < 0: to the last)
 void launch_bsens(const DevProblem &P, const double2 *kpot, const double2 *sigma,
-                  const double2 *volt, int mode, bool single, double2 *sens, cudaStream_t st);
+                  const double2 *volt, int mode, bool single, double2 *sens, cudaStream_t st,
+                  int e_first = 0, int e_count = -1);
 
 // adjoint of the forward block (adjoint.cu)
 void launch_adjoint_sources(const DevProblem &P, const double2 *g, double2 *src, int lsink, int nsink,

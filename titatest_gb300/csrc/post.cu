@@ -100,12 +100,12 @@ template <int MODE, typename R>
 __global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P, const double2 *__restrict__ kpot,
                                                          const double2 *__restrict__ sigma,
                                                          const double2 *__restrict__ volt,
-                                                         double2 *__restrict__ sens) {
+                                                         double2 *__restrict__ sens, int e_first) {
     using C = typename SensT<R>::C;
     extern __shared__ __align__(16) unsigned char kp_raw[];
     C *kp_sh = (C *)kp_raw;  // [4][eanz]
     __shared__ R kel[10];
-    const int e = blockIdx.x;
+    const int e = e_first + blockIdx.x;
     const int nk = P.etype[e] == 3 ? 3 : 4;
     int nodes[4];
 #pragma unroll
@@ -182,15 +182,17 @@ __global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P, const doub
 }
 
 void launch_bsens(const DevProblem &P, const double2 *kpot, const double2 *sigma, const double2 *volt, int mode,
-                  bool single, double2 *sens, cudaStream_t st) {
+                  bool single, double2 *sens, cudaStream_t st, int e_first, int e_count) {
+    if (e_count < 0) e_count = P.elanz - e_first;
+    if (e_count <= 0) return;
     if (single) {
         size_t smem = sizeof(float2) * 4 * P.eanz;
-        if (mode == 0) k_bsens<0, float><<<P.elanz, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens);
-        else k_bsens<1, float><<<P.elanz, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens);
+        if (mode == 0) k_bsens<0, float><<<e_count, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens, e_first);
+        else k_bsens<1, float><<<e_count, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens, e_first);
     } else {
         size_t smem = sizeof(double2) * 4 * P.eanz;
-        if (mode == 0) k_bsens<0, double><<<P.elanz, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens);
-        else k_bsens<1, double><<<P.elanz, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens);
+        if (mode == 0) k_bsens<0, double><<<e_count, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens, e_first);
+        else k_bsens<1, double><<<e_count, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens, e_first);
     }
 }
 
