@@ -174,3 +174,40 @@ def test_singularity_removal_homogeneous_is_analytic(gpu_lib):
         for l in (1, sv.eanz):
             pa = P.potana(l, kwn[k], s0)
             assert relerr(out["kpot"][k, l - 1], pa) < 1e-12
+
+
+def _wide_band_case(nx=190, nz=6, ne=16, seed=17):
+    """A strip in its natural numbering (x fastest): band width nx + 2 at
+    only (nx+1)(nz+1) nodes, beyond the register-window kernels."""
+    from titatest_gb300 import formats, synth
+    xs = np.arange(nx + 1, dtype=float)
+    depths = np.arange(nz + 1, dtype=float)
+    grid, surface, X, Y = synth._quad_grid(xs, depths)
+    area = grid.nrel[: grid.nelanz[0]]
+    grid.mb = int((area.max(axis=1) - area.min(axis=1)).max())
+    enr = surface[np.linspace(10, nx - 10, ne).astype(int)]
+    s, v = synth._encode(synth.dipole_dipole(ne, [1], [1, 2, 3]))
+    survey = formats.Survey(enr=enr, strnr=s, vnr=v, strom=np.ones(len(s)))
+    mag, pha = synth.random_model(grid, np.random.default_rng(seed))
+    return grid, survey, synth._sigma_from(mag, pha)
+
+
+def test_wide_band_mixed_factor_shared_memory_window(gpu_lib):
+    """mb = 192: the complex64 factor with its window in shared memory, against
+    the oracle's factor and, through refinement, the complex128 forward."""
+    from titatest_gb300 import MIXED, PLAIN, CRMod
+    g, sv, sig = _wide_band_case()
+    assert 176 <= g.mb + 1 <= 208
+    P = O.Problem(g, sv)
+    kwn, kwnwi = P.rwaven()
+    a_ref, fak_ref = P.factor(sig, kwn, 1, 1)
+    with CRMod(g, sv, kwn, kwnwi, precision=MIXED) as m:
+        a, fak = m.factor_system(sig, 1, 1)
+        m.set_refinement(10, 1e-10)
+        vm = m.forward(sig)["volt"]
+    with CRMod(g, sv, kwn, kwnwi, precision=PLAIN) as m:
+        vp = m.forward(sig)["volt"]
+    for i in range(g.sanz):
+        lo = max(0, g.mb - i)
+        assert relerr(a[i, lo:], a_ref[i, lo:]) < 1e-3, i
+    assert relerr(vm, vp) < MIXED_VOLT_TOL

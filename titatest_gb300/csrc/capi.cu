@@ -566,7 +566,7 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
         }
     }
     if (precision == CRGPU_MIXED && !mixed_window_supported(hg.mb + 1)) {
-        c->last_error = "mixed precision supports band widths up to 175";
+        c->last_error = "mixed precision supports band widths up to 207";
         *out = c;
         return ERR_UNSUPPORTED;
     }

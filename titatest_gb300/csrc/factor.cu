@@ -17,6 +17,8 @@
 //    GB300 the FP64 pipe, not memory, bounds this kernel.
 //  * complex64, mb <= 124: k_factor_tc (tc_factor.cu) keeps the window in
 //    tensor memory and applies the trailing updates with tcgen05.mma.
+//  * complex64, mb > 175: k_factor_mixed_smem<WP> (factor_smem.cu), the same
+//    algorithm with the tiles in shared memory.
 //  * complex64, larger mb: k_factor_mixed<WP>: the (mb+1) x (mb+1) window
 //    lives in registers.  Window rows rotate through W = mb+1 slots (row r in
 //    slot r mod W); every thread owns a fixed 4x4 tile of the lower triangle
@@ -292,7 +294,8 @@ __global__ __launch_bounds__(MixCfg<WP>::NT, 1) void k_factor_mixed(DevProblem P
                     // pivot row j+b4: its row of the diagonal block factor
                     if (j + b4 < n) {
                         float2 *row = L + (size_t)(j + b4) * Wb + (mb - b4);  // column j
-                        for (int q = 0; q <= b4; q++) row[q] = Ldsh[b4][q];
+                        for (int q = 0; q <= b4; q++)
+                            if (mb - b4 + q >= 0) row[q] = Ldsh[b4][q];
                     }
                     // the row entering this slot: its entries in the pivot columns
                     band0 = WP + b4 - mb;  // >= b4 + 1
@@ -402,12 +405,12 @@ __global__ __launch_bounds__(MixCfg<WP>::NT, 1) void k_factor_mixed(DevProblem P
 
 #define CRGPU_MIXED_SIZES(X) X(36) X(64) X(84) X(104) X(124) X(128) X(144) X(160) X(176)
 
-// smallest instantiated window holding W = mb + 1 rows
+// smallest instantiated window holding W = mb + 1 rows (registers, then shared memory)
 int mixed_window_supported(int W) {
 #define X(S) if (W <= S) return S;
     CRGPU_MIXED_SIZES(X)
 #undef X
-    return 0;
+    return mixed_smem_window_supported(W);
 }
 
 int launch_factor_mixed(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st) {
@@ -421,7 +424,7 @@ int launch_factor_mixed(const DevProblem &P, const DevBatch &B, int fuse, int ns
     }
     CRGPU_MIXED_SIZES(X)
 #undef X
-    return ERR_UNSUPPORTED;
+    return launch_factor_mixed_smem(P, B, fuse, nsm, st);
 }
 
 }  // namespace crgpu

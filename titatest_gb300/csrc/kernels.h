@@ -27,6 +27,9 @@ void launch_factor_plain(const DevProblem &P, const DevBatch &B, int fuse, int n
 int launch_factor_mixed(const DevProblem &P, const DevBatch &B, int fuse, int nsm,
                         cudaStream_t st);
 int mixed_window_supported(int W);
+// shared-memory window variant (factor_smem.cu) for 176 < mb + 1 <= 208
+int mixed_smem_window_supported(int W);
+int launch_factor_mixed_smem(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st);
 // tensor-core variant (tc_factor.cu) for band widths mb <= 124
 int launch_factor_tc(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st);
 
