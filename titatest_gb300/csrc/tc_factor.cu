@@ -7,35 +7,40 @@
 // real / imaginary part of the entry with the row of slot c.  One step
 // eliminates the 4 pivot columns j..j+3 (pivot slot block Bk = J mod 32):
 //
-//   1. tcgen05.ld of the 8 pivot columns: every thread (= slot) gets its
-//      row's 4 entries A(r, j..j+3);
-//   2. SIMT panel: 4x4 factor of the diagonal block, the slot's L entries
-//      l_r = A(r, j..j+3) Ld^{-T}, the band rows of L to global memory and
-//      the fused forward substitution;
+//   1. every thread (= slot) holds its row's 4 entries A(r, j..j+3) in the
+//      pivot columns (read ahead, see below);
+//   2. SIMT panel: L D L^T of the 4x4 diagonal block (in every thread),
+//      m_r = A(r, j..j+3) Lu^{-T} and l_r = m_r D^{-1} of the slot's row;
 //   3. one elected thread issues, into the TMEM window,
 //        D += A . B^T  (M=128, N=256, K=8, kind::tf32)
-//      with A row r = [Re l_r | Im l_r] and B rows 2c, 2c+1 =
-//      [-Re l_c | Im l_c], [-Im l_c | -Re l_c]: D -= l l^T in complex
-//      arithmetic.  Three products (hi.hi + hi.lo + lo.hi of the tf32
-//      splits of l) keep FP32 accuracy; pivot rows contribute zero.
+//      with A row r = [Re m_r | Im m_r] and B rows 2c, 2c+1 =
+//      [-Re l_c | Im l_c], [-Im l_c | -Re l_c]: D -= m l^T in complex
+//      arithmetic (the Schur complement A - a P^{-1} a^T of the pivot block
+//      P).  Three products (hi.hi + hi.lo + lo.hi of the tf32 splits) keep
+//      FP32 accuracy; pivot rows contribute zero.
 //   4. the 4 rows entering at this step take over the pivot slots.  Their
 //      row part D(p, :) is set by a fourth MMA whose A is one-hot on the
 //      pivot lanes and whose B holds new value - old value (hi + lo); the
 //      old value of D(p, c) is, by symmetry, the pivot column entry that
-//      thread c read in step 1.  Their column part D(:, p) is written by
+//      thread c holds in step 1.  Their column part D(:, p) is written by
 //      tcgen05.st once the MMAs of the step have completed.
 // Entering rows never reach back into eliminated columns because the window
 // has 128 >= mb + 4 rows, so they need no update of earlier steps.
 //
-// The MMAs of a step are issued in two parts: (a) the 16 columns holding the
-// next step's pivot block, then (b) the other 240.  The next panel starts
-// as soon as (a) has landed and overlaps (b); operands are double buffered.
+// One-step look-ahead: before handing step J over, the panel reads the
+// next pivot columns from TMEM as they stand after the MMAs of step J-1 and
+// applies step J's rank-4 update to them itself (4x4 complex products per
+// row), so the MMAs of step J have a whole panel step to complete.
 //
 // Roles: warps 0-3 (128 threads, thread t <-> TMEM lane t) run the panel;
 // warp 4 stages the entering rows from the scaled sparse values (cp.async
-// ring, kStageSteps ahead); warp 5 issues the MMAs when the panel hands over
-// a step's operands (named barrier 2).  Every mbarrier wait is bounded in
-// time and failures are agreed on by a barrier reduction, so all roles leave
+// ring, three steps ahead of their use); warp 5 issues the MMAs when the
+// panel hands over a step's operands, then, while they run, does the pivot
+// block's share of the factor (its rows of L, the fused forward substitution
+// and 1/sqrt(d), u = D^{-1} Lu^{-1} b for the panel, which stores its rows of L
+// and updates its right-hand side one step later).  All six warps meet at
+// one named barrier per step.  Every mbarrier wait is bounded in time and
+// failures are agreed on by a barrier reduction, so all roles leave
 // together.
 #include <mutex>
 
@@ -72,8 +77,11 @@ struct TcSmem {
     int ring_col[kStageSteps][4][32];
     float2 dm[2][4][4];  // diagonal block of the step
     float2 bp[2][4];     // right-hand side of the pivot rows
-    uint64_t bar_a, bar_b;  // MMA parts (a) and (b) of a step completed
-    uint64_t bar_nbF[kTcNNB], bar_nbE[kTcNNB];
+    float2 lnx[2][4][4];  // l of the next step's pivot rows [row][k]
+    float2 mp[2][4][4];   // m of the last step of the pivot rows [row][k]
+    float2 isq_s[2][4];   // 1/sqrt(d) of the step's pivots
+    float2 u_s[2][4];     // u = D^{-1} Lu^{-1} b of the step's pivot rows
+    uint64_t bar_m;  // the MMAs of a step completed
     uint32_t tmem_base;
     int bad;
     int abort_flag;
@@ -180,8 +188,8 @@ __device__ __forceinline__ void put_row8(float *op, int row, const float (&v)[8]
 
 
 // named barrier 2: the panel threads hand a step's operands to the MMA warp
-__device__ __forceinline__ void handoff_arrive() { asm volatile("bar.arrive 2, 160;\n" ::: "memory"); }
-__device__ __forceinline__ void handoff_sync() { asm volatile("bar.sync 2, 160;\n" ::: "memory"); }
+__device__ __forceinline__ void handoff_arrive() { asm volatile("bar.arrive 2, 192;\n" ::: "memory"); }
+__device__ __forceinline__ void handoff_sync() { asm volatile("bar.sync 2, 192;\n" ::: "memory"); }
 
 // L D L^T of the 4x4 pivot block (rows j..j+3, complex symmetric; rows
 // beyond n get a unit pivot): unit lower Lu, d and 1/d.  The only
@@ -260,12 +268,7 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
         const double2 *bv = B.b + (size_t)s * n;
         __syncthreads();
         if (tid == 0) {
-            mbar_init(&S.bar_a, 1);
-            mbar_init(&S.bar_b, 1);
-            for (int q = 0; q < kTcNNB; q++) {
-                mbar_init(&S.bar_nbF[q], 1);
-                mbar_init(&S.bar_nbE[q], 4);
-            }
+            mbar_init(&S.bar_m, 1);
             mbar_init_fence();
             S.bad = 0;
             S.abort_flag = 0;
@@ -273,6 +276,7 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
             S.stop_issue = 0;
         }
         for (int q = tid; q < kTcNNB * 4 * kTcWP; q += blockDim.x) (&S.nbuf[0][0][0])[q] = cf(0.f, 0.f);
+        for (int q = tid; q < kTcWP * 8; q += blockDim.x) S.op[0].a_e[q] = S.op[1].a_e[q] = 0.f;
         if (tid < 4 * kTcNNB) S.bnew[tid / 4][tid % 4] = cf(0.f, 0.f);
         __syncthreads();
         // ---- initial window (rows 0..127) from the full symmetric pattern;
@@ -324,33 +328,53 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
         if (is_panel) {
             // ================= panel warps: one thread per slot =================
             const int t = tid, b4 = t & 3, blk = t >> 2;
-            int Bk = 0, Bp = kTcNB - 1;
-            int issued = 0;  // steps handed to the MMA warp
+            int Bk = 0, Bp = kTcNB - 1;  // pivot block of this step, of the last step
+            int issued = 0;              // steps handed to the MMA warp
             int bad = 0;
-            for (int J = 0; J < nblk; J++) {
-                const int j = 4 * J, cn = J % kTcNNB, ob = J & 1;
-                bool ok = true;
-                if (J >= 1) {
-                    ok = __all_sync(0xffffffffu, mbar_wait_abort(&S.bar_a, (J - 1) & 1, abort_flag, 0u));
-                    tc_fence_after();
-                }
-                if (J >= kTcNNB)
-                    ok = __all_sync(0xffffffffu,
-                                    ok && mbar_wait_abort(&S.bar_nbF[cn], ((J - kTcNNB) / kTcNNB) & 1, abort_flag, 0u));
-                // pivot columns of this step (part (a) of the last step has landed)
-                float2 a[4], a0[4];
-                {
-                    float v[8];
-                    tmem_ld8(tlane + 8 * Bk, v);
+            bool failed = false;
+            // this row's entries in the pivot columns of the coming step, as in
+            // TMEM before the last step's update (which the panel applies itself)
+            float2 pre[4], mprev[4];
+            {
+                float v[8];
+                tmem_ld8(tlane, v);
 #pragma unroll
-                    for (int q = 0; q < 4; q++) a[q] = a0[q] = cf(v[2 * q], v[2 * q + 1]);
+                for (int q = 0; q < 4; q++) {
+                    pre[q] = cf(v[2 * q], v[2 * q + 1]);
+                    mprev[q] = cf(0.f, 0.f);
+                }
+            }
+            for (int J = 0; J < nblk; J++) {
+                const int j = 4 * J, cn = J % kTcNNB, cp = (J + kTcNNB - 1) % kTcNNB, ob = J & 1;
+                const int Bn = (Bk + 1 == kTcNB) ? 0 : Bk + 1;
+                bool ok = !failed;
+                // ---- this row's entries in the pivot columns: the rows that entered at the
+                //      last step as staged, the others with the last step's update applied
+                float2 a[4], mold[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) mold[q] = mprev[q];
+                if (J >= 1 && blk == Bp) {
+#pragma unroll
+                    for (int q = 0; q < 4; q++) a[q] = S.nbuf[cp][b4][4 * Bk + q];
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        float2 x = pre[q];
+                        if (J >= 1) {
+#pragma unroll
+                            for (int p = 0; p < 4; p++) x = cfmsf(x, mprev[p], S.lnx[ob ^ 1][q][p]);
+                        }
+                        a[q] = x;
+                    }
                 }
                 if (blk == Bk) {
 #pragma unroll
-                    for (int q = 0; q < 4; q++) S.dm[ob][b4][q] = a[q];
+                    for (int q = 0; q < 4; q++) {
+                        S.dm[ob][b4][q] = a[q];
+                        S.mp[ob][b4][q] = mprev[q];
+                    }
                     S.bp[ob][b4] = bsh;
                 }
-                tc_fence_before();
                 if (panel_bar_or(!ok)) {  // the same decision in every panel thread
                     if (t == 0) {
                         S.panel_fail = 1;
@@ -369,9 +393,6 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
                         for (int q = 0; q < 4; q++) d0[r][q] = S.dm[ob][r][q];
                     pivot_ldlt(d0, j, n, Lu, dv, dinv, bad);
                 }
-                float2 bpiv[4];
-#pragma unroll
-                for (int q = 0; q < 4; q++) bpiv[q] = S.bp[ob][q];
                 // ---- m = a Lu^{-T} and l = m D^{-1} of this slot's row (zero for the pivot rows)
                 float2 m[4], l[4];
                 int dist = t - 4 * Bk;
@@ -389,10 +410,15 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
                         l[q] = cmulf(x, dinv[q]);
                     }
                 }
-                // ---- MMA operands of this step (buffer ob)
+                if (blk == Bn) {  // the next pivot rows' l, for the next step's update of its pivot columns
+#pragma unroll
+                    for (int q = 0; q < 4; q++) S.lnx[ob][b4][q] = l[q];
+                }
+                // ---- MMA operands of this step (buffer ob; its last reader, the MMAs of
+                //      step J-2, completed before step J-1 ended)
                 {
                     TcOperands &o = S.op[ob];
-                    float ah[8], al[8], bh0[8], bl0[8], bh1[8], bl1[8], ae[8], be0[8], be1[8];
+                    float ah[8], al[8], bh0[8], bl0[8], bh1[8], bl1[8], be0[8], be1[8];
 #pragma unroll
                     for (int q = 0; q < 4; q++) {
                         const float mr = m[q].x, mi = m[q].y, re = l[q].x, im = l[q].y;
@@ -410,12 +436,10 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
                         bh1[4 + q] = -reh;
                         bl1[q] = -(im - imh);
                         bl1[4 + q] = -(re - reh);
-                        ae[q] = (blk == Bk && b4 == q) ? 1.f : 0.f;
-                        ae[4 + q] = ae[q];
                         // new - old value of entering row q at this slot's column; the old
-                        // value D(pivot q, t) equals this thread's pivot entry a0[q] by symmetry
+                        // value D(pivot q, t) equals this thread's pivot entry a[q] by symmetry
                         const float2 nv = (blk == Bk) ? entering_pair(S.nbuf[cn], Bk, q, b4) : S.nbuf[cn][q][t];
-                        const float dr = nv.x - a0[q].x, di = nv.y - a0[q].y;
+                        const float dr = nv.x - a[q].x, di = nv.y - a[q].y;
                         const float drh = tf32_hi(dr), dih = tf32_hi(di);
                         be0[q] = drh;
                         be0[4 + q] = dr - drh;
@@ -428,17 +452,25 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
                     put_row8(o.b_lo, 2 * t, bl0);
                     put_row8(o.b_hi, 2 * t + 1, bh1);
                     put_row8(o.b_lo, 2 * t + 1, bl1);
-                    put_row8(o.a_e, t, ae);
+                    // A of the injection: one-hot rows on the pivot lanes; the rows set
+                    // in this buffer two steps ago go back to zero
+                    const int B2 = Bk >= 2 ? Bk - 2 : Bk + kTcNB - 2;
+                    if (blk == Bk || (J >= 2 && blk == B2)) {
+                        float ae[8];
+#pragma unroll
+                        for (int q = 0; q < 4; q++) ae[q] = ae[4 + q] = (blk == Bk && b4 == q) ? 1.f : 0.f;
+                        put_row8(o.a_e, t, ae);
+                    }
                     put_row8(o.b_e, 2 * t, be0);
                     put_row8(o.b_e, 2 * t + 1, be1);
                 }
-                // ---- the last step's MMAs have all landed: column part of the rows
-                //      that entered then (they are read by this step's MMAs)
+                // ---- the last step's MMAs have landed: column part of the rows that
+                //      entered then (the MMAs of this step update it), and the next
+                //      pivot columns as they stand before this step's update
                 if (J >= 1) {
-                    ok = __all_sync(0xffffffffu, mbar_wait_abort(&S.bar_b, (J - 1) & 1, abort_flag, 0u));
+                    ok = __all_sync(0xffffffffu, mbar_wait_abort(&S.bar_m, (J - 1) & 1, abort_flag, 0u));
                     tc_fence_after();
                     if (ok) {
-                        const int cp = (J - 1) % kTcNNB;
                         float v[8];
 #pragma unroll
                         for (int b = 0; b < 4; b++) {
@@ -449,90 +481,62 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
                         }
                         tmem_st8(tlane + 8 * Bp, v);
                     }
-                    __syncwarp();
-                    if (lane == 0) mbar_arrive(&S.bar_nbE[(J - 1) % kTcNNB]);
                 }
-                if (!ok) {
-                    if (t == 0) S.panel_fail = 1;
-                }
-                fence_proxy_async();
-                tc_fence_before();
-                handoff_arrive();
-                issued = J + 1;
-                // ---- while the MMAs run: the Cholesky factor Lc = Lu D^{1/2} of the
-                //      step (as src/chol.f90 stores it), the fused forward substitution
-                //      and the rows of L in the band
-                {
-                    float2 sq[4], isq[4];
+                if (ok && J + 1 < nblk) {
+                    float v[8];
+                    tmem_ld8(tlane + 8 * Bn, v);
 #pragma unroll
                     for (int q = 0; q < 4; q++) {
-                        sq[q] = csqrt_fast(dv[q]);
-                        isq[q] = cmulf(sq[q], dinv[q]);  // 1/sqrt(d) = sqrt(d)/d
-                    }
-                    float2 ysh[4];
-                    if (fuse) {
-                        float2 bb[4];
-#pragma unroll
-                        for (int q = 0; q < 4; q++) bb[q] = bpiv[q];
-#pragma unroll
-                        for (int q = 0; q < 4; q++) {
-                            ysh[q] = cmulf(bb[q], isq[q]);
-#pragma unroll
-                            for (int r = q + 1; r < 4; r++) bb[r] = cfmsf(bb[r], cmulf(Lu[r][q], sq[q]), ysh[q]);
-                        }
-#pragma unroll
-                        for (int q = 0; q < 4; q++)
-                            if (t == q && j + q < n) yv[j + q] = ysh[q];
-                    }
-                    if (blk == Bk) {
-                        if (j + b4 < n) {  // row j+b4 of the pivot block's Cholesky factor
-                            float2 *row = L + (size_t)(j + b4) * Wb + (mb - b4);
-#pragma unroll
-                            for (int r = 0; r < 4; r++)
-                                if (r == b4) {
-#pragma unroll
-                                    for (int q = 0; q <= r; q++)
-                                        if (mb - r + q >= 0) row[q] = (q == r) ? sq[q] : cmulf(Lu[r][q], sq[q]);
-                                }
-                        }
-                        bsh = fuse ? S.bnew[cn][b4] : cf(0.f, 0.f);  // the entering row's right-hand side
-                    } else {
-                        const int r_l = j + dist, band0 = dist - mb;
-                        float2 lc[4];
-#pragma unroll
-                        for (int q = 0; q < 4; q++) lc[q] = cmulf(m[q], isq[q]);  // = l sqrt(d)
-                        if (r_l < n && band0 < 4) {
-                            float2 *row = L + (size_t)r_l * Wb + (j - r_l + mb);  // column j
-#pragma unroll
-                            for (int q = 0; q < 4; q++)
-                                if (q >= band0) row[q] = lc[q];
-                        }
-                        if (fuse) {
-#pragma unroll
-                            for (int q = 0; q < 4; q++) bsh = cfmsf(bsh, lc[q], ysh[q]);
-                        }
+                        pre[q] = cf(v[2 * q], v[2 * q + 1]);
+                        mprev[q] = m[q];
                     }
                 }
+                failed = !ok;
+                if (!ok && t == 0) S.panel_fail = 1;
+                fence_proxy_async();
+                tc_fence_before();
+                handoff_sync();  // also orders this step's lnx before the next step's reads
+                issued = J + 1;
+                // ---- while the MMAs run: this row's entries of Lc = Lu D^{1/2} (as
+                //      src/chol.f90 stores it) in the last step's pivot columns,
+                //      l sqrt(d) = m / sqrt(d), and the last step's update of the fused
+                //      forward substitution, b -= l (Lu^{-1} b_p) = m u, from 1/sqrt(d)
+                //      and u of the pivot block that the MMA warp left in shared memory
+                if (J >= 1 && blk != Bp) {
+                    const int r_l = j + dist, band0 = dist + 4 - mb;
+                    if (r_l < n && band0 < 4) {
+                        float2 *row = L + (size_t)r_l * Wb + (j - 4 - r_l + mb);  // column j-4
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            if (q >= band0) row[q] = cmulf(mold[q], S.isq_s[ob ^ 1][q]);
+                    }
+                    if (fuse) {
+#pragma unroll
+                        for (int q = 0; q < 4; q++) bsh = cfmsf(bsh, mold[q], S.u_s[ob ^ 1][q]);
+                    }
+                }
+                if (blk == Bk) bsh = fuse ? S.bnew[cn][b4] : cf(0.f, 0.f);  // the entering row's right-hand side
                 Bp = Bk;
-                Bk = (Bk + 1 == kTcNB) ? 0 : Bk + 1;
+                Bk = Bn;
             }
             // the MMAs issued last must land before the next system or the dealloc
             if (issued > 0) {
-                mbar_wait(&S.bar_b, (issued - 1) & 1);
+                mbar_wait(&S.bar_m, (issued - 1) & 1);
                 tc_fence_after();
-            }
-            if (issued == nblk) {
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&S.bar_nbE[(nblk - 1) % kTcNNB]);
             }
             if (bad) S.bad = bad;
         } else if (is_stage) {
             // ================= staging warp =================
+            // The buffer of step i-1's entering rows is free once step i has been
+            // handed over (its last reader is step i's column store): after
+            // handoff i it takes the rows of step i+3, which step i+3 reads after
+            // handoff i+2.  The per-step handoff barrier orders both sides.
             const int ln = lane;
-            for (int J = 0; J < nblk; J++) {
-                const int cn = J % kTcNNB, m = J + kTcNNB;  // refill buffer cn with step m
-                const bool ok = mbar_wait_abort(&S.bar_nbE[cn], (J / kTcNNB) & 1, abort_flag);
-                if (!__all_sync(0xffffffffu, ok)) break;
+            for (int i = 0; i < nblk; i++) {
+                handoff_sync();
+                if (S.stop_issue) break;
+                if (i == 0) continue;
+                const int m = i + kTcNNB - 1, cn = m % kTcNNB;
                 for (int q = ln; q < kTcWP; q += 32) {
 #pragma unroll
                     for (int r = 0; r < 4; r++) S.nbuf[cn][r][q] = cf(0.f, 0.f);
@@ -553,27 +557,79 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
                 __syncwarp();
                 stage_issue4(P, as, bv, 4 * (m + kStageSteps) + kTcWP, ln, rw, fuse, S.ring_val[sl], S.ring_col[sl],
                              S.ring_b[sl]);
-                if (ln == 0) mbar_arrive(&S.bar_nbF[cn]);
             }
             cp_wait<0>();
         } else if (is_mma) {
             // ================= MMA warp =================
-            int Bn = 1 % kTcNB;
+            // Issues each step's MMAs; then, while they run, lanes 0-3 do the pivot
+            // block's share of the factor: its rows of Lc, the fused forward
+            // substitution y = D^{-1/2} Lu^{-1} b and, for the panel's update of the
+            // other rows, 1/sqrt(d) and u = D^{-1} Lu^{-1} b.
+            float2 up[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) up[q] = cf(0.f, 0.f);
             for (int J = 0; J < nblk; J++) {
                 handoff_sync();
                 if (S.stop_issue) break;
                 tc_fence_after();
+                const int ob = J & 1;
                 if (lane == 0) {
-                    const TcOperands &o = S.op[J & 1];
-                    const int c0 = 16 * (Bn >> 1);  // 16 columns holding the next pivot block
-                    issue_range(tbase, o, c0, 16);
-                    tc_commit(&S.bar_a);
-                    if (c0 > 0) issue_range(tbase, o, 0, c0);
-                    if (c0 + 16 < kTcCols) issue_range(tbase, o, c0 + 16, kTcCols - c0 - 16);
-                    tc_commit(&S.bar_b);
+                    issue_range(tbase, S.op[ob], 0, kTcCols);
+                    tc_commit(&S.bar_m);
+                }
+                if (lane < 4) {
+                    const int j = 4 * J, q = lane;
+                    float2 d0[4][4], Lu[4][4], dv[4], dinv[4];
+#pragma unroll
+                    for (int r = 0; r < 4; r++)
+#pragma unroll
+                        for (int c = 0; c < 4; c++) d0[r][c] = S.dm[ob][r][c];
+                    int bad_m = 0;  // reported by the panel, which factors the same block
+                    pivot_ldlt(d0, j, n, Lu, dv, dinv, bad_m);
+                    // right-hand side of the pivot rows with the last step's update, then Lu^{-1}
+                    float2 w[4];
+#pragma unroll
+                    for (int r = 0; r < 4; r++) {
+                        float2 x = S.bp[ob][r];
+#pragma unroll
+                        for (int p = 0; p < 4; p++) x = cfmsf(x, S.mp[ob][r][p], up[p]);
+                        w[r] = x;
+                    }
+#pragma unroll
+                    for (int c = 0; c < 4; c++)
+#pragma unroll
+                        for (int r = c + 1; r < 4; r++) w[r] = cfmsf(w[r], Lu[r][c], w[c]);
+                    float2 sq[4];
+#pragma unroll
+                    for (int p = 0; p < 4; p++) {
+                        sq[p] = csqrt_fast(dv[p]);
+                        up[p] = cmulf(w[p], dinv[p]);
+                    }
+                    float2 sqq = sq[0], dinvq = dinv[0], wq = w[0], uq = up[0];
+#pragma unroll
+                    for (int p = 1; p < 4; p++)
+                        if (q == p) {
+                            sqq = sq[p];
+                            dinvq = dinv[p];
+                            wq = w[p];
+                            uq = up[p];
+                        }
+                    const float2 isqq = cmulf(sqq, dinvq);  // 1/sqrt(d) = sqrt(d)/d
+                    if (j + q < n) {
+                        if (fuse) yv[j + q] = cmulf(wq, isqq);
+                        float2 *row = L + (size_t)(j + q) * Wb + (mb - q);  // row j+q of the pivot block
+#pragma unroll
+                        for (int r = 0; r < 4; r++)
+                            if (r == q) {
+#pragma unroll
+                                for (int p = 0; p <= r; p++)
+                                    if (mb - r + p >= 0) row[p] = (p == r) ? sq[p] : cmulf(Lu[r][p], sq[p]);
+                            }
+                    }
+                    S.isq_s[ob][q] = isqq;
+                    S.u_s[ob][q] = uq;
                 }
                 __syncwarp();
-                Bn = (Bn + 1 == kTcNB) ? 0 : Bn + 1;
             }
         }
         tc_fence_before();
@@ -582,12 +638,7 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
         if (tid == 0) {
             if (S.abort_flag || S.panel_fail) atomicCAS(&B.status[s], 0, ERR_TIMEOUT);
             else if (S.bad) atomicCAS(&B.status[s], 0, S.bad);
-            mbar_inval(&S.bar_a);
-            mbar_inval(&S.bar_b);
-            for (int q = 0; q < kTcNNB; q++) {
-                mbar_inval(&S.bar_nbF[q]);
-                mbar_inval(&S.bar_nbE[q]);
-            }
+            mbar_inval(&S.bar_m);
         }
         stop = S.abort_flag || S.panel_fail;
         __syncthreads();
