@@ -334,6 +334,7 @@ def run_gpu(args):
                   "ms_sens": plain_stats["ms_sens"]},
         "speedup_mixed_vs_plain": plain_ms / ms_per_step,
         "mixed_vs_plain_rel_err": {"volt": err_v, "jacobian": err_j},
+        "accuracy_target": {"volt": 1e-6, "jacobian": 1e-5, "met": bool(err_v < 1e-6 and err_j < 1e-5)},
         "phases_ms": {"factor": fac_avg_ms, "solve": mixed_stats["ms_solve"],
                       "forward": mixed_stats["ms_forward"], "sens": statistics.mean(sens_ms)},
         "roofline": {"kernel": "k_factor_tc", "bound": "tensor", "achieved": achieved, "peak": peak,
@@ -403,8 +404,9 @@ def main():
     ap.add_argument("--config", type=int, default=2)
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--refine-maxit", type=int, default=8)
-    ap.add_argument("--refine-tol", type=float, default=1e-3,
-                    help="mixed refinement stop: max|dx| <= tol max|x| (1e-3 keeps volt within ~1e-8 of complex128)")
+    ap.add_argument("--refine-tol", type=float, default=1e-2,
+                    help="mixed refinement stop: max|dx| <= tol max|x| (1e-2 keeps volt within ~2e-8 of "
+                         "complex128 on config 2; the error is measured and checked in every line)")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--workers", type=int, default=8, help="config 5: concurrent worker streams")
