@@ -52,6 +52,24 @@ __device__ __forceinline__ double2 entry_value(const DevProblem &P, const double
     return v;
 }
 
+// 1/sqrt(|v|) = (re^2 + im^2)^(-1/4) without FP64 division or square root
+// (both cost tens of FP64 operations, and FP64 runs at a small fraction of the
+// FP32 rate here): an FP32 estimate refined by two Newton steps for
+// y^-4 = x, y <- y (5 - x y^4) / 4, which square the relative error
+// (~1e-7 -> ~1e-13 -> FP64 rounding).  Outside the FP32 range of x the FP64
+// functions are used.
+__device__ __forceinline__ double inv_sqrt_abs(double2 v) {
+    const double x = v.x * v.x + v.y * v.y;
+    if (!(x > 1e-30 && x < 1e30)) return 1.0 / sqrt(sqrt(x));
+    double y = (double)rsqrtf(sqrtf((float)x));
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const double y2 = y * y;
+        y = y * (5.0 - x * y2 * y2) * 0.25;
+    }
+    return y;
+}
+
 // fak of every row (src/scalab.f90:50-64): grid (row blocks, systems).  The
 // rows of the lower pattern are sorted by column, so the diagonal is the
 // last entry that is not padding.
@@ -65,52 +83,45 @@ __global__ void k_fak(DevProblem P, DevBatch B, const double2 *__restrict__ sigm
     int pd = -1;
     for (int p = P.rowptr[i]; p < P.rowptr[i + 1]; p++)
         if (P.col[p] == i) pd = p;
-    double dum = 0.0;
-    if (pd >= 0) dum = cabsd(entry_value(P, ad, kgl, sigma, pd, i, i, P.dirichlet[i] != 0));
-    if (!(dum > 0.0)) {  // src/scalab.f90:57-61
+    double2 d = cz(0.0, 0.0);
+    if (pd >= 0) d = entry_value(P, ad, kgl, sigma, pd, i, i, P.dirichlet[i] != 0);
+    double f = 1.0;
+    if (!(d.x * d.x + d.y * d.y > 0.0)) {  // src/scalab.f90:57-61
         atomicCAS(&B.status[s], 0, 27);
-        dum = 1.0;
+    } else {
+        f = inv_sqrt_abs(d);
     }
-    B.fak[(size_t)s * P.n + i] = 1.0 / sqrt(dum);
+    B.fak[(size_t)s * P.n + i] = f;
 }
 
-// Scaled values of row i (src/kompab.f90 + src/scalab.f90:63-80): the
-// diagonal becomes a_ii / |a_ii|, the others a_ij * fak_i * fak_j.
-__global__ void k_assemble_rows(DevProblem P, DevBatch B, const double2 *__restrict__ sigma,
-                                const double2 *__restrict__ adom) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
-    if (i >= P.n) return;
+// Scaled values (src/kompab.f90 + src/scalab.f90:63-80), one thread per
+// pattern entry: a_ij fak_i fak_j, which makes the diagonal a_ii / |a_ii| as
+// scalab sets it.  Grid (entry blocks, systems).
+__global__ void k_assemble_entries(DevProblem P, DevBatch B, const double2 *__restrict__ sigma,
+                                   const double2 *__restrict__ adom) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
+    if (p >= P.nnz) return;
+    double2 *as = B.As + (size_t)s * P.nnz;
+    const int c = P.col[p];
+    if (c < 0) {
+        as[p] = cz(0.0, 0.0);
+        return;
+    }
+    const int i = P.row[p];
     const int k = B.ks[s], l = B.ls[s];
     const double2 *ad = adom + (size_t)k * P.nnz;
-    double2 *as = B.As + (size_t)s * P.nnz;
     const double *kgl = P.kg + ((size_t)k * P.eanz + l) * P.relanz;
     const double *f = B.fak + (size_t)s * P.n;
-    const bool dir_i = P.dirichlet[i] != 0;
-    const double fi = f[i];
-    for (int p = P.rowptr[i]; p < P.rowptr[i + 1]; p++) {
-        const int c = P.col[p];
-        if (c < 0) {
-            as[p] = cz(0.0, 0.0);
-            continue;
-        }
-        double2 v = entry_value(P, ad, kgl, sigma, p, i, c, dir_i);
-        if (c == i) {
-            const double dum = cabsd(v);
-            if (dum > 0.0) v = cdiv(v, cz(dum, 0.0));
-        } else {
-            const double fk = fi * f[c];
-            v = cz(v.x * fk, v.y * fk);
-        }
-        as[p] = v;
-    }
+    const double2 v = entry_value(P, ad, kgl, sigma, p, i, c, P.dirichlet[i] != 0);
+    const double fk = f[i] * f[c];
+    as[p] = cz(v.x * fk, v.y * fk);
 }
 
 void launch_assemble(const DevProblem &P, const DevBatch &B, const double2 *sigma, const double2 *adom,
                      cudaStream_t st) {
     const int nt = 128;
-    const dim3 grid((P.n + nt - 1) / nt, B.nsys);
-    k_fak<<<grid, nt, 0, st>>>(P, B, sigma, adom);
-    k_assemble_rows<<<grid, nt, 0, st>>>(P, B, sigma, adom);
+    k_fak<<<dim3((P.n + nt - 1) / nt, B.nsys), nt, 0, st>>>(P, B, sigma, adom);
+    k_assemble_entries<<<dim3((P.nnz + nt - 1) / nt, B.nsys), nt, 0, st>>>(P, B, sigma, adom);
 }
 
 // Right-hand sides.  nrhs == 1: one system per (k, l), b of kompab (unit
