@@ -53,6 +53,11 @@ void launch_bvolt(const DevProblem &P, const double2 *hpot, int mode, const doub
 
 // sensitivities (src/bsens.f90, src/bsensi.f90)
 // elements e_first .. e_first + e_count - 1 (e_count < 0: to the last)
+// Jacobian on the tensor cores (Gram form, complex64 contraction; src/bsens.f90
+// mode, eanz <= 127)
+bool sens_tc_supported(const DevProblem &P, int mode);
+void launch_sens_tc(const DevProblem &P, const double2 *kpot, double2 *sens, cudaStream_t st, int e_first,
+                    int e_count);
 void launch_bsens(const DevProblem &P, const double2 *kpot, const double2 *sigma,
                   const double2 *volt, int mode, bool single, double2 *sens, cudaStream_t st,
                   int e_first = 0, int e_count = -1);

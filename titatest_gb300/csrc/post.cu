@@ -185,6 +185,10 @@ void launch_bsens(const DevProblem &P, const double2 *kpot, const double2 *sigma
                   bool single, double2 *sens, cudaStream_t st, int e_first, int e_count) {
     if (e_count < 0) e_count = P.elanz - e_first;
     if (e_count <= 0) return;
+    if (single && sens_tc_supported(P, mode)) {
+        launch_sens_tc(P, kpot, sens, st, e_first, e_count);
+        return;
+    }
     if (single) {
         size_t smem = sizeof(float2) * 4 * P.eanz;
         if (mode == 0) k_bsens<0, float><<<e_count, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens, e_first);
