@@ -89,8 +89,10 @@ int crgpu_destroy(crgpu_ctx *ctx);
 /* Message of the last error on this context (the reference's fetxt). */
 const char *crgpu_last_error(const crgpu_ctx *ctx);
 
-/* Iterative refinement of the mixed mode: at most maxit corrections, stop a
- * system when max|dx| <= tol * max|x|.  Defaults: 8, 1e-10. */
+/* Iterative refinement of the mixed mode: at most maxit corrections
+ * (0 <= maxit <= 64, else 1001), stop a system when max|dx| <= tol * max|x|.
+ * Defaults: 8, 1e-10.  The steps run without host synchronisation; a step
+ * after the last system stopped returns at once. */
 int crgpu_set_refinement(crgpu_ctx *ctx, int32_t maxit, double tol);
 
 /* Stream the context's work is issued on (a cudaStream_t; NULL restores the

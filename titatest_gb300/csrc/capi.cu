@@ -15,6 +15,14 @@ using namespace crgpu;
 
 namespace {
 
+// counters of one refinement step (written by k_accumulate)
+struct RefineCount {
+    int n;     // items still refining after the step
+    int pad;
+    double z;  // largest relative correction of the step
+};
+constexpr int kRefineCap = 64;  // refinement steps at most (crgpu_set_refinement)
+
 int fail(crgpu_ctx *c, int code, const std::string &msg) {
     if (c) c->last_error = msg;
     return code;
@@ -55,8 +63,7 @@ int upload(crgpu_ctx *c, const T **dst, const std::vector<T> &v) {
 
 void free_batch(crgpu_ctx *c) {
     void *ptrs[] = {c->Bmax.As, c->Bmax.fak, c->Bmax.b, c->Bmax.x, c->Bmax.r, c->Bmax.L, c->Bmax.y,
-                    c->Bmax.status, c->Bmax.active, (void *)c->Bmax.nactive, c->Bmax.pota,
-                    c->Bmax.potmax, c->d_ks, c->d_ls};
+                    c->Bmax.status, c->Bmax.active, c->Bmax.pota, c->Bmax.potmax, c->d_ks, c->d_ls};
     for (void *p : ptrs)
         if (p) {
             cudaFreeAsync(p, c->st);
@@ -94,11 +101,10 @@ int ensure_batch(crgpu_ctx *c, int want) {
     e = e ? e : dalloc(c, &y, (size_t)want * nr * n * esz);
     e = e ? e : dalloc(c, &B.status, (size_t)want);
     e = e ? e : dalloc(c, &B.active, (size_t)want * nr);
-    {
-        double *cnt = nullptr;  // [0]: int count (+pad), [1]: double zmax
-        e = e ? e : dalloc(c, &cnt, 2);
-        B.nactive = (int *)cnt;
-        B.zmax = cnt + 1;
+    if (!e && !c->d_refine) {
+        char *cnt = nullptr;  // [2][kRefineCap] steps of {int count, pad, double zmax}
+        e = dalloc(c, &cnt, 2 * kRefineCap * sizeof(RefineCount));
+        c->d_refine = cnt;
     }
     e = e ? e : dalloc(c, &c->d_ks, (size_t)want);
     e = e ? e : dalloc(c, &c->d_ls, (size_t)want);
@@ -154,6 +160,28 @@ DevBatch batch_view(crgpu_ctx *c, int ns) {
     return B;
 }
 
+// systems s0 .. s0+m-1 of a batch view as a batch of their own
+DevBatch sub_view(const crgpu_ctx *c, const DevBatch &B, int s0, int m) {
+    const size_t n = c->hg.n, nnz = c->pat.nnz, nr = c->nrhs;
+    const size_t esz = c->precision == CRGPU_MIXED ? sizeof(float2) : sizeof(double2);
+    DevBatch S = B;
+    S.nsys = m;
+    S.ks += s0;
+    S.ls += s0;
+    S.As += s0 * nnz;
+    S.fak += s0 * n;
+    S.b += s0 * nr * n;
+    S.x += s0 * nr * n;
+    S.r += s0 * nr * n;
+    S.L = (char *)B.L + s0 * B.lpitch * esz;
+    S.y = (char *)B.y + s0 * nr * n * esz;
+    S.status += s0;
+    S.active += s0 * nr;
+    if (B.pota) S.pota += s0 * n;
+    if (B.potmax) S.potmax += s0;
+    return S;
+}
+
 int load_batch(crgpu_ctx *c, int s0, int ns) {
     CUCHECK(c, cudaMemcpyAsync(c->d_ks, c->sys_k.data() + s0, sizeof(int32_t) * ns, cudaMemcpyHostToDevice, c->st));
     CUCHECK(c, cudaMemcpyAsync(c->d_ls, c->sys_l.data() + s0, sizeof(int32_t) * ns, cudaMemcpyHostToDevice, c->st));
@@ -161,54 +189,75 @@ int load_batch(crgpu_ctx *c, int s0, int ns) {
     return 0;
 }
 
-// Solves the ns systems of the current batch, whose band factors are in
-// B.L, for the right-hand sides in B.b (src/vre.f90); the forward sweep was
+// Solves the systems of batch view B, whose band factors are in B.L, for the
+// right-hand sides in B.b (src/vre.f90) on stream st; the forward sweep was
 // already done inside the factorisation when fused.  Mixed precision adds the
-// FP64 refinement.  The FP64 solution ends in B.x.
-int solve_batch(crgpu_ctx *c, int ns, bool fused) {
+// FP64 refinement: every step is launched without waiting for the host (a
+// step whose predecessor left no item active returns at once), with its
+// counters in refinement array `slot`.  The FP64 solution ends in B.x.
+int solve_view(crgpu_ctx *c, const DevBatch &B, bool fused, cudaStream_t st, int slot) {
     DevProblem &P = c->P;
     const bool mixed = c->precision == CRGPU_MIXED;
     const int nr = c->nrhs;
-    DevBatch B = batch_view(c, ns);
     DevBatch Bs = B;
     Bs.active = nullptr;
+    Bs.nactive = nullptr;
+    Bs.zmax = nullptr;
+    Bs.nprev = nullptr;
     if (!fused) {
-        launch_forward_solve(P, Bs, nr, mixed, B.b, c->st);
+        launch_forward_solve(P, Bs, nr, mixed, B.b, st);
         c->stats.kernel_launches += 1;
     }
-    launch_back_solve(P, Bs, nr, mixed, c->st);
+    launch_back_solve(P, Bs, nr, mixed, st);
     c->stats.kernel_launches += 1;
     if (!mixed) {
-        launch_copy_solution(P, B, nr, c->st);
+        launch_copy_solution(P, B, nr, st);
         c->stats.kernel_launches += 1;
         return 0;
     }
-    // all items active: a host array of ones (a memset cannot write int 1)
-    std::vector<int> ones((size_t)ns * nr, 1);
-    CUCHECK(c, cudaMemcpyAsync(B.active, ones.data(), sizeof(int) * ones.size(), cudaMemcpyHostToDevice, c->st));
+    RefineCount *cnt = (RefineCount *)c->d_refine + (size_t)slot * kRefineCap;
+    const int steps = std::min(c->refine_maxit, kRefineCap);
+    CUCHECK(c, cudaMemsetAsync(cnt, 0, sizeof(RefineCount) * kRefineCap, st));
+    launch_fill_active(B, nr, st);
     DevBatch B0 = B;
     B0.zmax = nullptr;
     B0.nactive = nullptr;
-    launch_accumulate(P, B0, nr, true, c->refine_tol, c->st);
-    c->stats.kernel_launches += 1;
-    for (int it = 0; it < c->refine_maxit; it++) {
-        CUCHECK(c, cudaMemsetAsync(B.nactive, 0, 2 * sizeof(double), c->st));
-        launch_residual(P, B, nr, c->st);
-        launch_forward_solve(P, B, nr, true, B.r, c->st);
-        launch_back_solve(P, B, nr, true, c->st);
-        launch_accumulate(P, B, nr, false, c->refine_tol, c->st);
+    B0.nprev = nullptr;
+    launch_accumulate(P, B0, nr, true, c->refine_tol, st);
+    c->stats.kernel_launches += 2;
+    for (int it = 0; it < steps; it++) {
+        DevBatch Bi = B;
+        Bi.nactive = &cnt[it].n;
+        Bi.zmax = &cnt[it].z;
+        Bi.nprev = it > 0 ? &cnt[it - 1].n : nullptr;
+        launch_residual(P, Bi, nr, st);
+        launch_forward_solve(P, Bi, nr, true, B.r, st);
+        launch_back_solve(P, Bi, nr, true, st);
+        launch_accumulate(P, Bi, nr, false, c->refine_tol, st);
         c->stats.kernel_launches += 4;
-        c->stats.refine_iterations = std::max(c->stats.refine_iterations, it + 1);
-        struct {
-            int n;
-            int pad;
-            double z;
-        } h{};
-        CUCHECK(c, cudaMemcpyAsync(&h, B.nactive, sizeof(h), cudaMemcpyDeviceToHost, c->st));
-        CUCHECK(c, cudaStreamSynchronize(c->st));
-        c->last_refine_zmax = h.z;
-        c->stats.refine_last_correction = h.z;
-        if (h.n == 0) break;
+    }
+    c->refine_used[slot] = std::max(c->refine_used[slot], steps);
+    return 0;
+}
+
+int solve_batch(crgpu_ctx *c, int ns, bool fused) { return solve_view(c, batch_view(c, ns), fused, c->st, 0); }
+
+// refinement statistics of the steps launched since the last collection (the
+// streams must be idle): steps that ran, and the largest relative correction
+// of the last one
+int collect_refine_stats(crgpu_ctx *c) {
+    for (int slot = 0; slot < 2; slot++) {
+        const int used = c->refine_used[slot];
+        if (!used) continue;
+        std::vector<RefineCount> h(used);
+        CUCHECK(c, cudaMemcpy(h.data(), (RefineCount *)c->d_refine + (size_t)slot * kRefineCap,
+                              sizeof(RefineCount) * used, cudaMemcpyDeviceToHost));
+        int ran = 0;  // step it ran if it was the first or its predecessor left items active
+        for (int it = 0; it < used; it++)
+            if (it == 0 || h[it - 1].n > 0) ran = it + 1;
+        c->stats.refine_iterations = std::max(c->stats.refine_iterations, ran);
+        if (ran > 0) c->stats.refine_last_correction = std::max(c->stats.refine_last_correction, h[ran - 1].z);
+        c->refine_used[slot] = 0;
     }
     return 0;
 }
@@ -224,16 +273,26 @@ int assemble_batch(crgpu_ctx *c, const double2 *d_sigma, int ns) {
 
 // band factorisation of the current batch (src/chol.f90); with fuse the
 // forward sweep of the right-hand sides in B.b runs inside the factor
-int run_factor(crgpu_ctx *c, int ns, int fuse) {
-    DevBatch B = batch_view(c, ns);
+int run_factor_view(crgpu_ctx *c, const DevBatch &B, int fuse, cudaStream_t st) {
     if (c->precision == CRGPU_MIXED) {
-        int e = launch_factor_mixed(c->P, B, fuse, c->nsm, c->st);
+        int e = launch_factor_mixed(c->P, B, fuse, c->nsm, st);
         if (e) return fail(c, e, "mixed precision: band width beyond the supported window");
     } else {
-        launch_factor_plain(c->P, B, fuse, c->nsm, c->st);
+        launch_factor_plain(c->P, B, fuse, c->nsm, st);
     }
     c->stats.kernel_launches += 1;
     return 0;
+}
+
+int run_factor(crgpu_ctx *c, int ns, int fuse) { return run_factor_view(c, batch_view(c, ns), fuse, c->st); }
+
+// systems of a batch beyond the last full round of the tensor-core factor
+// (two resident blocks per SM): they are factored and solved on the high
+// priority stream while the full rounds' systems are solved.  0: no split.
+int tail_systems(const crgpu_ctx *c, int ns) {
+    if (c->precision != CRGPU_MIXED || c->hg.mb + 4 > 128 || c->nsm <= 0) return 0;
+    const int round = 2 * c->nsm, tail = ns % round;
+    return (ns > round && tail > 0 && tail <= round / 2) ? tail : 0;
 }
 
 // the forward block on device-resident sigma
@@ -281,12 +340,29 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
             launch_rhs(P, B, nr, c->lsink, c->nsink, c->st);
             c->stats.kernel_launches += 1;
         }
+        const int tail = tail_systems(c, ns);
         cudaEventRecord(f0, c->st);
-        e = run_factor(c, ns, fuse);
-        if (e) return e;
-        cudaEventRecord(f1, c->st);
-        e = solve_batch(c, ns, fuse != 0);
-        if (e) return e;
+        if (!tail) {
+            e = run_factor(c, ns, fuse);
+            if (e) return e;
+            cudaEventRecord(f1, c->st);
+            e = solve_view(c, B, fuse != 0, c->st, 0);
+            if (e) return e;
+        } else {
+            // full rounds on st; the last, partial round starts on st_hi once they are
+            // done, beside the full rounds' solves, and is solved there
+            const DevBatch Bf = sub_view(c, B, 0, ns - tail), Bt = sub_view(c, B, ns - tail, tail);
+            e = run_factor_view(c, Bf, fuse, c->st);
+            if (e) return e;
+            cudaEventRecord(f1, c->st);
+            CUCHECK(c, cudaStreamWaitEvent(c->st_hi, f1, 0));
+            e = run_factor_view(c, Bt, fuse, c->st_hi);
+            if (!e) e = solve_view(c, Bt, fuse != 0, c->st_hi, 1);
+            if (!e) e = solve_view(c, Bf, fuse != 0, c->st, 0);
+            if (e) return e;
+            CUCHECK(c, cudaEventRecord(c->ev_join, c->st_hi));
+            CUCHECK(c, cudaStreamWaitEvent(c->st, c->ev_join, 0));
+        }
         launch_kpot(P, B, nr, c->d_kpot, c->st);
         c->stats.kernel_launches += 1;
         cudaEventRecord(f2, c->st);
@@ -314,6 +390,7 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
     c->stats.kernel_launches += 2;
     cudaEventRecord(ev[1], c->st);
     int ce = check_device_errors(c, nullptr, 0);
+    if (!ce) ce = collect_refine_stats(c);
     float tf = 0.f;
     cudaEventElapsedTime(&tf, ev[0], ev[1]);
     c->stats.ms_forward = tf;
@@ -383,6 +460,7 @@ int run_adjoint(crgpu_ctx *c, const double2 *d_g, double2 *d_grad) {
     c->stats.kernel_launches += 1;
     cudaEventRecord(a1, c->st);
     e = check_device_errors(c, nullptr, 0);
+    if (!e) e = collect_refine_stats(c);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, a0, a1);
     c->stats.ms_adjoint = ms;
@@ -426,6 +504,12 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
     c->lsr = (sv->lsr && c->hg.lbeta && sv->swrtr != 0) ? 1 : 0;
     cudaError_t ce = cudaStreamCreateWithFlags(&c->own_st, cudaStreamNonBlocking);
     c->st = c->own_st;
+    if (ce == cudaSuccess) {
+        int lo = 0, hi = 0;
+        cudaDeviceGetStreamPriorityRange(&lo, &hi);
+        ce = cudaStreamCreateWithPriority(&c->st_hi, cudaStreamNonBlocking, hi);
+    }
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
     if (ce != cudaSuccess) {
         c->last_error = cudaGetErrorString(ce);
         *out = c;
@@ -581,6 +665,8 @@ int crgpu_destroy(crgpu_ctx *c) {
     if (c->d_upd) cudaFreeAsync(c->d_upd, c->st);
     if (c->own_st) cudaStreamDestroy(c->own_st);
     if (c->copy_st) cudaStreamDestroy(c->copy_st);
+    if (c->st_hi) cudaStreamDestroy(c->st_hi);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     delete c;
     return 0;
 }
@@ -588,7 +674,7 @@ int crgpu_destroy(crgpu_ctx *c) {
 const char *crgpu_last_error(const crgpu_ctx *c) { return c ? c->last_error.c_str() : "null context"; }
 
 int crgpu_set_refinement(crgpu_ctx *c, int32_t maxit, double tol) {
-    if (!c || maxit < 0 || !(tol >= 0.0)) return ERR_ARG;
+    if (!c || maxit < 0 || maxit > kRefineCap || !(tol >= 0.0)) return ERR_ARG;
     c->refine_maxit = maxit;
     c->refine_tol = tol;
     return 0;

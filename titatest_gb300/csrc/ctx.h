@@ -18,6 +18,8 @@ struct crgpu_ctx {
     int swrtr = 1, lsr = 0, lsink = 0, nsink = -1, lsytop = 0;
     cudaStream_t st = nullptr, own_st = nullptr;
     cudaStream_t copy_st = nullptr;  // device -> host copies overlapped with compute
+    cudaStream_t st_hi = nullptr;    // high priority: the last, partial round of factors and its solves
+    cudaEvent_t ev_join = nullptr;
     int nsm = 0, device = 0;
     std::vector<void *> allocs;
     // device state
@@ -34,7 +36,10 @@ struct crgpu_ctx {
     // options
     int refine_maxit = 8;
     double refine_tol = 1e-10;
-    double last_refine_zmax = 0.0;
+    // refinement step counters on the device, one array per sub-batch of the
+    // current batch: {active count, pad, largest relative correction} per step
+    void *d_refine = nullptr;
+    int refine_used[2] = {0, 0};  // steps launched on each array since the last collection
     int64_t mem_budget = 0;
     bool have_forward = false;
     bool factors_resident = false;  // band factors of every system still in Bmax (one batch)

@@ -52,6 +52,7 @@ struct DevBatch {
     int *status;      // [nsys]        0 or reference error code
     int *active;      // [nsys]        refinement still running
     int *nactive;     // count of items still refining after the last correction
+    const int *nprev; // that count after the previous refinement step (0: the step's kernels return at once)
     double *zmax;     // largest relative correction of the last refinement step
     double2 *pota;    // [nsys][n] analytic potentials (singularity removal)
     double *potmax;   // [nsys]

@@ -40,6 +40,7 @@ void launch_back_solve(const DevProblem &P, const DevBatch &B, int nrhs, bool mi
                        cudaStream_t st);
 // refinement helpers (FP64)
 void launch_residual(const DevProblem &P, const DevBatch &B, int nrhs, cudaStream_t st);
+void launch_fill_active(const DevBatch &B, int nrhs, cudaStream_t st);
 void launch_accumulate(const DevProblem &P, const DevBatch &B, int nrhs, bool first,
                        double tol, cudaStream_t st);
 void launch_copy_solution(const DevProblem &P, const DevBatch &B, int nrhs, cudaStream_t st);

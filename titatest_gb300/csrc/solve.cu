@@ -130,6 +130,7 @@ __global__ __launch_bounds__(32) void k_fwd(DevProblem P, DevBatch B, int nrhs, 
     const int n = P.n, mb = P.mb, W = mb + 1, lane = threadIdx.x;
     const int item = blockIdx.x;
     if (item >= B.nsys * nrhs) return;
+    if (B.nprev && *B.nprev == 0) return;
     if (B.active && !B.active[item]) return;
     const SolveLayout lay = solve_layout<T>(W, wmask + 1);
     uint64_t *bar = (uint64_t *)(sm_raw + lay.bars);
@@ -213,6 +214,7 @@ __global__ __launch_bounds__(32) void k_bwd(DevProblem P, DevBatch B, int nrhs, 
     const int n = P.n, mb = P.mb, W = mb + 1, lane = threadIdx.x;
     const int item = blockIdx.x;
     if (item >= B.nsys * nrhs) return;
+    if (B.nprev && *B.nprev == 0) return;
     if (B.active && !B.active[item]) return;
     const SolveLayout lay = solve_layout<T>(W, wmask + 1);
     uint64_t *bar = (uint64_t *)(sm_raw + lay.bars);
@@ -337,6 +339,7 @@ __global__ void k_residual(DevProblem P, DevBatch B, int nrhs) {
     size_t nitems = (size_t)B.nsys * nrhs;
     if (gid >= nitems * P.n) return;
     int item = (int)(gid / P.n), i = (int)(gid % P.n);
+    if (B.nprev && *B.nprev == 0) return;
     if (B.active && !B.active[item]) return;
     int s = item / nrhs;
     const double2 *as = B.As + (size_t)s * P.nnz;
@@ -363,6 +366,7 @@ void launch_residual(const DevProblem &P, const DevBatch &B, int nrhs, cudaStrea
 // refining once max|z| <= tol * max|x|.
 __global__ void k_accumulate(DevProblem P, DevBatch B, int nrhs, int first, double tol) {
     int item = blockIdx.x;
+    if (B.nprev && *B.nprev == 0) return;
     if (B.active && !B.active[item]) return;
     const float2 *z = (const float2 *)B.y + (size_t)item * P.n;
     double2 *x = B.x + (size_t)item * P.n;
@@ -404,6 +408,17 @@ void launch_accumulate(const DevProblem &P, const DevBatch &B, int nrhs, bool fi
                        cudaStream_t st) {
     int nitems = B.nsys * nrhs;
     k_accumulate<<<nitems, 256, 0, st>>>(P, B, nrhs, first ? 1 : 0, tol);
+}
+
+// every item of the batch starts refining
+__global__ void k_fill_active(DevBatch B, int nitems) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nitems) B.active[i] = 1;
+}
+
+void launch_fill_active(const DevBatch &B, int nrhs, cudaStream_t st) {
+    const int nitems = B.nsys * nrhs;
+    k_fill_active<<<(nitems + 255) / 256, 256, 0, st>>>(B, nitems);
 }
 
 // plain mode: the back sweep left x (complex128) in B.y; copy to B.x
