@@ -3,7 +3,7 @@
 //
 // One warp solves one right-hand side, kRB = 8 band rows at a time.  A
 // block's rows are contiguous in the band layout (8 * (mb+1) entries), so one
-// bulk copy per block brings them into shared memory kStages blocks ahead;
+// bulk copy per block brings them into shared memory S blocks ahead;
 // the working vector lives in a shared window.  Per block the dependent
 // chain is one warp reduction (forward) and an 8-step triangle of shuffles;
 // the rest is independent multiply-adds over the lanes' columns.
@@ -53,8 +53,11 @@ struct Ops<float2> {
     }
 };
 
-constexpr int kRB = 8;      // rows per block of a sweep
-constexpr int kStages = 2;  // blocks of band rows in flight per warp
+constexpr int kRB = 8;  // rows per block of a sweep
+// blocks of band rows in flight per warp: 2 when many sweeps share the GPU
+// (together they saturate HBM), 8 when few do and each is latency bound
+constexpr int kStagesMany = 2, kStagesFew = 8;
+constexpr int kFewItems = 256;  // sweeps per launch up to which kStagesFew is used
 
 // Per-warp shared memory (byte offsets): stage barriers, the right-hand side
 // of each staged block (forward sweep), the staged band rows, the window of
@@ -63,15 +66,15 @@ constexpr int kStages = 2;  // blocks of band rows in flight per warp
 struct SolveLayout {
     int bars, rhs, rows, win, ent, total;
 };
-template <typename T>
+template <typename T, int S>
 __host__ __device__ inline SolveLayout solve_layout(int W, int WW) {
     SolveLayout s;
-    s.bars = 0;
+    s.bars = 0;  // S <= 8 barriers
     s.rhs = 64;
-    s.rows = s.rhs + kStages * kRB * (int)sizeof(double2);
-    s.win = s.rows + kStages * kRB * W * (int)sizeof(T);
+    s.rows = s.rhs + S * kRB * (int)sizeof(double2);
+    s.win = s.rows + S * kRB * W * (int)sizeof(T);
     s.ent = s.win + WW * (int)sizeof(T);
-    s.total = (s.ent + kStages * kRB * (int)sizeof(T) + 127) & ~127;
+    s.total = (s.ent + S * kRB * (int)sizeof(T) + 127) & ~127;
     return s;
 }
 
@@ -109,10 +112,11 @@ __device__ __forceinline__ T reduce_rows8(const T (&a)[kRB], int lane) {
     return d;
 }
 
+template <int S>
 __device__ __forceinline__ void solve_timeout(const DevProblem &P, uint64_t *bar, int next_use, int last_use) {
     // report, then let the copies still in flight land before the block exits
     if ((threadIdx.x & 31) == 0) atomicCAS(P.err, 0, ERR_TIMEOUT);
-    for (int u = next_use; u <= last_use; u++) mbar_wait(&bar[u % kStages], (u / kStages) & 1);
+    for (int u = next_use; u <= last_use; u++) mbar_wait(&bar[u % S], (u / S) & 1);
     cp_wait<0>();
 }
 
@@ -122,8 +126,8 @@ __device__ __forceinline__ void solve_timeout(const DevProblem &P, uint64_t *bar
 //   (2) warp reduction of the 8 sums
 //   (3) the 8x8 triangle, y_q broadcast from the lanes of row q
 // The block's band rows (contiguous, 8 W entries) and right-hand side arrive
-// by bulk copy kStages blocks ahead.
-template <typename T>
+// by bulk copy S blocks ahead.
+template <typename T, int S>
 __global__ __launch_bounds__(32) void k_fwd(DevProblem P, DevBatch B, int nrhs, const double2 *__restrict__ rin,
                                              int wmask) {
     extern __shared__ __align__(128) unsigned char sm_raw[];
@@ -132,7 +136,7 @@ __global__ __launch_bounds__(32) void k_fwd(DevProblem P, DevBatch B, int nrhs, 
     if (item >= B.nsys * nrhs) return;
     if (B.nprev && *B.nprev == 0) return;
     if (B.active && !B.active[item]) return;
-    const SolveLayout lay = solve_layout<T>(W, wmask + 1);
+    const SolveLayout lay = solve_layout<T, S>(W, wmask + 1);
     uint64_t *bar = (uint64_t *)(sm_raw + lay.bars);
     double2 *rv = (double2 *)(sm_raw + lay.rhs);
     T *rows = (T *)(sm_raw + lay.rows);
@@ -143,7 +147,7 @@ __global__ __launch_bounds__(32) void k_fwd(DevProblem P, DevBatch B, int nrhs, 
     const int nblk = (n + kRB - 1) / kRB;
     auto issue = [&](int t) {
         if (t >= nblk) return;
-        const int st = t % kStages, i0 = t * kRB, nr = min(kRB, n - i0);
+        const int st = t % S, i0 = t * kRB, nr = min(kRB, n - i0);
         const uint32_t bl = ((uint32_t)(nr * W * (int)sizeof(T)) + 15u) & ~15u;
         const uint32_t br = (uint32_t)nr * (uint32_t)sizeof(double2);
         mbar_expect_tx(&bar[st], bl + br);
@@ -151,17 +155,17 @@ __global__ __launch_bounds__(32) void k_fwd(DevProblem P, DevBatch B, int nrhs, 
         bulk_g2s(rv + st * kRB, r + i0, br, &bar[st]);
     };
     if (lane == 0) {
-        for (int q = 0; q < kStages; q++) mbar_init(&bar[q], 1);
+        for (int q = 0; q < S; q++) mbar_init(&bar[q], 1);
         mbar_init_fence();
-        for (int t = 0; t < kStages; t++) issue(t);
+        for (int t = 0; t < S; t++) issue(t);
     }
     __syncwarp();
     const int myr = lane >> 2;
     for (int t = 0; t < nblk; t++) {
-        const int st = t % kStages, i0 = t * kRB, nr = min(kRB, n - i0);
-        const bool ok = mbar_wait(&bar[st], (t / kStages) & 1);
+        const int st = t % S, i0 = t * kRB, nr = min(kRB, n - i0);
+        const bool ok = mbar_wait(&bar[st], (t / S) & 1);
         if (!__all_sync(0xffffffffu, ok)) {
-            solve_timeout(P, bar, t, min(nblk - 1, t + kStages - 1));
+            solve_timeout<S>(P, bar, t, min(nblk - 1, t + S - 1));
             return;
         }
         const T *Lb = rows + (size_t)st * kRB * W;
@@ -197,7 +201,7 @@ __global__ __launch_bounds__(32) void k_fwd(DevProblem P, DevBatch B, int nrhs, 
         __syncwarp();
         if (lane == 0) {
             fence_proxy_async();
-            issue(t + kStages);
+            issue(t + S);
         }
     }
 }
@@ -208,7 +212,7 @@ __global__ __launch_bounds__(32) void k_fwd(DevProblem P, DevBatch B, int nrhs, 
 //   (2) w_j -= sum_r L(r, j) x_r for the columns j < i0, lanes own columns
 // w lives in the shared window; entries enter it (w_j = y_j) when the first
 // block that touches column j is processed.
-template <typename T>
+template <typename T, int S>
 __global__ __launch_bounds__(32) void k_bwd(DevProblem P, DevBatch B, int nrhs, int wmask) {
     extern __shared__ __align__(128) unsigned char sm_raw[];
     const int n = P.n, mb = P.mb, W = mb + 1, lane = threadIdx.x;
@@ -216,7 +220,7 @@ __global__ __launch_bounds__(32) void k_bwd(DevProblem P, DevBatch B, int nrhs, 
     if (item >= B.nsys * nrhs) return;
     if (B.nprev && *B.nprev == 0) return;
     if (B.active && !B.active[item]) return;
-    const SolveLayout lay = solve_layout<T>(W, wmask + 1);
+    const SolveLayout lay = solve_layout<T, S>(W, wmask + 1);
     uint64_t *bar = (uint64_t *)(sm_raw + lay.bars);
     T *rows = (T *)(sm_raw + lay.rows);
     T *win = (T *)(sm_raw + lay.win);
@@ -228,7 +232,7 @@ __global__ __launch_bounds__(32) void k_bwd(DevProblem P, DevBatch B, int nrhs, 
     auto issue = [&](int u) {
         const int t = nblk - 1 - u;
         if (t >= 0) {
-            const int st = u % kStages, i0 = t * kRB;
+            const int st = u % S, i0 = t * kRB;
             if (lane == 0) {
                 const int nr = min(kRB, n - i0);
                 const uint32_t bl = ((uint32_t)(nr * W * (int)sizeof(T)) + 15u) & ~15u;
@@ -243,18 +247,18 @@ __global__ __launch_bounds__(32) void k_bwd(DevProblem P, DevBatch B, int nrhs, 
     const int i0l = (nblk - 1) * kRB;
     for (int j = max(0, i0l - mb) + lane; j < n; j += 32) win[j & wmask] = y[j];
     if (lane == 0) {
-        for (int q = 0; q < kStages; q++) mbar_init(&bar[q], 1);
+        for (int q = 0; q < S; q++) mbar_init(&bar[q], 1);
         mbar_init_fence();
     }
     __syncwarp();
-    for (int u = 0; u < kStages; u++) issue(u);
+    for (int u = 0; u < S; u++) issue(u);
     const int myr = lane >> 2;
     for (int u = 0; u < nblk; u++) {
-        const int t = nblk - 1 - u, st = u % kStages, i0 = t * kRB, nr = min(kRB, n - i0);
-        const bool ok = mbar_wait(&bar[st], (u / kStages) & 1);
-        cp_wait<kStages - 1>();
+        const int t = nblk - 1 - u, st = u % S, i0 = t * kRB, nr = min(kRB, n - i0);
+        const bool ok = mbar_wait(&bar[st], (u / S) & 1);
+        cp_wait<S - 1>();
         if (!__all_sync(0xffffffffu, ok)) {
-            solve_timeout(P, bar, u, min(nblk - 1, u + kStages - 1));
+            solve_timeout<S>(P, bar, u, min(nblk - 1, u + S - 1));
             return;
         }
         {
@@ -289,7 +293,7 @@ __global__ __launch_bounds__(32) void k_bwd(DevProblem P, DevBatch B, int nrhs, 
         }
         __syncwarp();
         if (lane == 0) fence_proxy_async();
-        issue(u + kStages);
+        issue(u + S);
     }
     cp_wait<0>();
 }
@@ -297,42 +301,51 @@ __global__ __launch_bounds__(32) void k_bwd(DevProblem P, DevBatch B, int nrhs, 
 // The kernels' dynamic shared memory depends on the band width; contexts of
 // different widths may launch concurrently from several host threads, so the
 // limit is raised once to the device's opt-in maximum instead of per width.
-template <typename T>
+template <typename T, int S>
 static int set_solve_smem(int W, int WW) {
     static std::once_flag once;
     std::call_once(once, [] {
         int dev = 0, optin = 48 * 1024;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        cudaFuncSetAttribute(k_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-        cudaFuncSetAttribute(k_bwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_fwd<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_bwd<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     });
-    return solve_layout<T>(W, WW).total;
+    return solve_layout<T, S>(W, WW).total;
+}
+
+template <typename T, int S>
+static void fwd_launch(const DevProblem &P, const DevBatch &B, int nrhs, const double2 *rin, cudaStream_t st) {
+    const int nitems = B.nsys * nrhs, W = P.mb + 1, WW = solve_window(P.mb);
+    const int bytes = set_solve_smem<T, S>(W, WW);
+    k_fwd<T, S><<<nitems, 32, bytes, st>>>(P, B, nrhs, rin, WW - 1);
+}
+
+template <typename T, int S>
+static void bwd_launch(const DevProblem &P, const DevBatch &B, int nrhs, cudaStream_t st) {
+    const int nitems = B.nsys * nrhs, W = P.mb + 1, WW = solve_window(P.mb);
+    const int bytes = set_solve_smem<T, S>(W, WW);
+    k_bwd<T, S><<<nitems, 32, bytes, st>>>(P, B, nrhs, WW - 1);
+}
+
+// the deep pipeline for few sweeps, when its staging fits the block's shared memory
+template <typename T>
+static bool use_few(const DevProblem &P, int nitems) {
+    return nitems <= kFewItems && solve_layout<T, kStagesFew>(P.mb + 1, solve_window(P.mb)).total <= 200 * 1024;
 }
 
 void launch_forward_solve(const DevProblem &P, const DevBatch &B, int nrhs, bool mixed, const double2 *rin,
                           cudaStream_t st) {
-    const int nitems = B.nsys * nrhs, W = P.mb + 1, WW = solve_window(P.mb);
-    if (mixed) {
-        const int bytes = set_solve_smem<float2>(W, WW);
-        k_fwd<float2><<<nitems, 32, bytes, st>>>(P, B, nrhs, rin, WW - 1);
-    } else {
-        const int bytes = set_solve_smem<double2>(W, WW);
-        k_fwd<double2><<<nitems, 32, bytes, st>>>(P, B, nrhs, rin, WW - 1);
-    }
+    const bool few = mixed ? use_few<float2>(P, B.nsys * nrhs) : use_few<double2>(P, B.nsys * nrhs);
+    if (mixed) few ? fwd_launch<float2, kStagesFew>(P, B, nrhs, rin, st) : fwd_launch<float2, kStagesMany>(P, B, nrhs, rin, st);
+    else few ? fwd_launch<double2, kStagesFew>(P, B, nrhs, rin, st) : fwd_launch<double2, kStagesMany>(P, B, nrhs, rin, st);
 }
 
 void launch_back_solve(const DevProblem &P, const DevBatch &B, int nrhs, bool mixed, cudaStream_t st) {
-    const int nitems = B.nsys * nrhs, W = P.mb + 1, WW = solve_window(P.mb);
-    if (mixed) {
-        const int bytes = set_solve_smem<float2>(W, WW);
-        k_bwd<float2><<<nitems, 32, bytes, st>>>(P, B, nrhs, WW - 1);
-    } else {
-        const int bytes = set_solve_smem<double2>(W, WW);
-        k_bwd<double2><<<nitems, 32, bytes, st>>>(P, B, nrhs, WW - 1);
-    }
+    const bool few = mixed ? use_few<float2>(P, B.nsys * nrhs) : use_few<double2>(P, B.nsys * nrhs);
+    if (mixed) few ? bwd_launch<float2, kStagesFew>(P, B, nrhs, st) : bwd_launch<float2, kStagesMany>(P, B, nrhs, st);
+    else few ? bwd_launch<double2, kStagesFew>(P, B, nrhs, st) : bwd_launch<double2, kStagesMany>(P, B, nrhs, st);
 }
-
 // r = b - A x with the full symmetric pattern (FP64)
 __global__ void k_residual(DevProblem P, DevBatch B, int nrhs) {
     size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
