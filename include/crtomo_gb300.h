@@ -127,7 +127,10 @@ int crgpu_forward_device(crgpu_ctx *ctx, const void *sigma_device, int32_t volt_
 /* Sensitivities of the last forward: src/bsens.f90:23-197 (mode 0, CRMod:
  * sens -= strom/pi * sum_k w_k ...) or src/bsensi.f90:23-194 (mode 1,
  * CRTomo: sens += sum_k w_k/pi ... * sigma_e / V_i).
- *   sens : sens(nanz, elanz) complex, column-major (src/alloci.f90) */
+ *   sens : sens(nanz, elanz) complex, column-major (src/alloci.f90)
+ * Mode 0 into page-locked host memory is written by the kernel directly;
+ * otherwise the device result is copied in chunks, overlapped with the
+ * computation (mode 1 keeps the device copy for crgpu_update). */
 int crgpu_sens(crgpu_ctx *ctx, int32_t mode, double *sens);
 int crgpu_sens_device(crgpu_ctx *ctx, int32_t mode, void *sens_device);
 

@@ -363,7 +363,7 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
             CUCHECK(c, cudaEventRecord(c->ev_join, c->st_hi));
             CUCHECK(c, cudaStreamWaitEvent(c->st, c->ev_join, 0));
         }
-        launch_kpot(P, B, nr, c->d_kpot, c->st);
+        launch_kpot(P, B, nr, c->d_kpot, c->d_kpot32, c->st);
         c->stats.kernel_launches += 1;
         cudaEventRecord(f2, c->st);
         c->stats.nbatches++;
@@ -621,6 +621,7 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
     if (!e) e = dalloc(c, &c->d_sigma, (size_t)hg.elanz);
     if (!e) e = dalloc(c, &c->d_adom, (size_t)c->K * c->pat.nnz);
     if (!e) e = dalloc(c, &c->d_kpot, (size_t)c->K * c->eanz * hg.n);
+    if (!e && precision == CRGPU_MIXED) e = dalloc(c, &c->d_kpot32, (size_t)c->K * c->eanz * hg.n);
     if (!e) e = dalloc(c, &c->d_hpot, (size_t)c->eanz * hg.n);
     if (!e) e = dalloc(c, &c->d_volt, (size_t)std::max(c->nanz, 1));
     if (!e) e = dalloc(c, &c->d_sigmaa, (size_t)std::max(c->nanz, 1));
@@ -732,7 +733,7 @@ int crgpu_sens_device(crgpu_ctx *c, int32_t mode, void *sens_device) {
     cudaEventCreate(&a);
     cudaEventCreate(&b);
     cudaEventRecord(a, c->st);
-    launch_bsens(c->P, c->d_kpot, c->d_sigma, c->d_volt, mode, c->precision == CRGPU_MIXED,
+    launch_bsens(c->P, c->d_kpot, c->d_kpot32, c->d_sigma, c->d_volt, mode, c->precision == CRGPU_MIXED,
                  (double2 *)sens_device, c->st);
     c->last_sens = (const double2 *)sens_device;
     cudaEventRecord(b, c->st);
@@ -758,6 +759,30 @@ int crgpu_sens(crgpu_ctx *c, int32_t mode, double *sens) {
         int e = dalloc(c, &c->d_sens, cnt);
         if (e) return e;
     }
+    // CRMod sensitivities into pinned (page-locked) host memory are written by
+    // the kernel itself, over the host link, while it computes; otherwise
+    // chunked copies of the device array (which crgpu_update reads for mode 1)
+    cudaPointerAttributes pa{};
+    if (mode == 0 && cudaPointerGetAttributes(&pa, sens) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+        pa.devicePointer) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, c->st);
+        launch_bsens(c->P, c->d_kpot, c->d_kpot32, c->d_sigma, c->d_volt, mode, c->precision == CRGPU_MIXED,
+                     (double2 *)pa.devicePointer, c->st);
+        c->stats.kernel_launches += 1;
+        cudaEventRecord(b, c->st);
+        CUCHECK(c, cudaStreamSynchronize(c->st));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        c->stats.ms_sens = ms;
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        CUCHECK(c, cudaGetLastError());
+        return 0;
+    }
+    cudaGetLastError();  // a pageable pointer is not an error
     if (!c->copy_st) CUCHECK(c, cudaStreamCreateWithFlags(&c->copy_st, cudaStreamNonBlocking));
     constexpr int kChunks = 8;
     cudaEvent_t a, b, done[kChunks];
@@ -769,7 +794,8 @@ int crgpu_sens(crgpu_ctx *c, int32_t mode, double *sens) {
     for (int q = 0; q < kChunks; q++) {
         const int e0 = q * per, ne = std::min<int>(per, (int)manz - e0);
         if (ne <= 0) break;
-        launch_bsens(c->P, c->d_kpot, c->d_sigma, c->d_volt, mode, c->precision == CRGPU_MIXED, c->d_sens, c->st, e0,
+        launch_bsens(c->P, c->d_kpot, c->d_kpot32, c->d_sigma, c->d_volt, mode, c->precision == CRGPU_MIXED,
+                     c->d_sens, c->st, e0,
                      ne);
         c->stats.kernel_launches += 1;
         CUCHECK(c, cudaEventRecord(done[q], c->st));

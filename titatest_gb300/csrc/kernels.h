@@ -44,7 +44,9 @@ void launch_fill_active(const DevBatch &B, int nrhs, cudaStream_t st);
 void launch_accumulate(const DevProblem &P, const DevBatch &B, int nrhs, bool first,
                        double tol, cudaStream_t st);
 void launch_copy_solution(const DevProblem &P, const DevBatch &B, int nrhs, cudaStream_t st);
-void launch_kpot(const DevProblem &P, const DevBatch &B, int nrhs, double2 *kpot,
+// kpot (complex128) and, when kpot32 is given, its complex64 copy for the
+// mixed-precision Jacobian
+void launch_kpot(const DevProblem &P, const DevBatch &B, int nrhs, double2 *kpot, float2 *kpot32,
                  cudaStream_t st);
 
 // back-transform and voltages (src/rtrafo.f90, src/bvolt.f90, src/bvolti.f90)
@@ -57,9 +59,11 @@ void launch_bvolt(const DevProblem &P, const double2 *hpot, int mode, const doub
 // Jacobian on the tensor cores (Gram form, complex64 contraction; src/bsens.f90
 // mode, eanz <= 127)
 bool sens_tc_supported(const DevProblem &P, int mode);
-void launch_sens_tc(const DevProblem &P, const double2 *kpot, double2 *sens, cudaStream_t st, int e_first,
+void launch_sens_tc(const DevProblem &P, const float2 *kpot32, double2 *sens, cudaStream_t st, int e_first,
                     int e_count);
-void launch_bsens(const DevProblem &P, const double2 *kpot, const double2 *sigma,
+// single: the complex64 contraction from kpot32 (mixed precision); else the
+// complex128 one from kpot
+void launch_bsens(const DevProblem &P, const double2 *kpot, const float2 *kpot32, const double2 *sigma,
                   const double2 *volt, int mode, bool single, double2 *sens, cudaStream_t st,
                   int e_first = 0, int e_count = -1);
 

@@ -83,21 +83,20 @@ struct SensT;
 template <>
 struct SensT<double> {
     using C = double2;
-    __device__ static C load(double2 v) { return v; }
     __device__ static C mk(double a, double b) { return cz(a, b); }
 };
 template <>
 struct SensT<float> {
     using C = float2;
-    __device__ static C load(double2 v) { return to_f(v); }
     __device__ static C mk(float a, float b) { return cf(a, b); }
 };
 
 // MODE 0: src/bsens.f90, MODE 1: src/bsensi.f90.  R: arithmetic type of the
-// element contraction (double: the reference arithmetic; float: the mixed
-// mode, with FP64 output).
+// element contraction (double: the reference arithmetic, from kpot; float: the
+// mixed mode, from its complex64 copy, with FP64 output).
 template <int MODE, typename R>
-__global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P, const double2 *__restrict__ kpot,
+__global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P,
+                                                         const typename SensT<R>::C *__restrict__ kpot,
                                                          const double2 *__restrict__ sigma,
                                                          const double2 *__restrict__ volt,
                                                          double2 *__restrict__ sens, int e_first) {
@@ -120,7 +119,7 @@ __global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P, const doub
             __syncthreads();
             for (int t = threadIdx.x; t < nk * eanz; t += kSensThreads) {
                 int q = t / eanz, l = t % eanz;
-                kp_sh[t] = SensT<R>::load(kpot[((size_t)k * eanz + l) * P.n + nodes[q]]);
+                kp_sh[t] = kpot[((size_t)k * eanz + l) * P.n + nodes[q]];
             }
             if (threadIdx.x < 10) kel[threadIdx.x] = (R)P.elbg[((size_t)k * P.elanz + e) * 10 + threadIdx.x];
             __syncthreads();
@@ -181,18 +180,19 @@ __global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P, const doub
     }
 }
 
-void launch_bsens(const DevProblem &P, const double2 *kpot, const double2 *sigma, const double2 *volt, int mode,
-                  bool single, double2 *sens, cudaStream_t st, int e_first, int e_count) {
+void launch_bsens(const DevProblem &P, const double2 *kpot, const float2 *kpot32, const double2 *sigma,
+                  const double2 *volt, int mode, bool single, double2 *sens, cudaStream_t st, int e_first,
+                  int e_count) {
     if (e_count < 0) e_count = P.elanz - e_first;
     if (e_count <= 0) return;
     if (single && sens_tc_supported(P, mode)) {
-        launch_sens_tc(P, kpot, sens, st, e_first, e_count);
+        launch_sens_tc(P, kpot32, sens, st, e_first, e_count);
         return;
     }
     if (single) {
         size_t smem = sizeof(float2) * 4 * P.eanz;
-        if (mode == 0) k_bsens<0, float><<<e_count, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens, e_first);
-        else k_bsens<1, float><<<e_count, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens, e_first);
+        if (mode == 0) k_bsens<0, float><<<e_count, kSensThreads, smem, st>>>(P, kpot32, sigma, volt, sens, e_first);
+        else k_bsens<1, float><<<e_count, kSensThreads, smem, st>>>(P, kpot32, sigma, volt, sens, e_first);
     } else {
         size_t smem = sizeof(double2) * 4 * P.eanz;
         if (mode == 0) k_bsens<0, double><<<e_count, kSensThreads, smem, st>>>(P, kpot, sigma, volt, sens, e_first);

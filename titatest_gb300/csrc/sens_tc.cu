@@ -60,7 +60,7 @@ struct StLayout {
     int off_b;               // offset of the B buffers inside one operand buffer
     int op_bytes;            // one operand buffer: A hi, A lo (128 x 8), B hi, B lo (N x 8) floats
     int p_bytes;             // P: E x E float2
-    int u_off, u_bytes;      // element potentials, two wavenumbers: [2][4][eanz] double2 (sized for E)
+    int u_off, u_bytes;      // element potentials, two wavenumbers: [2][4][eanz] float2 (sized for E)
     int total;
 };
 
@@ -72,7 +72,7 @@ __host__ __device__ inline StLayout st_layout(int E) {
     L.p_bytes = E * E * 8;
     const int region = (2 * L.op_bytes > L.p_bytes ? 2 * L.op_bytes : L.p_bytes);
     L.u_off = (region + 127) / 128 * 128;
-    L.u_bytes = 2 * 4 * E * 16;
+    L.u_bytes = 2 * 4 * E * 8;
     L.total = L.u_off + L.u_bytes + 192;  // + barriers, means and flags
     return L;
 }
@@ -86,7 +86,7 @@ struct StCtl {
 
 }  // namespace
 
-__global__ __launch_bounds__(kStThreads) void k_sens_tc(DevProblem P, const double2 *__restrict__ kpot,
+__global__ __launch_bounds__(kStThreads) void k_sens_tc(DevProblem P, const float2 *__restrict__ kpot,
                                                          double2 *__restrict__ sens, int e_first, int e_end) {
     extern __shared__ __align__(1024) unsigned char st_raw[];
     const int eanz = P.eanz, nanz = P.nanz, n = P.n, K = P.K;
@@ -95,7 +95,7 @@ __global__ __launch_bounds__(kStThreads) void k_sens_tc(DevProblem P, const doub
     const int N = Ly.N;
     auto opb = [&](int b) { return (float *)(st_raw + (size_t)b * Ly.op_bytes); };  // operand buffer b
     float2 *Psh = (float2 *)st_raw;
-    double2 *ush = (double2 *)(st_raw + Ly.u_off);  // [2][4][eanz]
+    float2 *ush = (float2 *)(st_raw + Ly.u_off);  // [2][4][eanz]
     StCtl &C = *(StCtl *)(st_raw + Ly.u_off + Ly.u_bytes);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -122,10 +122,10 @@ __global__ __launch_bounds__(kStThreads) void k_sens_tc(DevProblem P, const doub
 
     // potentials of element nodes, wavenumber k, all electrodes -> ush[slot]
     auto fetch_u = [&](int e, int nk, int k, int slot) {
-        double2 *dst = ush + (size_t)slot * 4 * eanz;
+        float2 *dst = ush + (size_t)slot * 4 * eanz;
         for (int t = tid; t < nk * eanz; t += kStThreads) {
             const int m = t / eanz, l = t % eanz;
-            cp_async16(&dst[m * eanz + l], kpot + ((size_t)k * eanz + l) * n + P.enodes[e * 4 + m]);
+            cp_async8(&dst[m * eanz + l], kpot + ((size_t)k * eanz + l) * n + P.enodes[e * 4 + m]);
         }
         cp_commit();
     };
@@ -161,11 +161,11 @@ __global__ __launch_bounds__(kStThreads) void k_sens_tc(DevProblem P, const doub
             }
             // ---- operands of wavenumber k into buffer kb
             {
-                const double2 *u = ush + (size_t)kb * 4 * eanz;
+                const float2 *u = ush + (size_t)kb * 4 * eanz;
                 float *A = opb(kb), *Bm = opb(kb) + Ly.off_b / 4;
                 // potential of electrode a at node m in FP32 (a == eanz: zero)
                 auto dev = [&](int m, int a) -> float2 {
-                    return (m < nk && a < eanz) ? to_f(u[m * eanz + a]) : cf(0.f, 0.f);
+                    return (m < nk && a < eanz) ? u[m * eanz + a] : cf(0.f, 0.f);
                 };
                 if (tid >= kStThreads - kStM) {  // A row a: [Re U | Im U]
                     const int a = tid - (kStThreads - kStM);
@@ -297,7 +297,7 @@ __global__ __launch_bounds__(kStThreads) void k_sens_tc(DevProblem P, const doub
 
 bool sens_tc_supported(const DevProblem &P, int mode) { return mode == 0 && P.eanz >= 1 && P.eanz + 1 <= kStM; }
 
-void launch_sens_tc(const DevProblem &P, const double2 *kpot, double2 *sens, cudaStream_t st, int e_first,
+void launch_sens_tc(const DevProblem &P, const float2 *kpot, double2 *sens, cudaStream_t st, int e_first,
                     int e_count) {
     const StLayout Ly = st_layout(P.eanz + 1);
     static std::once_flag once;

@@ -449,7 +449,7 @@ void launch_copy_solution(const DevProblem &P, const DevBatch &B, int nrhs, cuda
 }
 
 // kpot(j, l, k) = pot(j) * fak(j) with pot = -x (src/fem.f90:388-389)
-__global__ void k_kpot(DevProblem P, DevBatch B, int nrhs, double2 *kpot) {
+__global__ void k_kpot(DevProblem P, DevBatch B, int nrhs, double2 *kpot, float2 *kpot32) {
     size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t tot = (size_t)B.nsys * nrhs * P.n;
     if (gid >= tot) return;
@@ -461,12 +461,14 @@ __global__ void k_kpot(DevProblem P, DevBatch B, int nrhs, double2 *kpot) {
     double2 v = cz(-x.x * f, -x.y * f);
     if (P.lsr) v = cadd(v, B.pota[(size_t)s * P.n + i]);  // src/fem.f90:390-391
     kpot[((size_t)k * P.eanz + l) * P.n + i] = v;
+    if (kpot32) kpot32[((size_t)k * P.eanz + l) * P.n + i] = to_f(v);
 }
 
-void launch_kpot(const DevProblem &P, const DevBatch &B, int nrhs, double2 *kpot, cudaStream_t st) {
+void launch_kpot(const DevProblem &P, const DevBatch &B, int nrhs, double2 *kpot, float2 *kpot32,
+                 cudaStream_t st) {
     size_t tot = (size_t)B.nsys * nrhs * P.n;
     int nt = 256;
-    k_kpot<<<(unsigned)((tot + nt - 1) / nt), nt, 0, st>>>(P, B, nrhs, kpot);
+    k_kpot<<<(unsigned)((tot + nt - 1) / nt), nt, 0, st>>>(P, B, nrhs, kpot, kpot32);
 }
 
 }  // namespace crgpu
