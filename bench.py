@@ -223,6 +223,7 @@ def run_gpu(args):
     mixed = CRMod(g, sv, precision=MIXED)
     mixed.set_stream(stream.cuda_stream)
     mixed.set_refinement(args.refine_maxit, args.refine_tol)
+    tune = mixed.autotune(s.sigma) if not args.no_autotune else mixed.tune()
     K = mixed.kwnanz
 
     def unit(m):
@@ -325,7 +326,8 @@ def run_gpu(args):
                    "l2": "inputs larger than L2 (band factors of all systems, ~%d GB)" % int(
                        nsys * n * (mb + 1) * 8 / 1e9),
                    "refinement": {"maxit": args.refine_maxit, "tol": args.refine_tol,
-                                  "iterations": statistics.mean(iters)}},
+                                  "iterations": statistics.mean(iters)},
+                   "autotuned_kernels": tune},
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
         "e2e": {"value": 1e3 / e2e_ms, "unit": "units/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -365,8 +367,11 @@ def run_ensemble(args):
 
     torch.cuda.set_device(0)
     probs = synth.config5(count=args.ensemble_count)
+    # per-problem tuning is off by default here: choices timed one problem at a
+    # time do not maximise the throughput of concurrent problems (measured on
+    # config 5: 25.4 problems/s tuned against 27.1 with the built-in choices)
     ens = Ensemble(probs, precision=MIXED, workers=args.workers, refine_maxit=args.refine_maxit,
-                   refine_tol=args.refine_tol)
+                   refine_tol=args.refine_tol, autotune=args.autotune_ensemble)
     for _ in range(max(1, args.warmup)):
         ens.run(sens_mode=0)
     torch.cuda.synchronize()
@@ -404,6 +409,8 @@ def main():
     ap.add_argument("--config", type=int, default=2)
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--refine-maxit", type=int, default=8)
+    ap.add_argument("--no-autotune", action="store_true", help="keep the built-in kernel choices")
+    ap.add_argument("--autotune-ensemble", action="store_true", help="config 5: autotune every problem shape")
     ap.add_argument("--refine-tol", type=float, default=1e-2,
                     help="mixed refinement stop: max|dx| <= tol max|x| (1e-2 keeps volt within ~2e-8 of "
                          "complex128 on config 2; the error is measured and checked in every line)")

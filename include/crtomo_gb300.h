@@ -223,6 +223,22 @@ typedef struct {
 } crgpu_stats;
 int crgpu_get_stats(const crgpu_ctx *ctx, crgpu_stats *stats);
 
+/* Autotuner (mixed precision): times the band-factor kernels that can run
+ * this problem (tensor cores; SIMT register tiles at 1, 2 and 4 blocks per
+ * SM; SIMT shared-memory tiles) on its first batch of systems, and the two
+ * CRMod Jacobian kernels (tensor-core Gram form, SIMT direct form), for the
+ * conductivities sigma (elanz complex, host), and keeps the fastest for
+ * this context.  Choices are cached for the process by problem shape (n, mb,
+ * systems, electrodes, measurements, wavenumbers, SMs); flags & 1 re-times.
+ * Complex128 contexts return 0 without timing.  Leaves a forward done. */
+int crgpu_autotune(crgpu_ctx *ctx, const double *sigma, int32_t flags);
+
+/* The context's launch choices: out[0] factor kernel (0 default, 1 tensor
+ * cores, 2 SIMT register tiles, 3 SIMT shared-memory tiles), out[1] SIMT
+ * blocks per SM (0 default), out[2] CRMod Jacobian (0 default, 1 tensor
+ * cores, 2 SIMT). */
+int crgpu_get_tune(const crgpu_ctx *ctx, int32_t *out);
+
 #ifdef __cplusplus
 }
 #endif

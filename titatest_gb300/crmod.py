@@ -225,6 +225,21 @@ class CRMod:
             raise CRGPUError(code, "bkfak")
         return kf
 
+    def autotune(self, sigma, force: bool = False) -> dict:
+        """crgpu_autotune: the fastest factor and Jacobian kernels for this
+        problem (mixed precision), timed on its own systems; returns the
+        choices of tune()."""
+        sig = np.ascontiguousarray(sigma, np.complex128)
+        _check(self._h, lib().crgpu_autotune(self._h, sig.ctypes.data_as(f64p), int(bool(force))))
+        return self.tune()
+
+    def tune(self) -> dict:
+        out = np.zeros(3, np.int32)
+        _check(self._h, lib().crgpu_get_tune(self._h, out.ctypes.data_as(i32p)))
+        names = {0: "default", 1: "tensor cores", 2: "SIMT register tiles", 3: "SIMT shared-memory tiles"}
+        return {"factor": names[int(out[0])], "factor_blocks_per_sm": int(out[1]),
+                "jacobian": {0: "default", 1: "tensor cores", 2: "SIMT"}[int(out[2])]}
+
     def stats(self) -> dict:
         s = CStats()
         _check(self._h, lib().crgpu_get_stats(self._h, C.byref(s)))

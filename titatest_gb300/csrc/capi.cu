@@ -3,6 +3,10 @@
 // sensitivities (src/bsens.f90, src/bsensi.f90) and the model update
 // (src/update.f90).
 #include <algorithm>
+#include <array>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -470,6 +474,39 @@ int run_adjoint(crgpu_ctx *c, const double2 *d_g, double2 *d_grad) {
     return e;
 }
 
+}  // namespace
+
+// autotuner state (crgpu_autotune)
+namespace {
+struct TuneKey {
+    int n, mb, nsys, eanz, nanz, K, nsm;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(n, mb, nsys, eanz, nanz, K, nsm) < std::tie(o.n, o.mb, o.nsys, o.eanz, o.nanz, o.K, o.nsm);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, std::array<int, 3>> g_tune;
+
+// device time of fn() on the context's stream, best of two after a warm-up
+template <typename F>
+float time_on(crgpu_ctx *c, F &&fn) {
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float best = 1e30f;
+    for (int r = 0; r < 3; r++) {
+        cudaEventRecord(a, c->st);
+        fn();
+        cudaEventRecord(b, c->st);
+        cudaEventSynchronize(b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (r > 0) best = std::min(best, ms);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return best;
+}
 }  // namespace
 
 extern "C" {
@@ -940,6 +977,96 @@ int crgpu_bkfak(const crgpu_grid *grid, const crgpu_survey *sv, double *kfak) {
         if (std::fabs(dum) == 0.0) return 93;
         kfak[i] = 4.0 * pi / dum;
     }
+    return 0;
+}
+
+// ---- autotuner: the fastest mixed factor kernel (and its blocks per SM) and
+//      CRMod Jacobian kernel for this problem, timed on its own systems.
+//      Choices are cached for the process by problem shape.
+
+int crgpu_autotune(crgpu_ctx *c, const double *sigma, int32_t flags) {
+    if (!c || !sigma) return ERR_ARG;
+    if (c->precision != CRGPU_MIXED) return 0;  // complex128 has one kernel per step
+    const TuneKey key{(int)c->hg.n, c->hg.mb, (int)c->sys_k.size(), c->eanz, c->nanz, c->K, c->nsm};
+    if (!(flags & 1)) {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+            c->P.tune_factor = it->second[0];
+            c->P.tune_ctas = it->second[1];
+            c->P.tune_sens = it->second[2];
+            return 0;
+        }
+    }
+    // a forward with the current choices: sigma on the device, kpot for the Jacobian
+    int e = crgpu_forward(c, sigma, nullptr, nullptr, 0, nullptr, nullptr, nullptr);
+    if (e) return e;
+    DevProblem &P = c->P;
+    // ---- factor: the first batch of systems, assembled as the forward does
+    const int nsys_total = (int)c->sys_k.size(), ns = std::min(batch_size(c), nsys_total);
+    e = ensure_batch(c, ns);
+    if (!e) e = load_batch(c, 0, ns);
+    if (!e) e = assemble_batch(c, c->d_sigma, ns);
+    if (e) return e;
+    const int fuse = c->nrhs == 1 ? 1 : 0;
+    DevBatch B = batch_view(c, ns);
+    launch_rhs(P, B, c->nrhs, c->lsink, c->nsink, c->st);
+    std::vector<std::array<int, 2>> cand;
+    if (P.mb + 4 <= 128) cand.push_back({1, 0});
+    if (mixed_window_supported(P.mb + 1) <= 176 && mixed_window_supported(P.mb + 1) > 0)
+        for (int k : {1, 2, 4}) cand.push_back({2, k});
+    else if (mixed_window_supported(P.mb + 1) > 0)
+        for (int k : {1, 2}) cand.push_back({3, k});
+    float best = 1e30f;
+    std::array<int, 2> pick = {P.tune_factor, P.tune_ctas};
+    for (auto &cd : cand) {
+        P.tune_factor = cd[0];
+        P.tune_ctas = cd[1];
+        int fe = 0;
+        const float ms = time_on(c, [&] { fe = fe ? fe : run_factor(c, ns, fuse); });
+        if (fe) return fe;
+        int ce = check_device_errors(c, B.status, ns);
+        if (ce) return ce;
+        if (ms < best) {
+            best = ms;
+            pick = cd;
+        }
+    }
+    P.tune_factor = pick[0];
+    P.tune_ctas = pick[1];
+    c->factors_resident = false;
+    // ---- CRMod Jacobian: tensor cores or SIMT
+    if (sens_tc_supported(P, 0)) {
+        if (!c->d_sens) {
+            e = dalloc(c, &c->d_sens, (size_t)c->nanz * c->hg.elanz);
+            if (e) return e;
+        }
+        float bs = 1e30f;
+        int spick = 1;
+        for (int k : {1, 2}) {
+            P.tune_sens = k;
+            const float ms = time_on(c, [&] {
+                launch_bsens(P, c->d_kpot, c->d_kpot32, c->d_sigma, c->d_volt, 0, true, c->d_sens, c->st);
+            });
+            if (ms < bs) {
+                bs = ms;
+                spick = k;
+            }
+        }
+        P.tune_sens = spick;
+    }
+    e = check_device_errors(c, nullptr, 0);
+    if (e) return e;
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    g_tune[key] = {P.tune_factor, P.tune_ctas, P.tune_sens};
+    return 0;
+}
+
+int crgpu_get_tune(const crgpu_ctx *c, int32_t *out) {
+    if (!c || !out) return ERR_ARG;
+    out[0] = c->P.tune_factor;
+    out[1] = c->P.tune_ctas;
+    out[2] = c->P.tune_sens;
     return 0;
 }
 

@@ -12,6 +12,10 @@ struct DevProblem {
     int rw;               // padded row width of the lower pattern (row i at i*rw)
     int swrtr;
     int lsr;              // singularity removal
+    // launch choices of the autotuner (0: the built-in default)
+    int tune_factor;      // mixed factor: 1 tensor cores, 2 SIMT register tiles, 3 SIMT shared-memory tiles
+    int tune_ctas;        // SIMT factor: blocks per SM
+    int tune_sens;        // mixed CRMod Jacobian: 1 tensor cores (Gram form), 2 SIMT (direct form)
     double sytop;
     const double *earea;  // elanz: element areas of src/refsig.f90
     // grid (node order, 0-based)

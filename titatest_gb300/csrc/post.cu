@@ -185,7 +185,7 @@ void launch_bsens(const DevProblem &P, const double2 *kpot, const float2 *kpot32
                   int e_count) {
     if (e_count < 0) e_count = P.elanz - e_first;
     if (e_count <= 0) return;
-    if (single && sens_tc_supported(P, mode)) {
+    if (single && sens_tc_supported(P, mode) && P.tune_sens != 2) {
         launch_sens_tc(P, kpot32, sens, st, e_first, e_count);
         return;
     }

@@ -33,13 +33,15 @@ class Ensemble:
     .sigma, e.g. those of titatest_gb300.synth.config5()."""
 
     def __init__(self, problems: Sequence, precision: int = MIXED, workers: int = 8,
-                 refine_maxit: int = 8, refine_tol: float = 1e-6, budget_bytes: Optional[int] = None):
+                 refine_maxit: int = 8, refine_tol: float = 1e-6, budget_bytes: Optional[int] = None,
+                 autotune: bool = False):
         import torch
 
         self.problems = list(problems)
         self.precision = precision
         self.workers = max(1, int(workers))
         self.refine = (refine_maxit, refine_tol)
+        self.autotune = autotune  # per problem shape, cached by the library after the first run
         if budget_bytes is None:
             free, _ = torch.cuda.mem_get_info()
             budget_bytes = int(0.5 * free / self.workers)
@@ -65,6 +67,8 @@ class Ensemble:
                 m.set_stream(st.cuda_stream)
                 m.set_refinement(*self.refine)
                 m.set_memory_budget(self.budget)
+                if self.autotune:
+                    m.autotune(p.sigma)
                 m.forward_device(sig.data_ptr(), volt.data_ptr())
                 out = {"index": i, "nanz": p.survey.nanz, "elanz": p.grid.elanz}
                 if sens_mode is not None:
