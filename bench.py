@@ -230,8 +230,12 @@ def run_gpu(args):
         m.forward_device(sig_dev.data_ptr(), volt_dev.data_ptr())
         m.sens_device(0, sens_dev.data_ptr())
 
+    def unit_graph(m):  # the same unit replayed as one CUDA graph (recorded on the first call)
+        m.forward_sens_graph(sig_dev.data_ptr(), volt_dev.data_ptr(), 0, sens_dev.data_ptr())
+
+    timed_unit = unit if args.no_graph else unit_graph
     for _ in range(args.warmup):
-        unit(mixed)
+        timed_unit(mixed)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -241,10 +245,8 @@ def run_gpu(args):
         torch.cuda.synchronize()
         ev0.record(stream)
         for _ in range(args.steps):
-            unit(mixed)
+            timed_unit(mixed)
             st = mixed.stats()
-            fac_ms.append(st["ms_factor"])
-            sens_ms.append(st["ms_sens"])
             iters.append(st["refine_iterations"])
             launches += st["kernel_launches"]
         ev1.record(stream)
@@ -258,6 +260,12 @@ def run_gpu(args):
     value = world * 1e3 / ms_per_step
     volt_mixed = volt_dev.cpu().numpy().view(np.complex128).copy()
     sens_mixed = sens_dev.cpu().numpy().view(np.complex128).copy()
+    # per-phase figures (a replayed graph measures none): ordinary units
+    for _ in range(2):
+        unit(mixed)
+        st = mixed.stats()
+        fac_ms.append(st["ms_factor"])
+        sens_ms.append(st["ms_sens"])
 
     # ---- e2e through the host C ABI with pinned buffers
     L = _lib.lib()
@@ -323,6 +331,8 @@ def run_gpu(args):
         "data": "synthetic (seeded model and survey with the configuration's shapes)",
         "config": {"workload": workload_string(args.config, s, K),
                    "parallelism": "replicas" if world > 1 else "single GPU",
+                   "launch": "forward + Jacobian calls" if args.no_graph else
+                             "forward + Jacobian as one CUDA graph (crgpu_forward_sens_graph)",
                    "l2": "inputs larger than L2 (band factors of all systems, ~%d GB)" % int(
                        nsys * n * (mb + 1) * 8 / 1e9),
                    "refinement": {"maxit": args.refine_maxit, "tol": args.refine_tol,
@@ -410,6 +420,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--refine-maxit", type=int, default=8)
     ap.add_argument("--no-autotune", action="store_true", help="keep the built-in kernel choices")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="time the forward and Jacobian calls instead of their CUDA-graph replay")
     ap.add_argument("--autotune-ensemble", action="store_true", help="config 5: autotune every problem shape")
     ap.add_argument("--refine-tol", type=float, default=1e-2,
                     help="mixed refinement stop: max|dx| <= tol max|x| (1e-2 keeps volt within ~2e-8 of "

@@ -223,6 +223,15 @@ typedef struct {
 } crgpu_stats;
 int crgpu_get_stats(const crgpu_ctx *ctx, crgpu_stats *stats);
 
+/* Forward (crgpu_forward_device, volt_mode 0) and Jacobian
+ * (crgpu_sens_device) of device buffers as one CUDA graph: the first call,
+ * and any call after the buffers, the mode or the context's settings
+ * changed, runs them as usual and records the kernel sequence; later calls
+ * with the same buffers replay it (one launch) and check for errors.
+ * Problems whose systems need several batches run the ordinary path. */
+int crgpu_forward_sens_graph(crgpu_ctx *ctx, const void *sigma_device, void *volt_device, int32_t mode,
+                             void *sens_device);
+
 /* Autotuner (mixed precision): times the band-factor kernels that can run
  * this problem (tensor cores; SIMT register tiles at 1, 2 and 4 blocks per
  * SM; SIMT shared-memory tiles) on its first batch of systems, and the two

@@ -225,6 +225,12 @@ class CRMod:
             raise CRGPUError(code, "bkfak")
         return kf
 
+    def forward_sens_graph(self, sigma_ptr: int, volt_ptr: int, mode: int, sens_ptr: int):
+        """crgpu_forward_sens_graph: forward + Jacobian of device buffers,
+        replayed as one CUDA graph after the first call."""
+        _check(self._h, lib().crgpu_forward_sens_graph(self._h, C.c_void_p(sigma_ptr), C.c_void_p(volt_ptr),
+                                                        int(mode), C.c_void_p(sens_ptr)))
+
     def autotune(self, sigma, force: bool = False) -> dict:
         """crgpu_autotune: the fastest factor and Jacobian kernels for this
         problem (mixed precision), timed on its own systems; returns the

@@ -65,7 +65,16 @@ int upload(crgpu_ctx *c, const T **dst, const std::vector<T> &v) {
     return 0;
 }
 
+// the recorded forward + Jacobian graph refers to the batch buffers and the
+// launch choices: dropped when either changes
+void drop_graph(crgpu_ctx *c) {
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+    c->graph_mode = -1;
+}
+
 void free_batch(crgpu_ctx *c) {
+    drop_graph(c);
     void *ptrs[] = {c->Bmax.As, c->Bmax.fak, c->Bmax.b, c->Bmax.x, c->Bmax.r, c->Bmax.L, c->Bmax.y,
                     c->Bmax.status, c->Bmax.active, c->Bmax.pota, c->Bmax.potmax, c->d_ks, c->d_ls};
     for (void *p : ptrs)
@@ -303,11 +312,12 @@ int tail_systems(const crgpu_ctx *c, int ns) {
 int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const double *d_kfak, double2 *d_volt,
                 double2 *d_sigmaa) {
     DevProblem &P = c->P;
+    const bool cap = c->capturing;  // graph capture: no host copies, synchronisation or timing
     c->stats = crgpu_stats{};
     c->factors_resident = false;
     cudaEvent_t ev[4];
     for (auto &e : ev) cudaEventCreate(&e);
-    cudaEventRecord(ev[0], c->st);
+    if (!cap) cudaEventRecord(ev[0], c->st);
     CUCHECK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
     if (d_sigma != c->d_sigma)  // keep the model of this forward (adjoint, refactorisation)
         CUCHECK(c, cudaMemcpyAsync(c->d_sigma, d_sigma, sizeof(double2) * c->hg.elanz, cudaMemcpyDeviceToDevice, c->st));
@@ -319,7 +329,7 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
         c->stats.kernel_launches += 1;
     }
     const int nsys_total = (int)c->sys_k.size();
-    const int bs = batch_size(c);
+    const int bs = cap ? nsys_total : batch_size(c);  // recording: one batch, allocated by the ordinary run
     int e = ensure_batch(c, bs);
     if (e) return e;
     c->stats.nsystems = nsys_total;
@@ -334,7 +344,11 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
         const int nr = c->nrhs;
         const int fuse = nr == 1 ? 1 : 0;
         DevBatch B = batch_view(c, ns);
-        e = load_batch(c, s0, ns);
+        if (cap) {  // one batch: its systems' (k, l) are on the device already
+            CUCHECK(c, cudaMemsetAsync(c->Bmax.status, 0, sizeof(int) * ns, c->st));
+        } else {
+            e = load_batch(c, s0, ns);
+        }
         if (!e) e = assemble_batch(c, d_sigma, ns);
         if (e) return e;
         if (c->lsr) {
@@ -345,11 +359,11 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
             c->stats.kernel_launches += 1;
         }
         const int tail = tail_systems(c, ns);
-        cudaEventRecord(f0, c->st);
+        if (!cap) cudaEventRecord(f0, c->st);
         if (!tail) {
             e = run_factor(c, ns, fuse);
             if (e) return e;
-            cudaEventRecord(f1, c->st);
+            if (!cap) cudaEventRecord(f1, c->st);
             e = solve_view(c, B, fuse != 0, c->st, 0);
             if (e) return e;
         } else {
@@ -369,8 +383,9 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
         }
         launch_kpot(P, B, nr, c->d_kpot, c->d_kpot32, c->st);
         c->stats.kernel_launches += 1;
-        cudaEventRecord(f2, c->st);
         c->stats.nbatches++;
+        if (cap) continue;
+        cudaEventRecord(f2, c->st);
         int ce = check_device_errors(c, B.status, ns);
         if (ce) {
             worst = ce;
@@ -392,6 +407,12 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
     launch_rtrafo(P, c->d_kpot, c->d_hpot, c->st);
     launch_bvolt(P, c->d_hpot, volt_mode, d_kfak, d_volt, d_sigmaa, c->st);
     c->stats.kernel_launches += 2;
+    if (cap) {
+        for (auto &ev_ : ev) cudaEventDestroy(ev_);
+        c->have_forward = true;
+        c->factors_resident = true;
+        return 0;
+    }
     cudaEventRecord(ev[1], c->st);
     int ce = check_device_errors(c, nullptr, 0);
     if (!ce) ce = collect_refine_stats(c);
@@ -699,6 +720,7 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
 
 int crgpu_destroy(crgpu_ctx *c) {
     if (!c) return 0;
+    drop_graph(c);
     for (void *p : c->allocs) cudaFreeAsync(p, c->st);
     if (c->d_upd) cudaFreeAsync(c->d_upd, c->st);
     if (c->own_st) cudaStreamDestroy(c->own_st);
@@ -713,6 +735,7 @@ const char *crgpu_last_error(const crgpu_ctx *c) { return c ? c->last_error.c_st
 
 int crgpu_set_refinement(crgpu_ctx *c, int32_t maxit, double tol) {
     if (!c || maxit < 0 || maxit > kRefineCap || !(tol >= 0.0)) return ERR_ARG;
+    drop_graph(c);
     c->refine_maxit = maxit;
     c->refine_tol = tol;
     return 0;
@@ -760,6 +783,76 @@ int crgpu_forward(crgpu_ctx *c, const double *sigma, double *kpot, double *hpot,
     if (sigmaa)
         CUCHECK(c, cudaMemcpyAsync(sigmaa, c->d_sigmaa, (size_t)c->nanz * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
     CUCHECK(c, cudaStreamSynchronize(c->st));
+    return 0;
+}
+
+// Forward + Jacobian on device buffers as one CUDA graph.  The first call
+// (and any call after the buffers, the mode, the launch choices, the
+// refinement settings or the batching changed) runs the ordinary path, then
+// records the same kernel sequence, both streams included, without its host
+// copies, synchronisation and timing; later calls replay it and check for
+// errors once.  Problems that need several batches run the ordinary path.
+int crgpu_forward_sens_graph(crgpu_ctx *c, const void *sigma_device, void *volt_device, int32_t mode,
+                             void *sens_device) {
+    if (!c || !sigma_device || !volt_device || !sens_device || (mode != 0 && mode != 1)) return ERR_ARG;
+    const bool same = c->graph && c->graph_key[0] == sigma_device && c->graph_key[1] == volt_device &&
+                      c->graph_key[2] == sens_device && c->graph_mode == mode;
+    if (same) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, c->st);
+        CUCHECK(c, cudaGraphLaunch(c->graph, c->st));
+        cudaEventRecord(b, c->st);
+        int e = check_device_errors(c, c->Bmax.status, (int)c->sys_k.size());
+        c->stats.refine_iterations = 0;
+        c->stats.refine_last_correction = 0.0;
+        c->refine_used[0] = c->graph_refine_used[0];
+        c->refine_used[1] = c->graph_refine_used[1];
+        if (!e) e = collect_refine_stats(c);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        c->stats.ms_forward = ms;
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        c->last_sens = (const double2 *)sens_device;
+        return e;
+    }
+    drop_graph(c);
+    // the ordinary path: results of this call, buffers and uploads for the recording
+    int e = run_forward(c, (const double2 *)sigma_device, 0, nullptr, (double2 *)volt_device, nullptr);
+    if (!e) e = crgpu_sens_device(c, mode, sens_device);
+    if (e) return e;
+    if (c->stats.nbatches != 1) return 0;
+    const crgpu_stats keep = c->stats;  // this call's figures: the recording measures nothing
+    c->capturing = true;
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+        e = run_forward(c, (const double2 *)sigma_device, 0, nullptr, (double2 *)volt_device, nullptr);
+        if (!e) {
+            launch_bsens(c->P, c->d_kpot, c->d_kpot32, c->d_sigma, (const double2 *)volt_device, mode,
+                         c->precision == CRGPU_MIXED, (double2 *)sens_device, c->st);
+            c->stats.kernel_launches += 1;
+        }
+        ce = cudaStreamEndCapture(c->st, &graph);
+    }
+    c->capturing = false;
+    c->stats = keep;
+    c->graph_refine_used[0] = c->refine_used[0];
+    c->graph_refine_used[1] = c->refine_used[1];
+    c->refine_used[0] = c->refine_used[1] = 0;
+    if (!e && ce == cudaSuccess && graph) ce = cudaGraphInstantiate(&c->graph, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e || ce != cudaSuccess) {  // no graph: later calls record again; this call's results stand
+        c->graph = nullptr;
+        cudaGetLastError();
+        return e;
+    }
+    c->graph_key[0] = sigma_device;
+    c->graph_key[1] = volt_device;
+    c->graph_key[2] = sens_device;
+    c->graph_mode = mode;
     return 0;
 }
 
@@ -987,6 +1080,7 @@ int crgpu_bkfak(const crgpu_grid *grid, const crgpu_survey *sv, double *kfak) {
 int crgpu_autotune(crgpu_ctx *c, const double *sigma, int32_t flags) {
     if (!c || !sigma) return ERR_ARG;
     if (c->precision != CRGPU_MIXED) return 0;  // complex128 has one kernel per step
+    drop_graph(c);
     const TuneKey key{(int)c->hg.n, c->hg.mb, (int)c->sys_k.size(), c->eanz, c->nanz, c->K, c->nsm};
     if (!(flags & 1)) {
         std::lock_guard<std::mutex> g(g_tune_mu);

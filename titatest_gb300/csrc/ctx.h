@@ -41,6 +41,12 @@ struct crgpu_ctx {
     // current batch: {active count, pad, largest relative correction} per step
     void *d_refine = nullptr;
     int refine_used[2] = {0, 0};  // steps launched on each array since the last collection
+    // forward + Jacobian as one CUDA graph (crgpu_forward_sens_graph)
+    bool capturing = false;       // recording: no host copies, synchronisation or timing
+    cudaGraphExec_t graph = nullptr;
+    const void *graph_key[3] = {nullptr, nullptr, nullptr};  // sigma, volt, sens of the recorded graph
+    int graph_mode = -1;
+    int graph_refine_used[2] = {0, 0};  // refinement steps recorded in the graph per counter array
     int64_t mem_budget = 0;
     bool have_forward = false;
     bool factors_resident = false;  // band factors of every system still in Bmax (one batch)
