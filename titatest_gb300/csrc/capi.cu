@@ -65,6 +65,23 @@ int upload(crgpu_ctx *c, const T **dst, const std::vector<T> &v) {
     return 0;
 }
 
+// The contexts allocate from the device's default stream-ordered pool.  With
+// its default release threshold (0) every synchronisation hands freed memory
+// back to the driver, which made creating and destroying many contexts (an
+// ensemble of meshes) cost ~10 ms each; freed memory is kept for reuse
+// instead (it stays reserved by the process).
+void keep_pool_memory(int dev) {
+    static std::once_flag once;
+    std::call_once(once, [dev] {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        cudaGetLastError();
+    });
+}
+
 // the recorded forward + Jacobian graph refers to the batch buffers and the
 // launch choices: dropped when either changes
 void drop_graph(crgpu_ctx *c) {
@@ -577,6 +594,7 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
     cudaGetDevice(&dev);
     c->device = dev;
     cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev);
+    keep_pool_memory(dev);
     // device problem
     DevProblem &P = c->P;
     const HostGrid &hg = c->hg;
