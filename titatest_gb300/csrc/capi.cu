@@ -303,9 +303,9 @@ int assemble_batch(crgpu_ctx *c, const double2 *d_sigma, int ns) {
 
 // band factorisation of the current batch (src/chol.f90); with fuse the
 // forward sweep of the right-hand sides in B.b runs inside the factor
-int run_factor_view(crgpu_ctx *c, const DevBatch &B, int fuse, cudaStream_t st) {
+int run_factor_view(crgpu_ctx *c, const DevBatch &B, int fuse, cudaStream_t st, bool exclusive = false) {
     if (c->precision == CRGPU_MIXED) {
-        int e = launch_factor_mixed(c->P, B, fuse, c->nsm, st);
+        int e = launch_factor_mixed(c->P, B, fuse, c->nsm, exclusive, st);
         if (e) return fail(c, e, "mixed precision: band width beyond the supported window");
     } else {
         launch_factor_plain(c->P, B, fuse, c->nsm, st);
@@ -391,7 +391,7 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
             if (e) return e;
             cudaEventRecord(f1, c->st);
             CUCHECK(c, cudaStreamWaitEvent(c->st_hi, f1, 0));
-            e = run_factor_view(c, Bt, fuse, c->st_hi);
+            e = run_factor_view(c, Bt, fuse, c->st_hi, true);  // SMs of its own
             if (!e) e = solve_view(c, Bt, fuse != 0, c->st_hi, 1);
             if (!e) e = solve_view(c, Bf, fuse != 0, c->st, 0);
             if (e) return e;
@@ -1012,7 +1012,7 @@ int crgpu_factor_system(crgpu_ctx *c, const double *sigma, int32_t k, int32_t l,
     launch_assemble(c->P, B, c->d_sigma, c->d_adom, c->st);
     launch_rhs(c->P, B, 1, c->lsink, c->nsink, c->st);
     if (c->precision == CRGPU_MIXED) {
-        e = launch_factor_mixed(c->P, B, 1, c->nsm, c->st);
+        e = launch_factor_mixed(c->P, B, 1, c->nsm, false, c->st);
         if (e) return fail(c, e, "mixed window");
     } else {
         launch_factor_plain(c->P, B, 1, c->nsm, c->st);

@@ -416,13 +416,14 @@ int mixed_window_supported(int W) {
 // Kernel by P.tune_factor (0: tensor cores when the band fits their window,
 // else the smallest SIMT window), blocks per SM of the SIMT kernels by
 // P.tune_ctas (0: one).
-int launch_factor_mixed(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st) {
+int launch_factor_mixed(const DevProblem &P, const DevBatch &B, int fuse, int nsm, bool exclusive,
+                        cudaStream_t st) {
     const int W = P.mb + 1;
     int kind = P.tune_factor;
     if (kind == 1 && P.mb + 4 > 128) kind = 0;
     if (kind == 2 && mixed_window_supported(W) > 176) kind = 0;
     if (kind == 0) kind = P.mb + 4 <= 128 ? 1 : (mixed_window_supported(W) <= 176 ? 2 : 3);
-    if (kind == 1) return launch_factor_tc(P, B, fuse, nsm, st);
+    if (kind == 1) return launch_factor_tc(P, B, fuse, nsm, st, exclusive);
     const int per_sm = P.tune_ctas > 0 ? P.tune_ctas : 1;
     if (kind == 3) return launch_factor_mixed_smem(P, B, fuse, nsm * per_sm, st);
     int grid = B.nsys < nsm * per_sm ? B.nsys : nsm * per_sm;

@@ -24,14 +24,18 @@ void launch_pota_rhs(const DevProblem &P, const DevBatch &B, const double2 *sigm
 // factorisation (src/chol.f90) with fused forward substitution when fuse != 0
 void launch_factor_plain(const DevProblem &P, const DevBatch &B, int fuse, int nsm,
                          cudaStream_t st);
-int launch_factor_mixed(const DevProblem &P, const DevBatch &B, int fuse, int nsm,
+int launch_factor_mixed(const DevProblem &P, const DevBatch &B, int fuse, int nsm, bool exclusive,
                         cudaStream_t st);
 int mixed_window_supported(int W);
 // shared-memory window variant (factor_smem.cu) for 176 < mb + 1 <= 208
 int mixed_smem_window_supported(int W);
 int launch_factor_mixed_smem(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st);
 // tensor-core variant (tc_factor.cu) for band widths mb <= 124
-int launch_factor_tc(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st);
+// exclusive: each block asks for the whole shared memory of its SM, so that
+// no other kernel's blocks share the SM with it (the partial last round,
+// which runs beside the full rounds' solves)
+int launch_factor_tc(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st,
+                     bool exclusive = false);
 
 // triangular solves (src/vre.f90); item = system * nrhs + rhs
 void launch_forward_solve(const DevProblem &P, const DevBatch &B, int nrhs, bool mixed,

@@ -18,18 +18,19 @@
 //   B row 2b + 1 = [Im W(b, 0..3) |  Re W(b, 0..3)]   -> Im P[a][b]
 // Three products of the tf32 hi/lo splits (hi.hi + hi.lo + lo.hi) keep FP32
 // accuracy; an absent electrode (-1, zero potential) is one more row and
-// column of P, which stays zero.
+// column of P, which stays zero.  The accumulator stays in TMEM over the
+// wavenumbers; the epilogue copies P to shared memory and one thread per
+// measurement forms its four-term combination and the reference's scaling,
+// written coalesced into sens(e, :).
 //
 // Accuracy: P is rounded relative to its own size in the FP32 accumulator,
 // and the four-term combination cancels what the two potential (or current)
 // electrodes have in common at the element.  Relative to max|J| of
-// src/bsens.f90 that stays near 3e-7.  src/bsensi.f90 divides by V_i, which
-// amplifies the cancellation of long dipole-dipole measurements (1.3e-5 on a
-// 30-electrode survey); that mode keeps the SIMT contraction of post.cu,
-// which forms the dipole differences before the products.  The accumulator stays
-// in TMEM over the wavenumbers; the epilogue copies P to shared memory and
-// one thread per measurement forms its four-term combination and the
-// reference's scaling, written coalesced into sens(e, :).
+// src/bsens.f90 that stays below 1e-6 (8.7e-7 on a 96-electrode survey).
+// src/bsensi.f90 divides by V_i, which amplifies the cancellation of long
+// dipole-dipole measurements (1.3e-5 on a 30-electrode survey); that mode
+// keeps the SIMT contraction of post.cu, which forms the dipole differences
+// before the products.
 //
 // 256 threads per block, one element at a time (persistent over elements);
 // the element potentials of wavenumber k+1 are fetched by cp.async while the
@@ -73,7 +74,7 @@ __host__ __device__ inline StLayout st_layout(int E) {
     const int region = (2 * L.op_bytes > L.p_bytes ? 2 * L.op_bytes : L.p_bytes);
     L.u_off = (region + 127) / 128 * 128;
     L.u_bytes = 2 * 4 * E * 8;
-    L.total = L.u_off + L.u_bytes + 192;  // + barriers, means and flags
+    L.total = L.u_off + L.u_bytes + 192;  // + barriers and flags
     return L;
 }
 

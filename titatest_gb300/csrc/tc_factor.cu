@@ -578,15 +578,21 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tbase), "r"(kTcCols) : "memory");
 }
 
-int launch_factor_tc(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st) {
+int launch_factor_tc(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st, bool exclusive) {
     if (P.mb + 4 > kTcWP) return ERR_UNSUPPORTED;
     static std::once_flag once;
+    static int optin = kTcSmemRequest;
     std::call_once(once, [] {
-        cudaFuncSetAttribute(k_factor_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemRequest);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (optin < kTcSmemRequest) optin = kTcSmemRequest;
+        cudaFuncSetAttribute(k_factor_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     });
     static_assert(sizeof(TcSmem) <= kTcSmemRequest, "shared memory layout exceeds the request");
-    const int grid = B.nsys < 2 * nsm ? B.nsys : 2 * nsm;
-    k_factor_tc<<<grid, kTcThreads, kTcSmemRequest, st>>>(P, B, fuse);
+    const int per_sm = exclusive ? 1 : 2;
+    const int grid = B.nsys < per_sm * nsm ? B.nsys : per_sm * nsm;
+    k_factor_tc<<<grid, kTcThreads, exclusive ? optin : kTcSmemRequest, st>>>(P, B, fuse);
     return 0;
 }
 
