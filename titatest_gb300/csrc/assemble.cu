@@ -29,12 +29,6 @@ __global__ void k_adom(DevProblem P, const double2 *__restrict__ sigma, double2 
     adom[gid] = v;
 }
 
-void launch_adom(const DevProblem &P, const double2 *sigma, double2 *adom, cudaStream_t st) {
-    size_t tot = (size_t)P.K * P.nnz;
-    int nt = 256;
-    k_adom<<<(unsigned)((tot + nt - 1) / nt), nt, 0, st>>>(P, sigma, adom);
-}
-
 // Value of lower-pattern entry p of system (k, l) before scaling: area part
 // plus the mixed-boundary terms, with Dirichlet rows and columns replaced.
 __device__ __forceinline__ double2 entry_value(const DevProblem &P, const double2 *__restrict__ ad,
@@ -70,9 +64,44 @@ __device__ __forceinline__ double inv_sqrt_abs(double2 v) {
     return y;
 }
 
+// lower-pattern entry of the diagonal of row i (-1: none)
+__device__ __forceinline__ int diag_entry(const DevProblem &P, int i) {
+    int pd = -1;
+    for (int p = P.rowptr[i]; p < P.rowptr[i + 1]; p++)
+        if (P.col[p] == i) pd = p;
+    return pd;
+}
+
+// fak of the area part alone, per wavenumber and row (0: zero diagonal).  A
+// row whose diagonal has no mixed-boundary term and which is not a
+// Dirichlet row has this fak in every system of the wavenumber, whatever the
+// current electrode.
+__global__ void k_fak_area(DevProblem P, const double2 *__restrict__ adom, double *__restrict__ fak_area) {
+    const size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (size_t)P.K * P.n) return;
+    const int k = (int)(gid / P.n), i = (int)(gid % P.n);
+    const int pd = diag_entry(P, i);
+    double f = 0.0;
+    if (pd >= 0) {
+        const double2 d = adom[(size_t)k * P.nnz + pd];
+        if (d.x * d.x + d.y * d.y > 0.0) f = inv_sqrt_abs(d);
+    }
+    fak_area[gid] = f;
+}
+
+// the area parts of every wavenumber (adom[k][p]), followed in the same
+// allocation by fak_area[k][i]
+void launch_adom(const DevProblem &P, const double2 *sigma, double2 *adom, cudaStream_t st) {
+    const size_t tot = (size_t)P.K * P.nnz, totn = (size_t)P.K * P.n;
+    const int nt = 256;
+    k_adom<<<(unsigned)((tot + nt - 1) / nt), nt, 0, st>>>(P, sigma, adom);
+    k_fak_area<<<(unsigned)((totn + nt - 1) / nt), nt, 0, st>>>(P, adom, (double *)(adom + tot));
+}
+
 // fak of every row (src/scalab.f90:50-64): grid (row blocks, systems).  The
 // rows of the lower pattern are sorted by column, so the diagonal is the
-// last entry that is not padding.
+// last entry that is not padding.  Rows without a mixed-boundary term in the
+// diagonal (and not Dirichlet rows) take the wavenumber's fak_area.
 __global__ void k_fak(DevProblem P, DevBatch B, const double2 *__restrict__ sigma,
                       const double2 *__restrict__ adom) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
@@ -80,16 +109,20 @@ __global__ void k_fak(DevProblem P, DevBatch B, const double2 *__restrict__ sigm
     const int k = B.ks[s], l = B.ls[s];
     const double2 *ad = adom + (size_t)k * P.nnz;
     const double *kgl = P.kg + ((size_t)k * P.eanz + l) * P.relanz;
-    int pd = -1;
-    for (int p = P.rowptr[i]; p < P.rowptr[i + 1]; p++)
-        if (P.col[p] == i) pd = p;
-    double2 d = cz(0.0, 0.0);
-    if (pd >= 0) d = entry_value(P, ad, kgl, sigma, pd, i, i, P.dirichlet[i] != 0);
+    const int pd = diag_entry(P, i);
     double f = 1.0;
-    if (!(d.x * d.x + d.y * d.y > 0.0)) {  // src/scalab.f90:57-61
-        atomicCAS(&B.status[s], 0, 27);
+    if (pd >= 0 && !P.dirichlet[i] && P.bnd_ptr[pd] == P.bnd_ptr[pd + 1]) {
+        const double fa = ((const double *)(adom + (size_t)P.K * P.nnz))[(size_t)k * P.n + i];
+        if (fa > 0.0) f = fa;
+        else atomicCAS(&B.status[s], 0, 27);  // src/scalab.f90:57-61
     } else {
-        f = inv_sqrt_abs(d);
+        double2 d = cz(0.0, 0.0);
+        if (pd >= 0) d = entry_value(P, ad, kgl, sigma, pd, i, i, P.dirichlet[i] != 0);
+        if (!(d.x * d.x + d.y * d.y > 0.0)) {  // src/scalab.f90:57-61
+            atomicCAS(&B.status[s], 0, 27);
+        } else {
+            f = inv_sqrt_abs(d);
+        }
     }
     B.fak[(size_t)s * P.n + i] = f;
 }

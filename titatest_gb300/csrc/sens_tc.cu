@@ -62,10 +62,12 @@ struct StLayout {
     int op_bytes;            // one operand buffer: A hi, A lo (128 x 8), B hi, B lo (N x 8) floats
     int p_bytes;             // P: E x E float2
     int u_off, u_bytes;      // element potentials, two wavenumbers: [2][4][eanz] float2 (sized for E)
+    int ctl_off;             // StCtl
+    int scale_off;           // -strom_i / pi per measurement (FP32), or 0: read in FP64
     int total;
 };
 
-__host__ __device__ inline StLayout st_layout(int E) {
+__host__ __device__ inline StLayout st_layout(int E, int nanz) {
     StLayout L;
     L.N = ((2 * E + 15) / 16) * 16;
     L.off_b = 2 * kStM * 8 * 4;
@@ -74,8 +76,25 @@ __host__ __device__ inline StLayout st_layout(int E) {
     const int region = (2 * L.op_bytes > L.p_bytes ? 2 * L.op_bytes : L.p_bytes);
     L.u_off = (region + 127) / 128 * 128;
     L.u_bytes = 2 * 4 * E * 8;
-    L.total = L.u_off + L.u_bytes + 192;  // + barriers and flags
+    L.ctl_off = L.u_off + L.u_bytes;
+    L.total = L.ctl_off + 128;  // barriers and flags
+    L.scale_off = 0;
+    if (L.total + nanz * 4 <= 200 * 1024) {
+        L.scale_off = L.total;
+        L.total += (nanz * 4 + 15) / 16 * 16;
+    }
     return L;
+}
+
+// FP32 -> FP64 from the bit fields (exact for normal numbers; zero and
+// subnormals give a signed zero, inf / nan stay inf / nan) without the FP64
+// pipe, which runs at a small fraction of the FP32 rate here
+__device__ __forceinline__ double widen(float x) {
+    const uint32_t u = __float_as_uint(x), e8 = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+    const uint32_t e11 = e8 == 0u ? 0u : (e8 == 0xFFu ? 0x7FFu : e8 + 896u);
+    const uint32_t hi = (u & 0x80000000u) | (e11 << 20) | (e8 == 0u ? 0u : (m >> 3));
+    const uint32_t lo = e8 == 0u ? 0u : (m << 29);
+    return __hiloint2double((int)hi, (int)lo);
 }
 
 struct StCtl {
@@ -92,12 +111,13 @@ __global__ __launch_bounds__(kStThreads) void k_sens_tc(DevProblem P, const floa
     extern __shared__ __align__(1024) unsigned char st_raw[];
     const int eanz = P.eanz, nanz = P.nanz, n = P.n, K = P.K;
     const int E = eanz + 1;  // electrodes and the zero-potential one (index eanz)
-    const StLayout Ly = st_layout(E);
+    const StLayout Ly = st_layout(E, nanz);
     const int N = Ly.N;
     auto opb = [&](int b) { return (float *)(st_raw + (size_t)b * Ly.op_bytes); };  // operand buffer b
     float2 *Psh = (float2 *)st_raw;
     float2 *ush = (float2 *)(st_raw + Ly.u_off);  // [2][4][eanz]
-    StCtl &C = *(StCtl *)(st_raw + Ly.u_off + Ly.u_bytes);
+    StCtl &C = *(StCtl *)(st_raw + Ly.ctl_off);
+    float *scale = Ly.scale_off ? (float *)(st_raw + Ly.scale_off) : nullptr;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     if (warp == 0) {
@@ -113,6 +133,9 @@ __global__ __launch_bounds__(kStThreads) void k_sens_tc(DevProblem P, const floa
         C.fail = 0;
         C.uses[0] = C.uses[1] = 0u;
     }
+    if (scale)  // the measurements' scaling of src/bsens.f90, once per block
+        for (int i = tid; i < nanz; i += kStThreads)
+            scale[i] = (float)(-(P.swrtr ? P.strom[i] * (1.0 / kStPi) : P.strom[i]));
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -273,8 +296,13 @@ __global__ __launch_bounds__(kStThreads) void k_sens_tc(DevProblem P, const floa
                 const float2 p42 = Psh[x4 * E + x2], p41 = Psh[x4 * E + x1];
                 const float2 p32 = Psh[x3 * E + x2], p31 = Psh[x3 * E + x1];
                 const float dx = (p42.x - p41.x) - (p32.x - p31.x), dy = (p42.y - p41.y) - (p32.y - p31.y);
-                const double f = P.swrtr ? P.strom[i] * (1.0 / kStPi) : P.strom[i];
-                sens[(size_t)e * nanz + i] = cz(-(double)dx * f, -(double)dy * f);
+                if (scale) {
+                    const float f = scale[i];
+                    sens[(size_t)e * nanz + i] = cz(widen(dx * f), widen(dy * f));
+                } else {
+                    const double f = P.swrtr ? P.strom[i] * (1.0 / kStPi) : P.strom[i];
+                    sens[(size_t)e * nanz + i] = cz(-(double)dx * f, -(double)dy * f);
+                }
             }
         }
         __syncthreads();  // P is overwritten by the next element's operands
@@ -300,7 +328,7 @@ bool sens_tc_supported(const DevProblem &P, int mode) { return mode == 0 && P.ea
 
 void launch_sens_tc(const DevProblem &P, const float2 *kpot, double2 *sens, cudaStream_t st, int e_first,
                     int e_count) {
-    const StLayout Ly = st_layout(P.eanz + 1);
+    const StLayout Ly = st_layout(P.eanz + 1, P.nanz);
     static std::once_flag once;
     static int nsm = 0;
     std::call_once(once, [] {
