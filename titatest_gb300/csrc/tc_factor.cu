@@ -431,18 +431,9 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
                 //      l sqrt(d) = m / sqrt(d), and the last step's update of the fused
                 //      forward substitution, b -= l (Lu^{-1} b_p) = m u, from 1/sqrt(d)
                 //      and u of the pivot block that the MMA warp left in shared memory
-                if (J >= 1 && blk != Bp) {
-                    const int r_l = j + dist, band0 = dist + 4 - mb;
-                    if (r_l < n && band0 < 4) {
-                        float2 *row = L + (size_t)r_l * Wb + (j - 4 - r_l + mb);  // column j-4
+                if (J >= 1 && blk != Bp && fuse) {
 #pragma unroll
-                        for (int q = 0; q < 4; q++)
-                            if (q >= band0) row[q] = cmulf(mold[q], S.isq_s[ob ^ 1][q]);
-                    }
-                    if (fuse) {
-#pragma unroll
-                        for (int q = 0; q < 4; q++) bsh = cfmsf(bsh, mold[q], S.u_s[ob ^ 1][q]);
-                    }
+                    for (int q = 0; q < 4; q++) bsh = cfmsf(bsh, mold[q], S.u_s[ob ^ 1][q]);
                 }
                 if (blk == Bk) bsh = fuse ? S.bnew[cn][b4] : cf(0.f, 0.f);  // the entering row's right-hand side
                 Bp = Bk;
@@ -557,6 +548,33 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
                     }
                     S.isq_s[ob][q] = isqq;
                     S.u_s[ob][q] = uq;
+                }
+                __syncwarp();
+                // the step's entries of Lc = m / sqrt(d) for the other rows of the window:
+                // m rebuilt exactly from its tf32 hi + lo operand rows, which stay in this
+                // buffer until step J+2 writes it (after the next handoff)
+                {
+                    const int j = 4 * J, Bk = J % kTcNB;
+                    float2 isq[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) isq[q] = S.isq_s[ob][q];
+                    const TcOperands &o = S.op[ob];
+#pragma unroll
+                    for (int w = 0; w < 4; w++) {
+                        const int t = lane + 32 * w;
+                        int dist = t - 4 * Bk;
+                        if (dist < 0) dist += kTcWP;
+                        const int r_l = j + dist, band0 = dist - mb;
+                        if ((t >> 2) == Bk || r_l >= n || band0 >= 4) continue;  // pivot rows: stored above
+                        const float4 h0 = *(const float4 *)&o.a_hi[kmaj(t, 0)], h1 = *(const float4 *)&o.a_hi[kmaj(t, 4)];
+                        const float4 l0 = *(const float4 *)&o.a_lo[kmaj(t, 0)], l1 = *(const float4 *)&o.a_lo[kmaj(t, 4)];
+                        const float2 mq[4] = {cf(h0.x + l0.x, h1.x + l1.x), cf(h0.y + l0.y, h1.y + l1.y),
+                                              cf(h0.z + l0.z, h1.z + l1.z), cf(h0.w + l0.w, h1.w + l1.w)};
+                        float2 *row = L + (size_t)r_l * Wb + (j - r_l + mb);  // column j
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            if (q >= band0) row[q] = cmulf(mq[q], isq[q]);
+                    }
                 }
                 __syncwarp();
             }
