@@ -192,6 +192,25 @@ def _wide_band_case(nx=190, nz=6, ne=16, seed=17):
     return grid, survey, synth._sigma_from(mag, pha)
 
 
+def test_tensor_core_factor_matches_oracle_chol(gpu_lib):
+    """The complex64 tensor-core factor read back through crgpu_factor_system
+    (its band rows copied out of the batch buffer), against the oracle's chol
+    rows."""
+    from titatest_gb300 import MIXED, CRMod
+    g, sv, sig, cfg, _ = load_case("testmodinv")
+    assert g.mb + 4 <= 128
+    P = O.Problem(g, sv)
+    kwn, kwnwi = P.rwaven()
+    with CRMod(g, sv, kwn, kwnwi, precision=MIXED) as m:
+        for k, l in [(1, 1), (len(kwn), sv.eanz)]:
+            a_ref, fak_ref = P.factor(sig, kwn, k, l)
+            a, fak = m.factor_system(sig, k, l)
+            np.testing.assert_allclose(fak, fak_ref, rtol=1e-14)
+            for i in range(g.sanz):
+                lo = max(0, g.mb - i)
+                assert relerr(a[i, lo:], a_ref[i, lo:]) < 1e-3, (k, l, i)
+
+
 def test_wide_band_mixed_factor_shared_memory_window(gpu_lib):
     """mb = 192: the complex64 factor with its window in shared memory, against
     the oracle's factor and, through refinement, the complex128 forward."""

@@ -68,6 +68,9 @@ extern "C" int crgpu_factor_system_noalloc(crgpu_ctx *c, const void *sigma_devic
     }
     cudaStream_t st = stream ? (cudaStream_t)stream : c->st;
     int *ints = (int *)base;
+    // launch_adom writes the area parts (nnz) and then fak_area (n doubles) into
+    // the start of `as`; k_fak reads fak_area there before k_assemble_entries
+    // overwrites the region with the scaled entries (same stream)
     double2 *adom = (double2 *)(base + 16);
     double2 *as = adom + nnz;
     double2 *b = as + nnz;
