@@ -99,6 +99,16 @@ int crgpu_set_refinement(crgpu_ctx *ctx, int32_t maxit, double tol);
  * context's own stream).  The caller keeps the stream alive. */
 int crgpu_set_stream(crgpu_ctx *ctx, void *stream);
 
+/* Dirichlet boundary values (lrandb2 with the file read by src/rrandb.f90,
+ * src/fem.f90:296-299): node rwdnr[i] (1-based, band numbering) is held at
+ * the complex value (rwd[2i], rwd[2i+1]) by src/randb2.f90:1-82, applied
+ * after src/randb.f90 in every system assembled by src/kompab.f90
+ * (src/fem.f90:363).  Systems whose right-hand side src/kompb.f90 builds
+ * (no mixed boundary, electrodes after the first) keep the rows and columns
+ * eliminated with zero values, as the reference does.  rwdanz = 0 removes
+ * the values.  A node outside 1..sanz returns 30. */
+int crgpu_set_boundary_values(crgpu_ctx *ctx, int32_t rwdanz, const int32_t *rwdnr, const double *rwd);
+
 /* Upper bound of device memory for the per-system band factors; systems are
  * processed in batches that fit.  Default: 60% of free device memory. */
 int crgpu_set_memory_budget(crgpu_ctx *ctx, int64_t bytes);
@@ -109,7 +119,7 @@ int crgpu_set_memory_budget(crgpu_ctx *ctx, int64_t bytes);
 
 /* Forward block of src/fem.f90:327-400 (== src/inv.f90:426-491): for every
  * wavenumber k and current electrode l: src/potana.f90 (if lsr),
- * src/kompab.f90 / src/kompb.f90, src/randb.f90, src/scalab.f90,
+ * src/kompab.f90 / src/kompb.f90, src/randb.f90, src/randb2.f90, src/scalab.f90,
  * src/chol.f90, src/vre.f90 and the unscaling into kpot; then
  * src/rtrafo.f90, then src/bvolt.f90 (volt_mode 0: sigmaa = kfak*V, kfak
  * may be NULL) or src/bvolti.f90 (volt_mode 1: sigmaa = -log V).

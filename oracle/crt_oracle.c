@@ -551,6 +551,9 @@ typedef struct {
     const cx *sigma;
     cx sigma0;
     int lsr, lsink, nsink, lrandb;
+    int rwdanz;
+    const int *rwdnr;
+    const cx *rwd;
 } fe_ctx;
 
 /* src/kompab.f90:11-194 */
@@ -635,6 +638,39 @@ static void randb(const or_mesh *m, cx *a, cx *b) {
                     a[ji - 1] = cmk(0, 0);
                 }
             }
+        }
+    }
+}
+
+/* src/randb2.f90:1-82: node rwdnr(ir) held at the value rwd(ir).  Its row
+ * and column are eliminated (diagonal 1, b(k) = -rwd), the eliminated column
+ * moved to the right-hand side of the other rows, node by node in file order
+ * (a column already eliminated contributes nothing). */
+static void randb2(const fe_ctx *c, cx *a, cx *b) {
+    const or_mesh *m = c->m;
+    int mb = m->mb, sanz = m->sanz, m1 = mb + 1;
+    for (int ir = 0; ir < c->rwdanz; ir++) {
+        int k = c->rwdnr[ir];
+        cx rwert = c->rwd[ir];
+        b[k - 1] = cmk(-rwert.re, -rwert.im);
+        long idk = (long)k * m1;
+        a[idk - 1] = cmk(1, 0);
+        if (k != 1) {
+            int ia = 1 > mb + 2 - k ? 1 : mb + 2 - k;
+            for (int i = ia; i <= mb; i++) {
+                int j = k + i - m1;
+                long ki = idk + i - m1;
+                b[j - 1] = cadd(b[j - 1], cmul(rwert, a[ki - 1]));
+                a[ki - 1] = cmk(0, 0);
+            }
+        }
+        if (k == sanz) continue;
+        int ia = 1 > k - sanz + m1 ? 1 : k - sanz + m1;
+        for (int i = ia; i <= mb; i++) {
+            int j = k - i + m1;
+            long ji = (long)(j - 1) * m1 + i;
+            b[j - 1] = cadd(b[j - 1], cmul(rwert, a[ji - 1]));
+            a[ji - 1] = cmk(0, 0);
         }
     }
 }
@@ -726,6 +762,11 @@ static int setup_ctx(const or_mesh *m, const or_opts *o, int kwnanz, const doubl
     c->lsink = o->lsink;
     c->nsink = o->nsink;
     c->lrandb = lrandb;
+    c->rwdanz = o->rwdanz;
+    c->rwdnr = o->rwdnr;
+    c->rwd = (const cx *)o->rwd;
+    for (int ir = 0; ir < c->rwdanz; ir++)  /* src/rrandb.f90 (error 30) */
+        if (c->rwdnr[ir] < 1 || c->rwdnr[ir] > m->sanz) return 30;
     *lsr_eff = lsr;
     return 0;
 }
@@ -753,6 +794,7 @@ static int forward_k(const fe_ctx *c, int lbeta, int lana, int k, const double *
         if (refactor) {
             int e = kompab(c, l, k, a, b, pota);
             if (!e && c->lrandb) randb(m, a, b);
+            if (!e && c->rwdanz) randb2(c, a, b);
             if (!e) e = scalab(sanz, mb, a, b, fak);
             if (!e) e = chol(sanz, mb, a);
             if (e) { err = e; break; }
@@ -1398,7 +1440,7 @@ int or_update(int nanz, int manz, const double *sens_, const double *wmatd, cons
 }
 
 /* One system (k, l) (1-based): src/kompab.f90 + src/randb.f90 +
- * src/scalab.f90 + src/chol.f90, leaving the band factor a((mb+1)*sanz) and
+ * src/randb2.f90 + src/scalab.f90 + src/chol.f90, leaving the band factor a((mb+1)*sanz) and
  * fak(sanz).  Returns errnr. */
 int or_factor(const or_mesh *m, const or_opts *o, int kwnanz, const double *kwn, const double *sigma,
               int k, int l, double *a_out, double *fak_out) {
@@ -1412,6 +1454,7 @@ int or_factor(const or_mesh *m, const or_opts *o, int kwnanz, const double *kwn,
         cx *pota = (cx *)calloc((size_t)sanz, sizeof(cx));
         e = kompab(&c, l, k, (cx *)a_out, b, pota);
         if (!e && c.lrandb) randb(m, (cx *)a_out, b);
+        if (!e && c.rwdanz) randb2(&c, (cx *)a_out, b);
         if (!e) e = scalab(sanz, mb, (cx *)a_out, b, fak_out);
         if (!e) e = chol(sanz, mb, (cx *)a_out);
         free(b);

@@ -51,6 +51,9 @@ typedef struct {
     int nsink;      /* sink node */
     int lsytop;     /* use mean y of Neumann boundary as the image plane */
     int nthreads;   /* OpenMP threads (<=0: leave default) */
+    int rwdanz;     /* Dirichlet boundary values of src/randb2.f90 (lrandb2); 0: none */
+    const int *rwdnr;   /* rwdanz node numbers, 1-based */
+    const double *rwd;  /* rwdanz complex values (re, im pairs) */
 } or_opts;
 
 /* derived mesh counts */
@@ -85,7 +88,7 @@ int or_forward_pairs(const or_mesh *m, const or_opts *o, int kwnanz,
                      const double *sigma, int npairs, const int *pairs,
                      double *kpot);
 
-/* one system (k, l), 1-based: kompab + randb + scalab + chol; a_out has
+/* one system (k, l), 1-based: kompab + randb + randb2 + scalab + chol; a_out has
  * (mb+1)*sanz complex entries, fak_out sanz.  Returns errnr. */
 int or_factor(const or_mesh *m, const or_opts *o, int kwnanz, const double *kwn,
               const double *sigma, int k, int l, double *a_out, double *fak_out);

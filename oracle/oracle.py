@@ -42,7 +42,8 @@ class OrMesh(C.Structure):
 
 class OrOpts(C.Structure):
     _fields_ = [("swrtr", C.c_int), ("lsr", C.c_int), ("lana", C.c_int), ("lsink", C.c_int),
-                ("nsink", C.c_int), ("lsytop", C.c_int), ("nthreads", C.c_int)]
+                ("nsink", C.c_int), ("lsytop", C.c_int), ("nthreads", C.c_int),
+                ("rwdanz", C.c_int), ("rwdnr", i32p), ("rwd", f64p)]
 
 
 def lib():
@@ -94,6 +95,7 @@ class Problem:
             vnr=np.ascontiguousarray(survey.vnr, np.int32),
             strom=np.ascontiguousarray(survey.strom, np.float64),
         )
+        self._rwd = None
         k = self._keep
         self.m = OrMesh(
             grid.sanz, grid.typanz, grid.mb, _p(k["typ"], i32p), _p(k["nelanz"], i32p),
@@ -133,6 +135,27 @@ class Problem:
         return (elbg.reshape(K, 10, g.elanz), relbg.reshape(10, max(g.relanz, 1)),
                 kg.reshape(K, self.survey.eanz, max(g.relanz, 1)), bool(flags[0]), bool(flags[1]))
 
+    def set_boundary_values(self, nodes, values):
+        """Dirichlet boundary values of src/randb2.f90 (lrandb2): node numbers
+        (1-based, band numbering) and complex values, in file order; None or an
+        empty list switches them off."""
+        if nodes is None or len(nodes) == 0:
+            self._rwd = None
+            return
+        nr = np.ascontiguousarray(nodes, np.int32)
+        vv = np.ascontiguousarray(values, np.complex128)
+        assert nr.shape == vv.shape
+        self._rwd = (nr, vv)
+
+    def _opts(self, *args):
+        o = OrOpts(*args)
+        if self._rwd is not None:
+            nr, vv = self._rwd
+            o.rwdanz = len(nr)
+            o.rwdnr = _p(nr, i32p)
+            o.rwd = _p(vv, f64p)
+        return o
+
     # --- forward -----------------------------------------------------------
     def forward(self, sigma, kwn, kwnwi, swrtr=1, lsr=False, lana=False, lsink=False, nsink=0,
                 lsytop=False, nthreads=0):
@@ -143,7 +166,7 @@ class Problem:
         kwnwi = np.ascontiguousarray(kwnwi, np.float64)
         K = len(kwn)
         kpot = np.zeros((K, self.survey.eanz, g.sanz), np.complex128)
-        o = OrOpts(swrtr, int(lsr), int(lana), int(lsink), int(nsink), int(lsytop), int(nthreads))
+        o = self._opts(swrtr, int(lsr), int(lana), int(lsink), int(nsink), int(lsytop), int(nthreads))
         e = lib().or_forward(C.byref(self.m), C.byref(o), K, _p(kwn, f64p), _p(kwnwi, f64p),
                              _p(sigma, f64p), _p(kpot, f64p))
         if e:
@@ -159,7 +182,7 @@ class Problem:
         K = len(kwn)
         kpot = np.zeros((K, self.survey.eanz, g.sanz), np.complex128)
         pr = np.ascontiguousarray(np.asarray(pairs, np.int32) + 1)
-        o = OrOpts(kw.get("swrtr", 1), int(kw.get("lsr", 0)), int(kw.get("lana", 0)),
+        o = self._opts(kw.get("swrtr", 1), int(kw.get("lsr", 0)), int(kw.get("lana", 0)),
                    int(kw.get("lsink", 0)), int(kw.get("nsink", 0)), int(kw.get("lsytop", 0)),
                    int(nthreads))
         e = lib().or_forward_pairs(C.byref(self.m), C.byref(o), K, _p(kwn, f64p), _p(kwnwi, f64p),
@@ -175,7 +198,7 @@ class Problem:
         kwn = np.ascontiguousarray(kwn, np.float64)
         a = np.zeros((g.sanz, g.mb + 1), np.complex128)
         fak = np.zeros(g.sanz)
-        o = OrOpts(kw.get("swrtr", 1), 0, 0, int(kw.get("lsink", 0)), int(kw.get("nsink", 0)),
+        o = self._opts(kw.get("swrtr", 1), 0, 0, int(kw.get("lsink", 0)), int(kw.get("nsink", 0)),
                    int(kw.get("lsytop", 0)), 0)
         e = lib().or_factor(C.byref(self.m), C.byref(o), len(kwn), _p(kwn, f64p), _p(sigma, f64p),
                             int(k), int(l), _p(a, f64p), _p(fak, f64p))
@@ -225,7 +248,7 @@ class Problem:
         volt = np.ascontiguousarray(volt if volt is not None else np.ones(self.survey.nanz),
                                     np.complex128)
         sens = np.zeros((g.elanz, self.survey.nanz), np.complex128)  # column-major (nanz, manz)
-        o = OrOpts(swrtr, 0, 0, 0, 0, 0, int(nthreads))
+        o = self._opts(swrtr, 0, 0, 0, 0, 0, int(nthreads))
         lib().or_bsens_elbg(C.byref(self.m), C.byref(o), mode, swrtr, K, _p(kwnwi, f64p),
                             _p(elbg, f64p), _p(kpot, f64p), _p(sigma, f64p), _p(volt, f64p),
                             _p(sens, f64p))

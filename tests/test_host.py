@@ -112,3 +112,20 @@ def test_border_fix_takes_last_matching_element():
     g2.rnr[:] = 1  # corrupt every pointer
     n = F.fix_border_elements(g2)
     assert n > 0 and np.array_equal(g2.rnr, g.rnr)
+
+
+def test_boundary_values_file(tmp_path):
+    """src/rrandb.f90 (complex case): list-directed complex values, a value
+    split over two records, a bare real, the Neumann block read and dropped;
+    a node above sanz is errnr 30."""
+    p = tmp_path / "boundary.dat"
+    p.write_text("3\n5 (1.5, -2.0)\n7 ( 0.25 ,\n 1d-3 )\n9 2.0\n2\n(1,2) (3,4)\n")
+    nodes, vals = F.read_boundary_values(str(p), 20)
+    assert nodes.tolist() == [5, 7, 9]
+    assert np.array_equal(vals, [1.5 - 2j, 0.25 + 1e-3j, 2.0])
+    F.write_boundary_values(str(p), nodes, vals)
+    n2, v2 = F.read_boundary_values(str(p), 20)
+    assert np.array_equal(n2, nodes) and np.array_equal(v2, vals)
+    with pytest.raises(F.CRError) as ei:
+        F.read_boundary_values(str(p), 8)
+    assert ei.value.errnr == 30

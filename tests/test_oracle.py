@@ -80,3 +80,55 @@ def test_oracle_bessel_tables():
         assert abs(L.or_bessk0(x) - sp.k0(x)) <= 2e-7 * sp.k0(x) + 1e-300
         assert abs(L.or_bessk1(x) - sp.k1(x)) <= 2e-7 * sp.k1(x) + 1e-300
     assert L.or_bessk0(600.0) == 0.0
+
+
+def _valued_nodes(g, sv, count, seed, exclude=()):
+    rng = np.random.default_rng(seed)
+    skip = set(int(e) for e in sv.enr) | set(int(x) for x in exclude)
+    pool = [i for i in range(1, g.sanz + 1) if i not in skip]
+    return np.sort(rng.choice(pool, size=count, replace=False)).astype(np.int32)
+
+
+def test_oracle_randb2_keeps_a_system_that_satisfies_its_values():
+    """src/randb2.f90 restated: prescribing at some nodes the potential that
+    system (k0, 1) has there leaves that system's potential unchanged, and
+    every system assembled by kompab (all of them with mixed boundaries)
+    returns exactly the prescribed value at those nodes."""
+    g, sv, sig, cfg, _ = load_case("minimal")
+    P = O.Problem(g, sv)
+    kwn, kwnwi = P.rwaven()
+    kp = P.forward(sig, kwn, kwnwi)
+    nodes = _valued_nodes(g, sv, 12, seed=3)
+    k0 = 2
+    vals = kp[k0, 0, nodes - 1].copy()
+    P.set_boundary_values(nodes, vals)
+    kp2 = P.forward(sig, kwn, kwnwi)
+    assert np.max(np.abs(kp2[k0, 0] - kp[k0, 0])) < 1e-9 * np.max(np.abs(kp[k0, 0]))
+    assert np.array_equal(kp2[:, :, nodes - 1], np.broadcast_to(vals, kp2[:, :, nodes - 1].shape))
+    assert np.max(np.abs(kp2[k0 + 1, 1] - kp[k0 + 1, 1])) > 1e-6 * np.max(np.abs(kp[k0 + 1, 1]))
+
+
+def test_oracle_randb2_values_only_in_kompab_systems():
+    """Without mixed boundaries one factor per wavenumber serves all
+    electrodes: electrode 1's system is assembled by kompab (values applied),
+    the others' right-hand sides by kompb, which leaves the values out, so
+    their potential is 0 at the valued nodes (src/fem.f90:355-376)."""
+    g, sv, sig, cfg, _ = load_case("decoupling_2d_sink")
+    P = O.Problem(g, sv)
+    kwn, kwnwi = np.zeros(1), np.zeros(1)
+    nodes = _valued_nodes(g, sv, 8, seed=4, exclude=[cfg.nsink])
+    vals = np.linspace(0.5, 2.0, len(nodes)) * (1 - 0.1j)
+    P.set_boundary_values(nodes, vals)
+    kp = P.forward(sig, kwn, kwnwi, swrtr=0, lsink=cfg.lsink, nsink=cfg.nsink)
+    assert np.array_equal(kp[0, 0, nodes - 1], vals)
+    assert np.all(kp[0, 1:, nodes - 1] == 0)
+    assert np.all(np.isfinite(kp))
+
+
+def test_oracle_randb2_node_out_of_range_is_error_30():
+    g, sv, sig, cfg, _ = load_case("minimal")
+    P = O.Problem(g, sv)
+    kwn, kwnwi = P.rwaven()
+    P.set_boundary_values([g.sanz + 1], [1.0])
+    with pytest.raises(RuntimeError, match="errnr 30"):
+        P.forward(sig, kwn, kwnwi)

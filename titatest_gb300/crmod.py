@@ -126,6 +126,19 @@ class CRMod:
     def set_refinement(self, maxit: int, tol: float):
         _check(self._h, lib().crgpu_set_refinement(self._h, int(maxit), C.c_double(tol)))
 
+    def set_boundary_values(self, nodes, values):
+        """Dirichlet boundary values (src/randb2.f90): nodes 1-based in the band
+        numbering, complex values, in the order of the boundary-value file
+        (formats.read_boundary_values).  None or an empty list removes them."""
+        if nodes is None or len(nodes) == 0:
+            _check(self._h, lib().crgpu_set_boundary_values(self._h, 0, None, None))
+            return
+        nr = np.ascontiguousarray(nodes, np.int32)
+        vv = np.ascontiguousarray(values, np.complex128)
+        if nr.shape != vv.shape:
+            raise ValueError("nodes and values differ in length")
+        _check(self._h, lib().crgpu_set_boundary_values(self._h, len(nr), ptr(nr, i32p), ptr(vv, f64p)))
+
     def set_stream(self, stream_handle: int):
         """Issue the work on a caller-owned cudaStream_t (e.g.
         torch.cuda.current_stream().cuda_stream); 0 restores the own stream."""
@@ -284,6 +297,8 @@ def run_tomodir(exe_dir: str, precision: int = PLAIN, write: bool = True):
     m = CRMod(td.grid, td.survey, swrtr=cfg.swrtr, lsink=cfg.lsink, nsink=cfg.nsink,
               precision=precision, lsr=cfg.lsr)
     try:
+        if td.boundary_values is not None:
+            m.set_boundary_values(*td.boundary_values)
         kfak = m.bkfak() if (cfg.wkfak and td.grid.relanz and 11 in set(td.grid.typ.tolist())) else None
         out = m.forward(td.sigma, kfak=kfak)
         if write and cfg.lvolt:

@@ -108,7 +108,9 @@ __global__ __launch_bounds__(kAdjThreads) void k_adj_grad(DevProblem P, const do
         double2 kv[4], lv[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            kv[q] = dir[q] ? cz(0.0, 0.0) : kpot[base + nodes[q]];
+            // a Dirichlet node keeps its potential (its value enters the other
+            // rows through the moved column, src/randb2.f90); lambda is 0 there
+            kv[q] = q >= nk ? cz(0.0, 0.0) : kpot[base + nodes[q]];
             lv[q] = dir[q] ? cz(0.0, 0.0) : lambda[base + nodes[q]];
         }
         const double *K = P.elbg + ((size_t)k * P.elanz + e) * 10;
@@ -130,7 +132,7 @@ __global__ __launch_bounds__(kAdjThreads) void k_adj_grad(DevProblem P, const do
             const double beta = P.kg[(size_t)t * P.relanz + rb];
             const double r0 = P.relbg[rb * 3] * beta, r1 = P.relbg[rb * 3 + 1] * beta, r2 = P.relbg[rb * 3 + 2] * beta;
             const bool d0 = P.dirichlet[n0] != 0, d1 = P.dirichlet[n1] != 0;
-            const double2 k0 = d0 ? cz(0.0, 0.0) : kpot[base + n0], k1 = d1 ? cz(0.0, 0.0) : kpot[base + n1];
+            const double2 k0 = kpot[base + n0], k1 = kpot[base + n1];
             const double2 l0 = d0 ? cz(0.0, 0.0) : lambda[base + n0], l1 = d1 ? cz(0.0, 0.0) : lambda[base + n1];
             const double2 u0 = cz(r0 * k0.x + r1 * k1.x, r0 * k0.y + r1 * k1.y);
             const double2 u1 = cz(r1 * k0.x + r2 * k1.x, r1 * k0.y + r2 * k1.y);

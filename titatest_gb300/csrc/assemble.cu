@@ -1,6 +1,6 @@
 // Complex band assembly, Dirichlet rows, diagonal scaling and the right-hand
-// sides: src/kompab.f90:11-194, src/randb.f90:1-84, src/scalab.f90:14-87,
-// src/kompb.f90:1-69.
+// sides: src/kompab.f90:11-194, src/randb.f90:1-84, src/randb2.f90:1-82,
+// src/scalab.f90:14-87, src/kompb.f90:1-69.
 //
 // The matrix lives in a lower-triangular sparse pattern (Pattern in
 // host.cpp); each entry sums its element contributions in element order,
@@ -29,11 +29,11 @@ __global__ void k_adom(DevProblem P, const double2 *__restrict__ sigma, double2 
     adom[gid] = v;
 }
 
-// Value of lower-pattern entry p of system (k, l) before scaling: area part
-// plus the mixed-boundary terms, with Dirichlet rows and columns replaced.
-__device__ __forceinline__ double2 entry_value(const DevProblem &P, const double2 *__restrict__ ad,
-                                               const double *__restrict__ kgl, const double2 *__restrict__ sigma,
-                                               int p, int i, int c, bool dir_i) {
+// Value of lower-pattern entry p of system (k, l) as kompab assembles it:
+// area part plus the mixed-boundary terms.
+__device__ __forceinline__ double2 entry_raw(const DevProblem &P, const double2 *__restrict__ ad,
+                                             const double *__restrict__ kgl, const double2 *__restrict__ sigma,
+                                             int p) {
     double2 v = ad[p];
     for (int q = P.bnd_ptr[p]; q < P.bnd_ptr[p + 1]; q++) {
         const int code = P.bnd_list[q];
@@ -42,8 +42,16 @@ __device__ __forceinline__ double2 entry_value(const DevProblem &P, const double
         const double2 sg = sigma[P.brnr[rb]];
         v = cadd(v, cz(dum * sg.x, dum * sg.y));
     }
-    if (dir_i || P.dirichlet[c]) v = (c == i) ? cz(1.0, 0.0) : cz(0.0, 0.0);
     return v;
+}
+
+// The same before scaling, with Dirichlet rows and columns replaced
+// (src/randb.f90, src/randb2.f90: diagonal 1, the rest of the row and column 0).
+__device__ __forceinline__ double2 entry_value(const DevProblem &P, const double2 *__restrict__ ad,
+                                               const double *__restrict__ kgl, const double2 *__restrict__ sigma,
+                                               int p, int i, int c, bool dir_i) {
+    if (dir_i || P.dirichlet[c]) return (c == i) ? cz(1.0, 0.0) : cz(0.0, 0.0);
+    return entry_raw(P, ad, kgl, sigma, p);
 }
 
 // 1/sqrt(|v|) = (re^2 + im^2)^(-1/4) without FP64 division or square root
@@ -186,6 +194,49 @@ void launch_rhs(const DevProblem &P, const DevBatch &B, int nrhs, int lsink, int
     size_t tot = (size_t)B.nsys * nrhs * P.n;
     int nt = 256;
     k_rhs<<<(unsigned)((tot + nt - 1) / nt), nt, 0, st>>>(P, B, nrhs, lsink, nsink);
+}
+
+// Valued Dirichlet nodes (src/randb2.f90:37-79) in the right-hand sides that
+// kompab built: every system when nrhs == 1, right-hand side 0 of each
+// wavenumber when nrhs == eanz (the others are kompb's, src/fem.f90:355-376,
+// which leaves the values out).  A valued node's b is -value; any other row
+// that is not a Dirichlet row gains value * a(i, m) for each valued neighbour
+// m, with a(i, m) as kompab assembled it.  b is already scaled by fak; fak is 1
+// on Dirichlet rows.  Grid (row blocks, systems).
+__global__ void k_rhs_randb2(DevProblem P, DevBatch B, int nrhs, const double2 *__restrict__ sigma,
+                             const double2 *__restrict__ adom) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
+    if (i >= P.n) return;
+    double2 *b = B.b + ((size_t)s * nrhs) * P.n;
+    const uint8_t di = P.dirichlet[i];
+    if (di == 2) {
+        const double2 v = P.rwd_b[i];
+        b[i] = cz(-v.x, -v.y);
+        return;
+    }
+    if (di) return;
+    const int k = B.ks[s], l = B.ls[s];
+    const double2 *ad = adom + (size_t)k * P.nnz;
+    const double *kgl = P.kg + ((size_t)k * P.eanz + l) * P.relanz;
+    double2 acc = cz(0.0, 0.0);
+    bool any = false;
+    for (int q = P.fptr[i]; q < P.fptr[i + 1]; q++) {
+        const double2 w = P.rwd_col[P.fcol[q]];
+        if (w.x == 0.0 && w.y == 0.0) continue;
+        acc = cadd(acc, cmul(w, entry_raw(P, ad, kgl, sigma, P.fidx[q])));
+        any = true;
+    }
+    if (!any) return;
+    const double f = B.fak[(size_t)s * P.n + i];
+    const double2 v = b[i];
+    b[i] = cz(v.x + acc.x * f, v.y + acc.y * f);
+}
+
+void launch_rhs_randb2(const DevProblem &P, const DevBatch &B, int nrhs, const double2 *sigma,
+                       const double2 *adom, cudaStream_t st) {
+    if (!P.lrandb2) return;
+    const int nt = 128;
+    k_rhs_randb2<<<dim3((P.n + nt - 1) / nt, B.nsys), nt, 0, st>>>(P, B, nrhs, sigma, adom);
 }
 
 }  // namespace crgpu

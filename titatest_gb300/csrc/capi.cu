@@ -375,6 +375,10 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
             launch_rhs(P, B, nr, c->lsink, c->nsink, c->st);
             c->stats.kernel_launches += 1;
         }
+        if (P.lrandb2) {
+            launch_rhs_randb2(P, B, nr, d_sigma, c->d_adom, c->st);
+            c->stats.kernel_launches += 1;
+        }
         const int tail = tail_systems(c, ns);
         if (!cap) cudaEventRecord(f0, c->st);
         if (!tail) {
@@ -757,6 +761,41 @@ int crgpu_set_refinement(crgpu_ctx *c, int32_t maxit, double tol) {
     drop_graph(c);
     c->refine_maxit = maxit;
     c->refine_tol = tol;
+    return 0;
+}
+
+int crgpu_set_boundary_values(crgpu_ctx *c, int32_t rwdanz, const int32_t *rwdnr, const double *rwd) {
+    if (!c || rwdanz < 0 || (rwdanz > 0 && (!rwdnr || !rwd))) return ERR_ARG;
+    const int n = (int)c->hg.n;
+    for (int ir = 0; ir < rwdanz; ir++)  // src/rrandb.f90 (error 30)
+        if (rwdnr[ir] < 1 || rwdnr[ir] > n)
+            return fail(c, 30, "boundary value node " + std::to_string(rwdnr[ir]) + " outside 1.." +
+                                   std::to_string(n));
+    drop_graph(c);
+    c->factors_resident = false;
+    // type-13 nodes (src/randb.f90) first; src/randb2.f90 then sets b(k) = -value
+    // (the last value of a node listed twice) and moves the column of a node
+    // whose column is still in the matrix (the first value)
+    std::vector<uint8_t> dir(c->hg.dirichlet);
+    std::vector<double2> vals((size_t)2 * n, make_double2(0.0, 0.0));
+    for (int ir = 0; ir < rwdanz; ir++) {
+        const int k = rwdnr[ir] - 1;
+        const double2 v = make_double2(rwd[2 * ir], rwd[2 * ir + 1]);
+        vals[k] = v;
+        if (dir[k] == 0) vals[(size_t)n + k] = v;
+        dir[k] = 2;
+    }
+    if (!c->d_rwd) {
+        int e = dalloc(c, &c->d_rwd, (size_t)2 * n);
+        if (e) return e;
+    }
+    CUCHECK(c, cudaMemcpyAsync((void *)c->P.dirichlet, dir.data(), (size_t)n, cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemcpyAsync(c->d_rwd, vals.data(), vals.size() * sizeof(double2), cudaMemcpyHostToDevice,
+                               c->st));
+    CUCHECK(c, cudaStreamSynchronize(c->st));
+    c->P.lrandb2 = rwdanz > 0;
+    c->P.rwd_b = c->d_rwd;
+    c->P.rwd_col = c->d_rwd + n;
     return 0;
 }
 

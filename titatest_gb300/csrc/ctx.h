@@ -27,6 +27,7 @@ struct crgpu_ctx {
     double2 *d_volt = nullptr, *d_sigmaa = nullptr, *d_sens = nullptr;
     float2 *d_kpot32 = nullptr;  // complex64 copy of kpot (mixed precision: the Jacobian's input)
     double *d_kfak = nullptr;
+    double2 *d_rwd = nullptr;     // [2][n] valued Dirichlet nodes: b values, moved-column values
     double2 *d_sigma0 = nullptr;  // reference conductivity (singularity removal)
     int *d_err = nullptr;
     // batch buffers

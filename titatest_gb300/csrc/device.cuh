@@ -22,7 +22,12 @@ struct DevProblem {
     const double *x, *y;
     const int32_t *etype, *enodes;          // elanz, elanz*4
     const int32_t *btype, *bnodes, *brnr;   // relanz, relanz*2, relanz
-    const uint8_t *dirichlet;               // n
+    const uint8_t *dirichlet;               // n: 1 type-13 node (src/randb.f90), 2 valued node (src/randb2.f90)
+    // valued Dirichlet nodes (src/randb2.f90), when lrandb2: rwd_b[i] the value
+    // whose negative becomes b(i); rwd_col[i] the value whose column is moved to
+    // the other rows' right-hand sides (0 where that column was already removed)
+    int lrandb2;
+    const double2 *rwd_b, *rwd_col;         // n, n
     // band pattern
     const int32_t *rowptr, *col, *row;
     const int32_t *dom_ptr, *dom_list, *bnd_ptr, *bnd_list;

@@ -15,6 +15,8 @@ void launch_assemble(const DevProblem &P, const DevBatch &B, const double2 *sigm
                      const double2 *adom, cudaStream_t st);
 void launch_rhs(const DevProblem &P, const DevBatch &B, int nrhs, int lsink, int nsink,
                 cudaStream_t st);
+void launch_rhs_randb2(const DevProblem &P, const DevBatch &B, int nrhs, const double2 *sigma,
+                       const double2 *adom, cudaStream_t st);
 
 // singularity removal (src/refsig.f90, src/potana.f90, kompab lsr branch)
 void launch_refsig(const DevProblem &P, const double2 *sigma, double2 *sigma0, cudaStream_t st);

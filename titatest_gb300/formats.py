@@ -10,6 +10,7 @@ discards the rest of its last record):
 * ``config.dat``-- src/rdatm.f90:6-136
 * ``crmod.cfg`` -- src/fem.f90:163-205
 * ``volt.dat``  -- src/wdatm.f90 (written by CRMod)
+* boundary values -- src/rrandb.f90 (lrandb2)
 
 Node, element and electrode numbers are kept 1-based, exactly as in the
 files, so that the arrays can be handed to the C ABI unchanged.
@@ -462,6 +463,70 @@ def read_volt(path: str):
     return s, v, bet, pha
 
 
+def _read_items(rec: _Records, kinds: Sequence[str]) -> list:
+    """One list-directed READ of integers ("i"), reals ("r") and complex
+    numbers ("c", written ``(re, im)``; a bare real reads as re + 0i)."""
+    out: list = []
+    toks: List[str] = []
+    q = 0
+    while len(out) < len(kinds):
+        if q >= len(toks):
+            toks = rec._tokens(rec.read_line())
+            q = 0
+            continue
+        kind = kinds[len(out)]
+        t = toks[q]
+        if kind == "c" and t.startswith("("):
+            parts = [t]
+            while not parts[-1].endswith(")"):
+                q += 1
+                while q >= len(toks):
+                    toks = rec._tokens(rec.read_line())
+                    q = 0
+                parts.append(toks[q])
+            nums = " ".join(parts).strip("()").replace("(", " ").replace(")", " ").split()
+            if len(nums) != 2:
+                raise CRError(3, f"complex value {' '.join(parts)!r} in {rec.path}")
+            out.append(complex(_f(nums[0]), _f(nums[1])))
+        elif kind == "i":
+            out.append(int(t))
+        elif kind == "c":
+            out.append(complex(_f(t), 0.0))
+        else:
+            out.append(_f(t))
+        q += 1
+    return out
+
+
+def read_boundary_values(path: str, sanz: int):
+    """Boundary values of src/rrandb.f90 (complex case): rwdanz, then rwdanz
+    records ``node value`` (Dirichlet), then rwnanz and rwnanz values
+    (Neumann; read and not used, as in the reference).  Returns (nodes int32
+    1-based, values complex128).  A node above sanz raises errnr 30."""
+    rec = _Records(path)
+    n = _read_items(rec, "i")[0]
+    nodes = np.zeros(n, np.int32)
+    vals = np.zeros(n, np.complex128)
+    for i in range(n):
+        nodes[i], vals[i] = _read_items(rec, "ic")
+        if nodes[i] > sanz:
+            raise CRError(30, f"boundary node {nodes[i]} in {path}")
+    nn = _read_items(rec, "i")[0]
+    if nn > 0:
+        _read_items(rec, "c" * nn)
+    return nodes, vals
+
+
+def write_boundary_values(path: str, nodes, values):
+    """The file read by read_boundary_values (no Neumann values)."""
+    with open(path, "w") as fh:
+        fh.write(f"{len(nodes)}\n")
+        for k, v in zip(nodes, values):
+            v = complex(v)
+            fh.write(f"{int(k)} ({v.real!r},{v.imag!r})\n")
+        fh.write("0\n")
+
+
 @dataclasses.dataclass
 class Tomodir:
     """A CRMod working set loaded from crmod.cfg."""
@@ -470,6 +535,7 @@ class Tomodir:
     grid: Grid
     survey: Survey
     sigma: np.ndarray
+    boundary_values: Optional[tuple] = None  # (nodes, values) when lrandb2
 
 
 def load_crmod(exe_dir: str, config_override: Optional[str] = None) -> Tomodir:
@@ -484,5 +550,6 @@ def load_crmod(exe_dir: str, config_override: Optional[str] = None) -> Tomodir:
     cpath = config_override or p(cfg.dstrom)
     strnr, vnr, strom = read_config(cpath, len(enr))
     sigma = read_rho(p(cfg.dsigma), grid.elanz)
+    bv = read_boundary_values(p(cfg.drandb), grid.sanz) if cfg.lrandb2 else None
     return Tomodir(cfg=cfg, grid=grid, survey=Survey(enr=enr, strnr=strnr, vnr=vnr, strom=strom),
-                   sigma=sigma)
+                   sigma=sigma, boundary_values=bv)
