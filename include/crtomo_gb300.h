@@ -140,7 +140,8 @@ int crgpu_forward_device(crgpu_ctx *ctx, const void *sigma_device, int32_t volt_
  *   sens : sens(nanz, elanz) complex, column-major (src/alloci.f90)
  * Mode 0 into page-locked host memory is written by the kernel directly;
  * otherwise the device result is copied in chunks, overlapped with the
- * computation (mode 1 keeps the device copy for crgpu_update). */
+ * computation (mode 1 keeps the device copy for crgpu_update).  sens NULL:
+ * the device copy only, nothing copied to the host. */
 int crgpu_sens(crgpu_ctx *ctx, int32_t mode, double *sens);
 int crgpu_sens_device(crgpu_ctx *ctx, int32_t mode, void *sens_device);
 

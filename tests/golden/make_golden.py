@@ -8,6 +8,7 @@ Run in a container where the reference checkout is present:
 Forward cases (<case>/): the CRMod inputs (elem.dat, elec.dat, rho.dat,
 crmod.cfg) and the CRMod output volt.dat of a reference tomodir.  The
 measurement configurations are the (strnr, vnr) columns of volt.dat.
+Inversion cases add the tomodir's crtomo.cfg and CRTomo's inv.ctr.
 
 CutMcK cases (cutmck_<case>/): the grid before (elem.dat.orig, elec.dat.orig)
 and after (elem.dat, elec.dat) the reference's Cuthill-McKee renumbering.
@@ -25,6 +26,14 @@ FORWARD = {
     "testmodinv": "tests/TestModInv/Reference",
     "mixed_surf": "tests/2.5D_mixed_surf/Reference",
     "decoupling_2d_sink": "tests/GridDecoupling/regular_grids/01_no_decoupling",
+}
+
+# inversion cases: the CRTomo configuration and its control output inv.ctr
+# (src/kont2.f90), added to the forward case of the same tomodir, whose
+# volt.dat is the inverted data set
+INVERSION = {
+    "minimal": "tests/minimal/Reference",
+    "mixed_surf": "tests/2.5D_mixed_surf/Reference",
 }
 
 CUTMCK = {
@@ -47,6 +56,11 @@ def main(ref: str):
             shutil.copyfile(os.path.join(src, f), os.path.join(out, os.path.basename(f)))
         with open(os.path.join(out, "SOURCE"), "w") as fh:
             fh.write(d + "\n")
+    for name, d in INVERSION.items():
+        out = os.path.join(here, name)
+        src = os.path.join(ref, d)
+        for f in ("exe/crtomo.cfg", "inv/inv.ctr"):
+            shutil.copyfile(os.path.join(src, f), os.path.join(out, os.path.basename(f)))
     for name, d in CUTMCK.items():
         out = os.path.join(here, "cutmck_" + name)
         os.makedirs(out, exist_ok=True)

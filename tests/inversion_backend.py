@@ -1,0 +1,102 @@
+"""Test infrastructure: the CPU oracle as a backend of
+titatest_gb300.inversion.Inversion, and a reader of the IT/UP rows of the
+reference's inv.ctr (src/kont2.f90)."""
+import os
+
+import numpy as np
+
+from conftest import GOLDEN
+
+from oracle import oracle as O
+
+
+class OracleBackend:
+    """forward + src/bvolti.f90, src/bsensi.f90 and src/update.f90 by the
+    oracle (complex128)."""
+
+    def __init__(self, grid, survey, kwn, kwnwi, swrtr=1, lsink=False, nsink=0):
+        self.P = O.Problem(grid, survey)
+        self.grid, self.kwn, self.kwnwi = grid, kwn, kwnwi
+        self.kw = dict(swrtr=swrtr, lsink=lsink, nsink=nsink)
+
+    def forward(self, sigma):
+        self.sigma = np.array(sigma, np.complex128)
+        self.kp = self.P.forward(self.sigma, self.kwn, self.kwnwi, **self.kw)
+        hp = self.P.rtrafo(self.kp, self.kwnwi, self.kw["swrtr"])
+        self.volt, sa = self.P.bvolt(hp, 1, None)
+        return sa
+
+    def sensitivities(self):
+        self.J = self.P.bsens(self.kp, self.kwn, self.kwnwi, self.sigma, self.volt, mode=1,
+                              swrtr=self.kw["swrtr"])
+
+    def update(self, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx, nachbar, lam, eps, ncgmax, step, par):
+        _, dpar, _, _, ncg = O.update(self.J, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx=nx, nachbar=nachbar,
+                                      maxnk=self.grid.maxnk, lam=lam, eps=eps, ncgmax=ncgmax, step=step, par=par)
+        return dpar, ncg
+
+    def jacobian(self):
+        return self.J
+
+
+def golden_rows(case):
+    """(kind, index, nrmsd, bdpar, lam, rough, ncg, step) of every IT/UP
+    line of the case's inv.ctr; None where the line has no such column."""
+    rows = []
+    with open(os.path.join(GOLDEN, case, "inv.ctr")) as fh:
+        for line in fh:
+            t = line.split()
+            if not t or t[0] not in ("IT", "UP"):
+                continue
+            if t[0] == "IT" and len(t) == 6:
+                rows.append(("IT", int(t[1]), float(t[2]), None, None, None, None, None))
+            elif t[0] == "IT":
+                rows.append(("IT", int(t[1]), float(t[2]), float(t[3]), float(t[4]), float(t[5]), int(t[6]),
+                             float(t[10])))
+            else:
+                rows.append(("UP", int(t[1]), float(t[2]), float(t[3]), float(t[4]), float(t[5]), int(t[6]),
+                             float(t[7])))
+    return rows
+
+
+def inversion_case(case):
+    """(grid, survey, data, cfg, kwn, kwnwi) of a golden inversion case."""
+    from titatest_gb300 import formats as F
+    from titatest_gb300 import inversion as I
+    d = os.path.join(GOLDEN, case)
+    cfg = I.read_crtomo_cfg(os.path.join(d, "crtomo.cfg"))
+    g = F.read_elem(os.path.join(d, "elem.dat"))
+    enr = F.read_elec(os.path.join(d, "elec.dat"), g.sanz)
+    data = I.read_data(os.path.join(d, "volt.dat"), cfg, len(enr))
+    sv = F.Survey(enr=enr, strnr=data.strnr, vnr=data.vnr, strom=np.ones(len(data.strnr)))
+    kwn, kwnwi = O.Problem(g, sv).rwaven()
+    return g, sv, data, cfg, kwn, kwnwi
+
+
+# Tolerances against the printed trace (4 significant digits, the step size
+# 3).  A trial whose CG ran to its cap (ncg = ncgmax) is a fixed sequence of
+# operations: all fields within a few 1e-3.  A trial whose CG stopped on its
+# residual test (|r| <= 1e-4 |b|, src/cg_mod.f90) stops wherever rounding puts
+# the residual below the bound, and the model it returns can move by the
+# system's condition times 1e-4: misfit, roughness and model change within a
+# few percent, lambda (set by the earlier misfits) within 1e-2, the CG count
+# within 8 steps.  Kind, index and step length always agree.
+TIGHT = dict(rms=3e-3, lam=3e-3, rough=5e-3, bdpar=1.5e-2, ncg=0)
+LOOSE = dict(rms=5e-2, lam=1e-2, rough=5e-2, bdpar=1e-1, ncg=8)
+
+
+def compare_rows(gold, rows, ncgmax):
+    assert len(rows) >= len(gold), (len(rows), len(gold))
+    for i, g in enumerate(gold):
+        r = rows[i]
+        where = (i, g[0], g[1])
+        assert (r.kind, r.index) == (g[0], g[1]), where
+        t = TIGHT if (g[6] is None or g[6] == ncgmax) else LOOSE
+        assert abs(r.nrmsd / g[2] - 1) < t["rms"], (where, r.nrmsd, g[2])
+        if g[3] is None:
+            continue
+        assert abs(r.bdpar / g[3] - 1) < t["bdpar"], (where, r.bdpar, g[3])
+        assert abs(r.lam / g[4] - 1) < t["lam"], (where, r.lam, g[4])
+        assert abs(r.rough / g[5] - 1) < t["rough"], (where, r.rough, g[5])
+        assert abs(r.ncg - g[6]) <= t["ncg"], (where, r.ncg, g[6])
+        assert r.step == g[7], (where, r.step, g[7])

@@ -1,0 +1,65 @@
+"""CRTomo's inversion loop with the GPU backend (crgpu_forward in bvolti
+mode, crgpu_sens kept on the device, crgpu_update) against the reference's
+inv.ctr, with the tolerances of tests/test_inversion.py, in complex128 and in
+mixed precision (complex64 factor with FP64 refinement to 1e-10).  In
+mixed precision the Jacobian carries ~1e-5 relative error, which moves the
+trials whose CG stops on its residual test the most (mixed_surf UP 9: 1.4% in
+misfit, 6 CG steps), inside the tolerances for such trials."""
+import pytest
+
+from inversion_backend import compare_rows, golden_rows, inversion_case
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(case, precision, max_iterations=None):
+    from titatest_gb300 import inversion as I
+    g, sv, data, cfg, kwn, kwnwi = inversion_case(case)
+    b = I.DeviceBackend(g, sv, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink, precision, refinement=(8, 1e-10))
+    try:
+        inv = I.Inversion(g, data, cfg, b)
+        rows = inv.run(max_iterations=max_iterations)
+    finally:
+        b.close()
+    return inv, rows
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_gpu_inversion_reproduces_reference_trace_minimal(gpu_lib, prec):
+    inv, rows = _run("minimal", prec)
+    gold = golden_rows("minimal")
+    assert len(rows) == len(gold) == 21
+    compare_rows(gold, rows, inv.ncgmax)
+    assert inv.status == "fpi"
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_gpu_inversion_reproduces_reference_trace_mixed_surf(gpu_lib, prec):
+    inv, rows = _run("mixed_surf", prec, max_iterations=1)
+    gold = golden_rows("mixed_surf")[:15]
+    assert len(rows) == 15 and inv.status == "max_iterations"
+    compare_rows(gold, rows, inv.ncgmax)
+
+
+def test_run_crtomo_on_a_tomodir(gpu_lib, tmp_path):
+    """The tomodir entry point: crtomo.cfg with its relative paths, the
+    inverted model and inv.ctr written to the result directory."""
+    import os
+    import shutil
+
+    import numpy as np
+
+    from conftest import GOLDEN
+    from titatest_gb300 import formats as F
+    from titatest_gb300 import inversion as I
+    src = os.path.join(GOLDEN, "minimal")
+    for sub, files in (("exe", ["crtomo.cfg"]), ("grid", ["elem.dat", "elec.dat"]), ("mod", ["volt.dat"])):
+        os.makedirs(tmp_path / sub)
+        for f in files:
+            shutil.copyfile(os.path.join(src, f), tmp_path / sub / f)
+    inv = I.run_crtomo(str(tmp_path / "exe"), precision=0)
+    compare_rows(golden_rows("minimal"), inv.rows, inv.ncgmax)
+    lines = (tmp_path / "inv" / "inv.ctr").read_text().splitlines()
+    assert len(lines) == 21 and lines[0].split()[:3] == ["IT", "0", "111.9"]
+    sig = F.read_rho(str(tmp_path / "inv" / "rho.dat"), inv.grid.elanz)
+    assert np.max(np.abs(sig / inv.sigma - 1)) < 1e-8

@@ -191,6 +191,11 @@ class CRMod:
         _check(self._h, lib().crgpu_sens(self._h, int(mode), ptr(buf, f64p)))
         return buf.T
 
+    def sens_on_device(self, mode: int = 1):
+        """The sensitivities of the last forward into the context's device
+        array only (for update), with no host copy."""
+        _check(self._h, lib().crgpu_sens(self._h, int(mode), None))
+
     def bsens(self) -> np.ndarray:
         return self.sens(0)
 

@@ -940,12 +940,31 @@ int crgpu_sens_device(crgpu_ctx *c, int32_t mode, void *sens_device) {
 // columns (contiguous in sens(nanz, manz)) copied by a second stream while
 // the next chunk is computed.
 int crgpu_sens(crgpu_ctx *c, int32_t mode, double *sens) {
-    if (!c || !sens || (mode != 0 && mode != 1)) return ERR_ARG;
+    if (!c || (mode != 0 && mode != 1)) return ERR_ARG;
     if (!c->have_forward) return fail(c, ERR_ARG, "crgpu_sens before crgpu_forward");
     const size_t nanz = c->nanz, manz = c->hg.elanz, cnt = nanz * manz;
     if (!c->d_sens) {
         int e = dalloc(c, &c->d_sens, cnt);
         if (e) return e;
+    }
+    if (!sens) {  // kept on the device only, for crgpu_update
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, c->st);
+        launch_bsens(c->P, c->d_kpot, c->d_kpot32, c->d_sigma, c->d_volt, mode, c->precision == CRGPU_MIXED,
+                     c->d_sens, c->st);
+        c->stats.kernel_launches += 1;
+        cudaEventRecord(b, c->st);
+        CUCHECK(c, cudaStreamSynchronize(c->st));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        c->stats.ms_sens = ms;
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        c->last_sens = c->d_sens;
+        CUCHECK(c, cudaGetLastError());
+        return 0;
     }
     // CRMod sensitivities into pinned (page-locked) host memory are written by
     // the kernel itself, over the host link, while it computes; otherwise

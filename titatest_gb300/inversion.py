@@ -1,0 +1,814 @@
+"""CRTomo's complex-resistivity inversion loop over the GPU hot path.
+
+The outer loop of src/inv.f90:330-990 restated on the host: the data misfit
+(src/dmisft.f90), the first regularisation parameter (src/blam0.f90), the
+lambda search and the step-length search (src/inv.f90:760-905 with
+src/parfit.f90), src/bpar.f90, src/bsigma.f90 and the roughness
+(src/brough_mod.f90).  Each step calls a backend for the three heavy parts:
+the forward with src/bvolti.f90 voltages, the Jacobian of src/bsensi.f90, and
+the Gauss-Newton update of src/update.f90 + src/cg_mod.f90.  DeviceBackend
+runs them through the C ABI (crgpu_forward, crgpu_sens, crgpu_update); the
+controller holds only O(nanz + manz) vectors.
+
+Covered: the complex inversion stage (CRI) with the error model of
+src/rdati.f90 (or individual errors), homogeneous or file start models
+(src/bsigm0.f90), structured (ltri 0) and triangular (ltri 1, 2)
+smoothness, a fixed lambda (llamf), the polarity checks (src/chkpol.f90,
+chkpo2 of src/dmisft.f90) and the stopping rules of src/inv.f90:560-640.
+The final phase improvement (lfphai, a real-valued phase-only CG) is not
+built: the run ends where the reference would switch to it, with
+status "fpi".  Robust inversion, difference inversion, prior models, data
+noise and DC inversion (ldc) raise NotImplementedError.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+import os
+from typing import List, Optional
+
+import numpy as np
+
+from . import formats
+from . import regularization as R
+
+_PI = math.acos(-1.0)
+
+
+# ---------------------------------------------------------------------------
+# crtomo.cfg (src/rall.f90:230-470)
+# ---------------------------------------------------------------------------
+@dataclasses.dataclass
+class CRTomoConfig:
+    mswitch: int
+    delem: str
+    delectr: str
+    dstrom: str
+    ramd: str
+    ldiff: bool
+    dd0: str
+    dm0: str
+    dfm0: str
+    nx: int
+    nz: int
+    alfx: float
+    alfz: float
+    itmax: int
+    ldc: bool
+    lrobust: bool
+    lfphai: bool
+    stabw0: float
+    stabm0: float
+    stabpA1: float
+    stabpB: float
+    stabpA2: float
+    stabp0: float
+    lrho0: bool
+    bet0: float
+    pha0: float
+    lagain: bool
+    swrtr: int
+    lsink: bool
+    nsink: int
+    lrandb2: bool
+    drandb: str
+    ltri: int = 0
+    llamf: int = 0
+    lamfix: float = 0.0
+    lffhom: bool = False
+
+
+def _cfg_lines(path: str):
+    with open(path) as fh:
+        lines = fh.read().splitlines()
+    pos = 0
+
+    def next_line() -> str:
+        """src/get_unit.f90 read_comments, then one record."""
+        nonlocal pos
+        while pos < len(lines) and lines[pos].lstrip().startswith("#"):
+            pos += 1
+        if pos >= len(lines):
+            raise formats.CRError(2, f"end of file in {path}")
+        pos += 1
+        return lines[pos - 1]
+
+    def at_end() -> bool:
+        q = pos
+        while q < len(lines) and lines[q].lstrip().startswith("#"):
+            q += 1
+        return q >= len(lines)
+
+    return next_line, at_end
+
+
+def _tok(line: str, n: int = 1):
+    toks = formats._Records._tokens(line)
+    if len(toks) < n:
+        raise ValueError(line)
+    return toks[:n]
+
+
+def read_crtomo_cfg(path: str) -> CRTomoConfig:
+    """crtomo.cfg in the order src/rall.f90:230-470 reads it."""
+    nxt, at_end = _cfg_lines(path)
+    v = {}
+    line = nxt()
+    try:
+        v["mswitch"] = int(_tok(line)[0])
+    except ValueError:  # src/rall.f90:234 (err=98: mswitch stays 0)
+        v["mswitch"] = 0
+    for key in ("delem", "delectr", "dstrom", "ramd"):
+        v[key] = nxt().strip()
+    v["ldiff"] = formats._logical(_tok(nxt())[0])
+    for key in ("dd0", "dm0", "dfm0"):
+        v[key] = nxt().strip()
+    line = nxt()  # iseedpri, modl_stdn (a failing read consumes the record)
+    v["nx"] = int(_tok(nxt())[0])
+    v["nz"] = int(_tok(nxt())[0])
+    v["alfx"] = formats._f(_tok(nxt())[0])
+    v["alfz"] = formats._f(_tok(nxt())[0])
+    v["itmax"] = int(_tok(nxt())[0])
+    for key in ("ldc", "lrobust", "lfphai"):
+        v[key] = formats._logical(_tok(nxt())[0])
+    for key in ("stabw0", "stabm0", "stabpA1", "stabpB", "stabpA2", "stabp0"):
+        v[key] = formats._f(_tok(nxt())[0])
+    v["lrho0"] = formats._logical(_tok(nxt())[0])
+    v["bet0"] = formats._f(_tok(nxt())[0])
+    v["pha0"] = formats._f(_tok(nxt())[0])
+    v["lagain"] = formats._logical(_tok(nxt())[0])
+    v["swrtr"] = int(_tok(nxt())[0])
+    v["lsink"] = formats._logical(_tok(nxt())[0])
+    v["nsink"] = int(_tok(nxt())[0])
+    v["lrandb2"] = formats._logical(_tok(nxt())[0])
+    v["drandb"] = nxt().strip()
+    cfg = CRTomoConfig(**v)
+    if not at_end():  # src/rall.f90:420-445, read '(I2)'
+        line = nxt()
+        try:
+            cfg.ltri = int(line[:2])
+        except ValueError:
+            cfg.ltri = 0
+        if cfg.ltri & 32:
+            cfg.llamf = 1
+            try:
+                cfg.lamfix = formats._f(_tok(nxt())[0])
+            except (ValueError, formats.CRError):
+                cfg.lamfix = 1.0
+            cfg.ltri -= 32
+            if cfg.ltri & 64:
+                cfg.llamf += 2
+                cfg.ltri -= 64
+    if cfg.ltri > 15:
+        raise formats.CRError(1, "ltri switch above 15")
+    cfg.lffhom = cfg.stabp0 < 0  # src/rall.f90:470-471
+    if cfg.lffhom:
+        cfg.stabp0 = -cfg.stabp0
+    if (cfg.nx <= 0 or cfg.nz <= 0) and cfg.ltri == 0:
+        cfg.ltri = 1
+    if cfg.ltri == 0 and (cfg.nx < 2 or cfg.nz < 2):
+        raise formats.CRError(89, "structured smoothness needs nx, nz >= 2")
+    if cfg.itmax < 0 or cfg.itmax >= 100:
+        raise formats.CRError(61, "itmax outside 0..99")
+    if cfg.stabw0 <= 0.0 or cfg.stabm0 < 0.0:
+        raise formats.CRError(104, "resistance error model")
+    if (not cfg.ldc and cfg.lfphai and (cfg.stabp0 < 0 or cfg.stabpA2 < 0 or
+                                        (cfg.stabp0 == 0 and cfg.stabpA2 == 0 and cfg.stabpA1 == 0))):
+        raise formats.CRError(105, "phase error model")
+    if cfg.lrho0 and (cfg.bet0 <= 0.0 or (not cfg.ldc and abs(cfg.pha0) > 1e3 * _PI)):
+        raise formats.CRError(91, "homogeneous start model")
+    if cfg.ldc:
+        cfg.lfphai = False
+    return cfg
+
+
+# ---------------------------------------------------------------------------
+# data and error model (src/rdati.f90:100-375)
+# ---------------------------------------------------------------------------
+@dataclasses.dataclass
+class Data:
+    strnr: np.ndarray
+    vnr: np.ndarray
+    dat: np.ndarray        # -ln|R| - i phase/1000 (complex)
+    wmatdr: np.ndarray     # 1/eps_r^2
+    wmatdp: np.ndarray     # 1/eps_p^2
+    wmatd_cri: np.ndarray  # 1/(eps_r^2 + eps_p^2)
+
+
+def read_data(path: str, cfg: CRTomoConfig, eanz: int) -> Data:
+    """Measurements and their weights.  Without individual errors the error
+    model err(R) = A1 |R| + A2 (as an error of ln R: 1e-2 A1 + A2/|R|) and
+    err(phase) = (A1p |R|^B + 1e-2 A2p |phase| + A3p) mrad."""
+    rec = formats._Records(path)
+    first = rec._tokens(rec.read_line())
+    nanz = int(first[0])
+    lindiv = False
+    if len(first) > 1:
+        try:
+            lindiv = formats._logical(first[1])
+        except ValueError:
+            lindiv = False
+    strnr = np.zeros(nanz, np.int32)
+    vnr = np.zeros(nanz, np.int32)
+    dat = np.zeros(nanz, np.complex128)
+    wr = np.zeros(nanz)
+    wp = np.zeros(nanz)
+    wc = np.zeros(nanz)
+    crtf = None
+    for i in range(nanz):
+        t = rec._tokens(rec.read_line())
+        if crtf is None:
+            crtf = int(t[0]) - 10000 >= 0
+        if crtf:
+            s, v, rest = int(t[0]), int(t[1]), t[2:]
+        else:
+            e = [int(x) for x in t[:4]]
+            s, v, rest = e[0] * 10000 + e[1], e[2] * 10000 + e[3], t[4:]
+        bet = formats._f(rest[0])
+        pha = 0.0 if cfg.ldc else formats._f(rest[1])
+        if lindiv:
+            k = 1 if cfg.ldc else 2
+            stabw = formats._f(rest[k]) / bet
+            stabwp = 0.0 if cfg.ldc else 1e-3 * formats._f(rest[k + 1])
+            if stabw <= 0 or (not cfg.ldc and stabwp <= 0):
+                raise formats.CRError(88, f"datum {i + 1}: error not positive")
+        else:
+            stabwp = (cfg.stabpA1 * bet ** cfg.stabpB + 1e-2 * cfg.stabpA2 * abs(pha) + cfg.stabp0) * 1e-3
+            if bet <= 0.0:
+                raise formats.CRError(94, f"datum {i + 1}: resistance not positive")
+            stabw = 1e-2 * cfg.stabw0 + cfg.stabm0 / bet
+        if bet <= 0.0:
+            raise formats.CRError(94, f"datum {i + 1}: resistance not positive")
+        if not cfg.ldc and abs(pha) > 1e3 * _PI:
+            raise formats.CRError(95, f"datum {i + 1}: phase beyond pi")
+        e1, e2, e3, e4 = s % 10000, s // 10000, v % 10000, v // 10000
+        if min(e1, e2, e3, e4) < 0 or max(e1, e2, e3, e4) > eanz:
+            raise formats.CRError(46, f"datum {i + 1}: electrode number")
+        strnr[i], vnr[i] = s, v
+        dat[i] = complex(-math.log(bet), -pha / 1e3)
+        wr[i] = 1.0 / stabw ** 2
+        if not cfg.ldc:
+            wc[i] = 1.0 / (stabw ** 2 + stabwp ** 2)
+            wp[i] = 1.0 / stabwp ** 2
+    if lindiv:
+        t = rec._tokens(rec.read_line())
+        sw = formats._f(t[0])
+        if cfg.ldc:
+            wr *= sw * sw
+        else:
+            swp = formats._f(t[1])
+            if sw <= 0 or swp <= 0:
+                raise formats.CRError(88, "error scale not positive")
+            wr *= sw * sw
+            wp *= swp * swp
+    return Data(strnr=strnr, vnr=vnr, dat=dat, wmatdr=wr, wmatdp=wp, wmatd_cri=wc)
+
+
+# ---------------------------------------------------------------------------
+# misfit, polarity, first lambda, step length, roughness
+# ---------------------------------------------------------------------------
+def _phase_class(im: float) -> int:
+    """+1 / -1 when a phase lies outside (-pi/2, pi/2] (src/chkpol.f90)."""
+    if im > _PI / 2.0:
+        return -1
+    if im <= -_PI / 2.0:
+        return 1
+    return 0
+
+
+def chkpo2(dati: complex, sigi: complex, lpol: bool = False):
+    """Local polarity correction of one datum for the misfit (chkpo2 of
+    src/dmisft.f90:230-300): (cdat, csig, wdlok)."""
+    redat, imdat, resig, imsig = dati.real, dati.imag, sigi.real, sigi.imag
+    idat, isig = _phase_class(imdat), _phase_class(imsig)
+    wdlok = 1
+    if idat == 0 and isig != 0:
+        imsig = imsig + isig * _PI
+        if not lpol:
+            imdat = imdat - math.copysign(_PI, imdat)
+        wdlok = 0
+    elif idat != 0 and isig == 0:
+        if lpol:
+            imdat = imdat + idat * _PI
+        wdlok = 0
+    elif idat != 0 and isig != 0:
+        imsig = imsig + isig * _PI
+        imdat = imdat + idat * _PI
+    return complex(redat, imdat), complex(resig, imsig), wdlok
+
+
+@dataclasses.dataclass
+class Misfit:
+    nrmsd: float
+    betrms: float
+    pharms: float
+    npol: int
+
+
+def dmisft(dat, sigmaa, wmatd, wmatdr, wmatdp, lfpi: bool = False, lpol: bool = False) -> Misfit:
+    """src/dmisft.f90:60-125 (without robust reweighting or difference data)."""
+    nrmsd = betrms = pharms = 0.0
+    idum = 0
+    for i in range(len(dat)):
+        cdat, csig, wdlok = chkpo2(complex(dat[i]), complex(sigmaa[i]), lpol)
+        cdum = cdat - csig
+        psi = math.sqrt(wmatd[i]) * (abs(cdum.imag) if lfpi else abs(cdum))
+        idum += wdlok
+        nrmsd += psi * psi * wdlok
+        betrms += wmatdr[i] * wdlok * cdum.real * cdum.real
+        pharms += wmatdp[i] * wdlok * cdum.imag * cdum.imag
+    if idum == 0:
+        raise formats.CRError(99, "no datum left for the misfit")
+    return Misfit(math.sqrt(nrmsd / idum), math.sqrt(betrms / idum), math.sqrt(pharms / idum), len(dat) - idum)
+
+
+def parfit(fa: float, fb: float, fc: float, fmin: float, smin: float, step: float) -> float:
+    """src/parfit.f90: step length from the misfits at steps 0, 0.5 and 1
+    (parabola through the three, or a linear interpolation to fmin), clipped
+    to [smin, 1].  `step` is kept where no case applies."""
+    a, b, c = 0.0, 0.5, 1.0
+
+    def parabola():
+        bma, fbmfc, bmc, fbmfa = b - a, fb - fc, b - c, fb - fa
+        return b - (bma * bma * fbmfc - bmc * bmc * fbmfa) / (2.0 * (bma * fbmfc - bmc * fbmfa))
+
+    if fa > fb:
+        if fb <= fc:
+            if fb <= fmin:
+                if fa < fmin and fc > fa:
+                    step = b + (c - b) * (fmin - fb) / (fc - fb)
+                else:
+                    step = a + (b - a) * (fmin - fa) / (fb - fa)
+            else:
+                step = parabola()
+        elif fb > fc:
+            if fb <= fmin:
+                step = a + (b - a) * (fmin - fa) / (fb - fa)
+            elif fc <= fmin:
+                step = b + (c - b) * (fmin - fb) / (fc - fb)
+            else:
+                step = c
+    elif fa < fb:
+        if fb >= fc:
+            if fb >= fmin:
+                if fa > fmin and fc < fa:
+                    step = b + (c - b) * (fmin - fb) / (fc - fb)
+                else:
+                    step = a + (b - a) * (fmin - fa) / (fb - fa)
+            else:
+                step = parabola()
+        elif fb < fc:
+            if fb >= fmin:
+                step = a + (b - a) * (fmin - fa) / (fb - fa)
+            elif fc >= fmin:
+                step = b + (c - b) * (fmin - fb) / (fc - fb)
+            else:
+                step = c
+    elif fa == fb:
+        if fb > fc:
+            if fb < fmin:
+                step = parabola()
+            elif fc <= fmin:
+                step = b + (c - b) * (fmin - fb) / (fc - fb)
+            else:
+                step = c
+        elif fb < fc:
+            if fb > fmin:
+                step = parabola()
+            elif fc >= fmin:
+                step = b + (c - b) * (fmin - fb) / (fc - fb)
+            else:
+                step = c
+        elif fb == fc:
+            step = smin
+    step = max(smin, step)
+    return min(c, step)
+
+
+def roughness(par: np.ndarray, ltri: int, smatm: np.ndarray, nachbar: Optional[np.ndarray], nx: int,
+              lfpi: bool = False) -> float:
+    """Re(m^H R^T R m) of src/brough_mod.f90 (broughreg, broughtri)."""
+    manz = len(par)
+    if ltri == 0:
+        cd = smatm[0] * par
+        cd[1:] += smatm[1][:-1] * par[:-1]
+        cd[:-1] += smatm[1][:-1] * par[1:]
+        cd[nx:] += smatm[2][:-nx] * par[:-nx]
+        cd[:manz - nx] += smatm[2][:manz - nx] * par[nx:]
+    elif ltri in (1, 2):
+        nk = smatm.shape[0] - 1
+        cd = smatm[nk] * par
+        for j in range(nk):
+            nbj = nachbar[j]
+            ok = nbj != 0
+            cd[ok] += smatm[j][ok] * par[nbj[ok] - 1]
+    else:
+        raise NotImplementedError(f"roughness for ltri = {ltri}")
+    # the reference sums element by element; the order changes only rounding
+    if lfpi:
+        return float(np.sum(cd.imag * par.imag))
+    return float(np.sum((cd * np.conj(par)).real))
+
+
+# ---------------------------------------------------------------------------
+# backends: forward + bvolti, bsensi, update
+# ---------------------------------------------------------------------------
+class DeviceBackend:
+    """The heavy steps on the GPU through the C ABI (one context)."""
+
+    def __init__(self, grid, survey, kwn, kwnwi, swrtr: int, lsink: bool, nsink: int, precision: int,
+                 refinement: Optional[tuple] = None):
+        from .crmod import CRMod
+        self.m = CRMod(grid, survey, kwn, kwnwi, swrtr=swrtr, lsink=lsink, nsink=nsink, precision=precision)
+        if refinement is not None:
+            self.m.set_refinement(*refinement)
+
+    def forward(self, sigma: np.ndarray) -> np.ndarray:
+        return self.m.forward(sigma, volt_mode=1)["sigmaa"]
+
+    def sensitivities(self):
+        self.m.sens_on_device(1)
+
+    def update(self, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx, nachbar, lam, eps, ncgmax, step, par):
+        p, dp, cgfac, cgres, ncg = self.m.update(wmatd, wdfak, dat, sigmaa, ltri, smatm, nx=nx, nachbar=nachbar,
+                                                 lam=lam, eps=eps, ncgmax=ncgmax, step=step, par=par)
+        return dp, ncg
+
+    def jacobian(self) -> np.ndarray:
+        return self.m.sens(1)
+
+    def close(self):
+        self.m.close()
+
+
+def blam0(cfg: CRTomoConfig, lamnull_cri: float, lamnull_fpi: float, manz: int, nanz: int, lfpi: bool,
+          jacobian, wmatd, wdfak) -> float:
+    """src/blam0.f90: a preset lambda_0 (nz = -1: max(manz, nanz); nz < -1:
+    |nz|; crt.lamnull), else 5 mean_j |(J^H W J 1)_j| 2/(alfx + alfz) --
+    the double sum of the reference factorises into two products with J."""
+    eps = np.finfo(np.float64).eps
+    if ((cfg.llamf & 1) or lamnull_cri > eps) and not lfpi:
+        return float(max(manz, nanz)) if cfg.nz == -1 else float(lamnull_cri)
+    if (cfg.llamf & 1) or lamnull_fpi > eps:
+        return float(lamnull_fpi)
+    J = jacobian()
+    w = np.asarray(wmatd) * np.asarray(wdfak, np.float64)
+    if lfpi:
+        Jr = J.real
+        jtj = np.abs(Jr.T @ (w * (Jr @ np.ones(manz))))
+    else:
+        jtj = np.abs(np.conj(J).T @ (w * (J @ np.ones(manz))))
+    lam = float(np.sum(jtj)) / manz
+    return lam * 2.0 / (cfg.alfx + cfg.alfz) * 5.0
+
+
+# ---------------------------------------------------------------------------
+# the loop (src/inv.f90:330-990)
+# ---------------------------------------------------------------------------
+@dataclasses.dataclass
+class Row:
+    """One line of inv.ctr (src/kont2.f90): kind 'IT' (an accepted model) or
+    'UP' (a trial of the lambda or step-length search)."""
+    kind: str
+    index: int
+    nrmsd: float
+    bdpar: float = 0.0
+    lam: float = 0.0
+    rough: float = 0.0
+    ncg: int = 0
+    betrms: float = 0.0
+    pharms: float = 0.0
+    npol: int = 0
+    step: float = 0.0
+    first: bool = False
+
+
+class Inversion:
+    """CRTomo's inversion of one data set (complex stage).
+
+    grid, enr: the mesh and electrodes; data: read_data(); cfg:
+    read_crtomo_cfg().  backend: an object with forward(sigma) -> sigmaa,
+    sensitivities(), update(...) -> (dpar, ncg) and jacobian(), as
+    DeviceBackend.  sigma_start: the start model when cfg.lrho0 is off."""
+
+    # src/rall.f90:196-222 defaults
+    nrmsdm = 1.0
+    mqrms = 2e-2
+    eps = 1e-4
+    stpmin = 1e-3
+    bdmin = 1e-3
+    nlam = 30
+    fstart = 0.5
+    fstop = 0.9
+    lpol = False
+
+    def __init__(self, grid, data: Data, cfg: CRTomoConfig, backend, sigma_start=None,
+                 lamnull: Optional[tuple] = None):
+        if cfg.lrobust or cfg.ldiff or cfg.ldc:
+            raise NotImplementedError("robust, difference and DC inversion are not built")
+        if cfg.ltri not in (0, 1, 2):
+            raise NotImplementedError(f"regularisation ltri = {cfg.ltri} is not built")
+        self.grid, self.data, self.cfg, self.b = grid, data, cfg, backend
+        self.manz = grid.elanz if cfg.ltri != 0 else cfg.nx * cfg.nz
+        if self.manz != grid.elanz:
+            raise formats.CRError(50, "manz /= elanz is not implemented")
+        self.nanz = len(data.dat)
+        self.ncgmax = self.manz // 10 if cfg.ltri < 5 else self.manz  # src/rall.f90:745-746
+        # first lambda (src/rall.f90:768-796; lamnull = the crt.lamnull file)
+        if lamnull is not None:
+            self.lamnull_cri, self.lamnull_fpi = lamnull
+        elif cfg.llamf & 1:
+            self.lamnull_cri = self.lamnull_fpi = cfg.lamfix
+        elif cfg.nz == -1:
+            self.lamnull_cri, self.lamnull_fpi = float(max(self.manz, self.nanz)), 0.0
+        elif cfg.nz < 0:
+            self.lamnull_cri, self.lamnull_fpi = float(abs(cfg.nz)), 0.0
+        else:
+            self.lamnull_cri = self.lamnull_fpi = 0.0
+        # weights (src/rall.f90:805-817): the complex stage with a final phase
+        # improvement fits the magnitude error only
+        lelerr = (not cfg.lfphai and not cfg.ldc) or bool(cfg.mswitch & 32)
+        self.wmatd = (data.wmatd_cri if lelerr else data.wmatdr).copy()
+        # smoothness (src/bsmatm_mod.f90)
+        if cfg.ltri == 0:
+            self.nachbar = None
+            self.smatm = R.bsmatmreg(grid, cfg.nx, cfg.nz, cfg.alfx, cfg.alfz)
+        else:
+            self.nachbar = R.bnachbar(grid)
+            self.smatm = R.bsmatmtri(grid, self.nachbar, cfg.alfx, cfg.alfz)
+        # start model (src/bsigm0.f90)
+        if cfg.lrho0:
+            s = complex(math.cos(cfg.pha0 / 1e3) / cfg.bet0, -math.sin(cfg.pha0 / 1e3) / cfg.bet0)
+            self.sigma = np.full(grid.elanz, s, np.complex128)
+        elif sigma_start is not None:
+            self.sigma = np.array(sigma_start, np.complex128)
+        else:
+            raise NotImplementedError("start model from kfak-weighted data (lrho0 off, no start model)")
+        self.dat = data.dat.copy()
+        self.swapped = np.zeros(self.nanz, bool)
+        self.rows: List[Row] = []
+        self.status = ""
+
+    # -- pieces -----------------------------------------------------------------
+    def _forward(self, sigma):
+        sa = np.array(self.b.forward(sigma), np.complex128)
+        s = self.swapped  # polarity already changed by chkpol: -ln(-V)
+        if s.any():
+            im = sa.imag[s]
+            sa.imag[s] = np.where(im < 0, im + _PI, im - _PI)
+        return sa
+
+    def _chkpol(self, lsetup: bool):
+        """src/chkpol.f90 with lpol off: change the polarity of the model
+        datum (the potential electrodes swap) and exclude the datum."""
+        wdfak = np.ones(self.nanz, np.int32)
+        for i in range(self.nanz):
+            redat, imdat = self.dat[i].real, self.dat[i].imag
+            resig, imsig = self.sigmaa[i].real, self.sigmaa[i].imag
+            idat, isig = _phase_class(imdat), _phase_class(imsig)
+            if idat == 0 and isig != 0:
+                self.swapped[i] = ~self.swapped[i]
+                self.sigmaa[i] = complex(resig, imsig + isig * _PI)
+                self.dat[i] = complex(redat, imdat - math.copysign(_PI, imdat))
+                wdfak[i] = 0
+            elif idat != 0 and isig == 0:
+                wdfak[i] = 0
+            elif idat != 0 and isig != 0:
+                self.swapped[i] = ~self.swapped[i]
+                self.sigmaa[i] = complex(resig, imsig + isig * _PI)
+                self.dat[i] = complex(redat, imdat + idat * _PI)
+        self.wdfak = wdfak
+
+    def _misfit(self):
+        m = dmisft(self.dat, self.sigmaa, self.wmatd, self.data.wmatdr, self.data.wmatdp, self.lfpi, self.lpol)
+        self.nrmsd, self.betrms, self.pharms, self.npol = m.nrmsd, m.betrms, m.pharms, m.npol
+
+    def _kont2(self, lsetup: bool):
+        if lsetup:
+            self.rows.append(Row("IT", self.it, self.nrmsd, betrms=self.betrms, pharms=self.pharms,
+                                 npol=self.npol, first=True))
+        elif self.llam and not self.lstep:
+            self.rows.append(Row("IT", self.it, self.nrmsd, self.bdpar, self.lam, self.rough, self.ncg,
+                                 self.betrms, self.pharms, self.npol, self.step))
+        else:
+            self.rows.append(Row("UP", self.itr, self.nrmsd, self.bdpar, self.lam, self.rough, self.ncg,
+                                 step=self.step))
+
+    # -- the loop ---------------------------------------------------------------
+    def run(self, max_iterations: Optional[int] = None) -> List[Row]:
+        """Runs until a stopping rule of src/inv.f90:560-640 holds; the rule
+        is in self.status ('79' iteration limit, '80' target misfit, '81' no
+        misfit decrease, '92' minimal step twice, '109' minimal model change,
+        'fpi' where the final phase improvement would start).  With
+        max_iterations the run also ends ('max_iterations') once that many
+        models have been accepted."""
+        cfg, b = self.cfg, self.b
+        it = itr = 0
+        rmsalt = 0.0
+        lamalt = 1.0
+        self.bdpar = bdalt = 1.0
+        self.lsetup, self.lsetip, self.lfpi = True, False, False
+        self.llam, ldlami, self.lstep, lfstep = False, True, False, False
+        self.step, stpalt, alam = 1.0, 1.0, 0.0
+        self.lam, dlam, dlalt, rmsreg, ldlamf = 0.0, 1.0, 1.0, 0.0, False
+        self.rough, self.ncg = 0.0, 0
+        dpar = np.zeros(self.manz, np.complex128)
+        dpar2 = dpar.copy()
+        ncg2 = 0
+        sigma2 = self.sigma.copy()
+        sgmaa2 = None
+        self.wdfak = np.ones(self.nanz, np.int32)
+        while True:
+            self.it, self.itr = it, itr
+            # modelling (src/inv.f90:342-503)
+            try:
+                self.sigmaa = self._forward(self.sigma)
+            except Exception:
+                if sgmaa2 is None:
+                    raise
+                self.sigma, self.sigmaa = sigma2, sgmaa2
+                self.status = "forward"
+                break
+            setup = self.lsetup or self.lsetip
+            if setup:
+                self._chkpol(setup)
+            self._misfit()
+            if self.nrmsd < 1e-12:
+                self.nrmsd = self.nrmsdm * (1.0 - self.mqrms)
+            self._kont2(setup)
+            # stopping rules (src/inv.f90:560-640)
+            if self.llam and not self.lstep:
+                self._chkpol(setup)
+                err2 = 0
+                if stpalt == 0.0:
+                    err2 = 92
+                if abs(1.0 - rmsalt / self.nrmsd) <= self.mqrms:
+                    err2 = 81
+                if abs(1.0 - self.nrmsd / self.nrmsdm) <= self.mqrms and ldlamf:
+                    err2 = 80
+                if it >= cfg.itmax:
+                    err2 = 79
+                if abs(1.0 - self.bdpar / bdalt) < self.bdmin:
+                    err2 = 109
+                if err2 != 0:
+                    self.status = "fpi" if (cfg.lfphai and err2 != 79) else str(err2)
+                    break
+                lamalt = self.lam
+                if max_iterations is not None and it >= max_iterations:
+                    self.status = "max_iterations"
+                    break
+            if (self.llam and not self.lstep) or setup:
+                it += 1
+                itr = 0
+                rmsreg, dlam, dlalt, ldlamf = 0.0, 1.0, 1.0, False
+                self.bdpar = bdalt = 1.0
+                rmsalt = self.nrmsd
+                if it > 1:
+                    lamalt = self.lam
+                sigma2, sgmaa2 = self.sigma.copy(), self.sigmaa.copy()
+                b.sensitivities()
+            else:
+                self.sigma, self.sigmaa = sigma2.copy(), sgmaa2.copy()
+            self.it, self.itr = it, itr
+            if cfg.itmax == 0:
+                self.status = "109"
+                break
+            # regularisation and step length (src/inv.f90:768-905)
+            if cfg.llamf & 1:
+                self.lam = cfg.lamfix
+                if (cfg.llamf & 2) and it > 1:
+                    self.lam = cfg.lamfix / (2.0 * (it - 1))
+                self.llam = False
+                if self.lsetup or self.lsetip:
+                    self.lsetup = self.lsetip = False
+            elif not self.lstep:
+                if self.llam:
+                    self.llam = False
+                    self.step = 1.0
+                else:
+                    itr += 1
+                    self.itr = itr
+                    nr = self.nrmsd
+                    search = ((((nr < rmsreg and itr <= self.nlam) or (dlam > 1.0 and itr <= self.nlam))
+                               and (not ldlamf or dlalt <= 1.0)
+                               and abs(1.0 - self.bdpar / bdalt) > self.bdmin
+                               and abs(1.0 - rmsreg / self.nrmsdm) > self.mqrms)
+                              or rmsreg == 0.0)
+                    if search:
+                        if self.lsetup or self.lsetip:
+                            self.lam = blam0(cfg, self.lamnull_cri, self.lamnull_fpi, self.manz, self.nanz,
+                                             self.lfpi, b.jacobian, self.wmatd, self.wdfak)
+                            lamalt = self.lam
+                        else:
+                            dlalt = dlam
+                            lr = math.log(nr / self.nrmsdm)
+                            if ldlami:
+                                ldlami = False
+                                alam = max(abs(lr), math.log(1.0 + self.mqrms))
+                                dlam = self.fstart
+                            else:
+                                alam = max(alam, abs(lr))
+                                dlam = (math.log(self.fstop) * math.copysign(1.0, lr)
+                                        + math.log(self.fstart / self.fstop) * lr / alam)
+                                dlam = math.exp(dlam)
+                            self.lam *= dlam
+                            if dlalt > 1.0 and dlam < 1.0:
+                                ldlamf = True
+                    else:
+                        self.llam = True
+                        self.lam /= dlam
+                        if lfstep:
+                            lfstep = False
+                        else:
+                            self.lstep = True
+                            self.step = 0.5
+                    if self.lsetup or self.lsetip:
+                        self.lsetup = self.lsetip = False
+                    elif not self.lstep:
+                        rmsreg = self.nrmsd
+            else:
+                self.lstep = False
+                self.step = parfit(rmsalt, self.nrmsd, rmsreg, self.nrmsdm, self.stpmin, self.step)
+                if self.step == self.stpmin and stpalt == self.stpmin:
+                    stpalt = 0.0
+                else:
+                    stpalt = self.step
+            # update (src/bpar.f90, src/update.f90, src/bsigma.f90, src/brough_mod.f90)
+            par = np.log(self.sigma)
+            bdalt = self.bdpar
+            if not self.llam:
+                dpar2, ncg2 = dpar, self.ncg
+                dpar, self.ncg = b.update(self.wmatd, self.wdfak, self.dat, self.sigmaa, cfg.ltri, self.smatm,
+                                          cfg.nx, self.nachbar, self.lam, self.eps, self.ncgmax, 1.0, par)
+                dpar = np.array(dpar, np.complex128)
+            else:
+                dpar, self.ncg = dpar2, ncg2
+            par = par + self.step * dpar
+            self.bdpar = float(np.sum((dpar * np.conj(dpar)).real)) * self.step
+            self.sigma = np.exp(par)
+            self.rough = roughness(par, cfg.ltri, self.smatm, self.nachbar, cfg.nx, self.lfpi)
+            if cfg.llamf & 1:
+                self.llam = True
+        self.it, self.itr = it, itr
+        return self.rows
+
+
+def format_rows(rows: List[Row]) -> str:
+    """The IT/UP lines in the columns of src/kont2.f90 (formats 101, 105,
+    111); the numbers in Python's g notation, not Fortran's G edit."""
+    out = []
+    for r in rows:
+        if r.first:
+            out.append(f"{r.kind:>3s}{r.index:4d}   {r.nrmsd:10.4g}{'':48s}{r.betrms:10.4g}  {r.pharms:10.4g}  {r.npol:4d}")
+        elif r.kind == "IT":
+            out.append(f"{r.kind:>3s}{r.index:4d}   {r.nrmsd:10.4g}  {r.bdpar:10.4g} {r.lam:10.4g}  {r.rough:10.4g}  "
+                       f"{r.ncg:6d}     {r.betrms:10.4g}  {r.pharms:10.4g}  {r.npol:4d}        {r.step:5.3f}")
+        else:
+            out.append(f"{r.kind:>3s}{r.index:4d}   {r.nrmsd:10.4g}  {r.bdpar:9.3g}  {r.lam:10.4g}  {r.rough:10.4g}  "
+                       f"{r.ncg:6d}{'':46s}{r.step:5.3f}")
+    return "\n".join(out) + "\n"
+
+
+def run_crtomo(exe_dir: str, precision: int = 1, refinement=(8, 1e-10), write: bool = True):
+    """CRTomo's complex stage on a tomodir: reads exe_dir/crtomo.cfg and its
+    inputs, inverts on the GPU and (write) puts the IT/UP lines into
+    <ramd>/inv.ctr and the final model into <ramd>/rho.dat (magnitude in
+    ohm m and phase in mrad, as src/rsigma.f90 reads a model).  Returns the
+    Inversion."""
+    cfg = read_crtomo_cfg(os.path.join(exe_dir, "crtomo.cfg"))
+
+    def p(x):
+        return os.path.normpath(os.path.join(exe_dir, x))
+
+    grid = formats.read_elem(p(cfg.delem))
+    enr = formats.read_elec(p(cfg.delectr), grid.sanz)
+    data = read_data(p(cfg.dstrom), cfg, len(enr))
+    survey = formats.Survey(enr=enr, strnr=data.strnr, vnr=data.vnr, strom=np.ones(len(data.strnr)))
+    if cfg.swrtr:
+        from .crmod import rwaven
+        kwn, kwnwi = rwaven(grid, survey)
+    else:  # src/rall.f90:818-838
+        if 11 in set(np.asarray(grid.typ).tolist()):
+            raise formats.CRError(110, "2D with mixed boundaries")
+        kwn = np.array([0.0 if cfg.lrandb2 else 1e-6])
+        kwnwi = np.zeros(1)
+    sigma_start = None
+    if not cfg.lrho0 and cfg.dm0:
+        sigma_start = formats.read_rho(p(cfg.dm0), grid.elanz)
+    b = DeviceBackend(grid, survey, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink, precision, refinement)
+    try:
+        if cfg.lrandb2:
+            b.m.set_boundary_values(*formats.read_boundary_values(p(cfg.drandb), grid.sanz))
+        inv = Inversion(grid, data, cfg, b, sigma_start=sigma_start)
+        inv.run()
+    finally:
+        b.close()
+    if write:
+        ramd = p(cfg.ramd)
+        os.makedirs(ramd, exist_ok=True)
+        with open(os.path.join(ramd, "inv.ctr"), "w") as fh:
+            fh.write(format_rows(inv.rows))
+        mag = 1.0 / np.abs(inv.sigma)
+        pha = -1e3 * np.angle(inv.sigma)  # resistivity phase in mrad
+        formats.write_rho(os.path.join(ramd, "rho.dat"), mag, pha)
+    return inv
