@@ -201,6 +201,15 @@ int crgpu_update(crgpu_ctx *ctx, const double *wmatd, const int32_t *wdfak, cons
                  const int32_t *nachbar, double lam, double eps, int32_t ncgmax, double step,
                  double *par, double *dpar, double *cgfac, float *cgres, int32_t *ncg);
 
+/* The same update in the final phase improvement (lfpi of src/update.f90 and
+ * src/cg_mod.f90): preconditioner and right-hand side from Re(J), the real
+ * CG of cjggdc (src/cg_mod.f90:136-400) on the imaginary part of the
+ * right-hand side, and the update i cgfac o dpar in the phases only. */
+int crgpu_update_fpi(crgpu_ctx *ctx, const double *wmatd, const int32_t *wdfak, const double *dat,
+                     const double *sigmaa, int32_t ltri, const double *smatm, int32_t nx,
+                     const int32_t *nachbar, double lam, double eps, int32_t ncgmax, double step,
+                     double *par, double *dpar, double *cgfac, float *cgres, int32_t *ncg);
+
 /* ------------------------------------------------------------------ */
 /* host-side set-up routines                                            */
 /* ------------------------------------------------------------------ */

@@ -754,9 +754,7 @@ static int setup_ctx(const or_mesh *m, const or_opts *o, int kwnanz, const doubl
     double s0[2];
     or_refsig(m, sigma, s0);
     c->sigma0 = cmk(s0[0], s0[1]);
-    int lsr = o->lsr, lana = o->lana;
-    if (o->swrtr == 0) { lsr = 0; lana = 0; }
-    if (lsr) lana = 0;
+    int lsr = o->swrtr == 0 ? 0 : o->lsr;  /* lana is decided by the callers */
     if (!*lbeta) lsr = 0; /* src/fem.f90:311 */
     c->lsr = lsr;
     c->lsink = o->lsink;
@@ -1351,6 +1349,93 @@ static void rmul_tri(int manz, int maxnk, const int *nachbar, const double *smat
         if (w) out[i - 1] = cadd(cdum, cscale(cmul(v[i - 1], cmk(sd, 0.0)), w[i - 1]));
         else out[i - 1] = cadd(cdum, cmul(cmk(sd, 0.0), v[i - 1]));
     }
+}
+
+/* src/update.f90 with lfpi and cjggdc (src/cg_mod.f90:136-260, bapdc, bpdc,
+ * bpdctri, bbdc): Re(J) in the preconditioner, the right-hand side and the
+ * products; the real CG runs on Im(bvec); the update goes into the phases. */
+static int update_fpi(int nanz, int manz, const cx *sens, const double *wmatd, const int *wdfak,
+                      const cx *dat, const cx *sigmaa, int ltri, const double *smatm, int nx,
+                      const int *nachbar, int maxnk, double lam, double eps, int ncgmax, double step,
+                      cx *par, cx *dpar, double *cgfac, float *cgres) {
+    cx *bvec = (cx *)calloc((size_t)manz, sizeof(cx));
+    cx *tmp = (cx *)calloc((size_t)manz, sizeof(cx));
+    double *bdc = (double *)calloc((size_t)manz, sizeof(double));
+    double *rdc = (double *)calloc((size_t)manz, sizeof(double));
+    double *pdc = (double *)calloc((size_t)manz, sizeof(double));
+    double *dp = (double *)calloc((size_t)manz, sizeof(double));
+    double *apdc = (double *)calloc((size_t)nanz, sizeof(double));
+#define RS(i, j) sens[(size_t)(j) * nanz + (i)].re
+    if (ltri == 0) rmul_reg(manz, nx, smatm, par, NULL, bvec);
+    else rmul_tri(manz, maxnk, nachbar, smatm, par, NULL, bvec);
+    for (int j = 0; j < manz; j++) {
+        double dum = 0.0;
+        for (int i = 0; i < nanz; i++) dum += RS(i, j) * RS(i, j) * wmatd[i] * (double)wdfak[i];
+        dum += lam * (ltri == 0 ? smatm[j] : smatm[(size_t)maxnk * manz + j]);
+        cgfac[j] = 1.0 / sqrt(dum);
+    }
+    for (int j = 0; j < manz; j++) {
+        cx cdum = cmk(0, 0);
+        for (int i = 0; i < nanz; i++)
+            cdum = cadd(cdum, cmul(cmk(RS(i, j) * wmatd[i] * (double)wdfak[i], 0.0), csub(dat[i], sigmaa[i])));
+        bvec[j] = cmul(csub(cdum, cmul(cmk(lam, 0.0), bvec[j])), cmk(cgfac[j], 0.0));
+        bdc[j] = bvec[j].im;
+        rdc[j] = bdc[j];
+    }
+    double dr = 0, dr0 = 0, dr1 = 0, beta = 0, alpha;
+    int ncg = ncgmax, k;
+    for (k = 1; k <= ncgmax; k++) {
+        ncg = k - 1;
+        dr = 0.0;
+        for (int j = 0; j < manz; j++) dr += rdc[j] * rdc[j];
+        if (k == 1) {
+            dr0 = dr * eps;
+            beta = 0.0;
+        } else {
+            beta = dr / dr1;
+        }
+        if (dr <= dr0) break;
+        for (int j = 0; j < manz; j++) pdc[j] = rdc[j] + beta * pdc[j];
+        for (int i = 0; i < nanz; i++) {
+            double a = 0.0;
+            for (int j = 0; j < manz; j++) a += pdc[j] * RS(i, j) * cgfac[j];
+            apdc[i] = a;
+        }
+        for (int j = 0; j < manz; j++) tmp[j] = cmk(pdc[j], 0.0);
+        if (ltri == 0) rmul_reg(manz, nx, smatm, tmp, cgfac, bvec);
+        else rmul_tri(manz, maxnk, nachbar, smatm, tmp, cgfac, bvec);
+        for (int j = 0; j < manz; j++) {
+            double dum = 0.0;
+            for (int i = 0; i < nanz; i++) dum += RS(i, j) * wmatd[i] * (double)wdfak[i] * apdc[i];
+            bdc[j] = (dum + lam * bvec[j].re) * cgfac[j];
+        }
+        dr1 = 0.0;
+        for (int j = 0; j < manz; j++) dr1 += pdc[j] * bdc[j];
+        alpha = dr / dr1;
+        for (int j = 0; j < manz; j++) {
+            dp[j] += alpha * pdc[j];
+            rdc[j] -= alpha * bdc[j];
+        }
+        dr1 = dr;
+        cgres[k] = (float)(eps * dr / dr0);
+    }
+    if (k > ncgmax) ncg = ncgmax;
+    cgres[0] = (float)ncg;
+    for (int j = 0; j < manz; j++) {
+        dpar[j] = cmk(0.0, dp[j] * cgfac[j]);
+        par[j] = cadd(par[j], cmul(cmk(step, 0.0), dpar[j]));
+    }
+#undef RS
+    free(bvec); free(tmp); free(bdc); free(rdc); free(pdc); free(dp); free(apdc);
+    return ncg;
+}
+
+int or_update_fpi(int nanz, int manz, const double *sens, const double *wmatd, const int *wdfak,
+                  const double *dat, const double *sigmaa, int ltri, const double *smatm, int nx,
+                  const int *nachbar, int maxnk, double lam, double eps, int ncgmax, double step,
+                  double *par, double *dpar, double *cgfac, float *cgres) {
+    return update_fpi(nanz, manz, (const cx *)sens, wmatd, wdfak, (const cx *)dat, (const cx *)sigmaa, ltri,
+                      smatm, nx, nachbar, maxnk, lam, eps, ncgmax, step, (cx *)par, (cx *)dpar, cgfac, cgres);
 }
 
 int or_update(int nanz, int manz, const double *sens_, const double *wmatd, const int *wdfak,

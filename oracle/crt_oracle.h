@@ -155,6 +155,13 @@ int or_update(int nanz, int manz, const double *sens, const double *wmatd,
               int maxnk, double lam, double eps, int ncgmax, double step,
               double *par, double *dpar, double *cgfac, float *cgres);
 
+/* the same in the final phase improvement (lfpi; cjggdc on Re(J)) */
+int or_update_fpi(int nanz, int manz, const double *sens, const double *wmatd,
+                  const int *wdfak, const double *dat, const double *sigmaa,
+                  int ltri, const double *smatm, int nx, const int *nachbar,
+                  int maxnk, double lam, double eps, int ncgmax, double step,
+                  double *par, double *dpar, double *cgfac, float *cgres);
+
 #ifdef __cplusplus
 }
 #endif

@@ -301,9 +301,10 @@ def cutmck(grid, enr):
 
 
 def update(sens, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx=0, nachbar=None, maxnk=4, lam=1.0,
-           eps=1e-4, ncgmax=100, step=1.0, par=None):
-    """src/update.f90 + cjggra; sens (nanz, manz) complex.  Returns
-    (par_new, dpar, cgfac, cgres, ncg)."""
+           eps=1e-4, ncgmax=100, step=1.0, par=None, phase_only=False):
+    """src/update.f90 + cjggra (phase_only: the final phase improvement with
+    cjggdc); sens (nanz, manz) complex.  Returns (par_new, dpar, cgfac,
+    cgres, ncg)."""
     nanz, manz = sens.shape
     s = np.ascontiguousarray(np.asarray(sens, np.complex128).T)  # column-major
     par = np.zeros(manz, np.complex128) if par is None else np.array(par, np.complex128)
@@ -316,7 +317,8 @@ def update(sens, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx=0, nachbar=None, max
     sa = np.ascontiguousarray(sigmaa, np.complex128)
     sm = np.ascontiguousarray(smatm, np.float64)
     nb = np.ascontiguousarray(nachbar if nachbar is not None else np.zeros(1), np.int32)
-    ncg = lib().or_update(nanz, manz, _p(s, f64p), _p(wm, f64p), _p(wd, i32p), _p(d, f64p),
+    fn = lib().or_update_fpi if phase_only else lib().or_update
+    ncg = fn(nanz, manz, _p(s, f64p), _p(wm, f64p), _p(wd, i32p), _p(d, f64p),
                           _p(sa, f64p), ltri, _p(sm, f64p), nx, _p(nb, i32p), maxnk,
                           C.c_double(lam), C.c_double(eps), ncgmax, C.c_double(step),
                           _p(par, f64p), _p(dpar, f64p), _p(cgfac, f64p),

@@ -3,9 +3,10 @@ src/dmisft.f90, src/blam0.f90, src/parfit.f90, src/brough_mod.f90) on the
 oracle's forward, Jacobian and update, against the reference's own control
 output inv.ctr (src/kont2.f90).
 
-minimal: the whole complex stage -- 21 lines over two accepted models, with
-the lambda search, a failed trial, the half step and the parabolic step fit,
-ending where the reference switches to the final phase improvement.
+minimal: the whole run -- 21 lines of the complex stage over two accepted
+models (the lambda search, a failed trial, the half step and the parabolic
+step fit), then the final phase improvement with its restart from the
+homogeneous phase, lambda_0 from Re(J) and the phase-only CG (4 lines).
 mixed_surf: lambda_0 from the Jacobian (src/blam0.f90), complex error
 ellipses, phase data; the first iteration (15 lines).  Its UP 12 (lambda 77,
 a CG stopped by its residual test after 54 of 96 steps) differs by 4% in
@@ -29,10 +30,12 @@ def _run(case, max_iterations=None):
 def test_inversion_loop_reproduces_reference_trace_minimal():
     inv, rows = _run("minimal")
     gold = golden_rows("minimal")
-    assert len(gold) == 21 and len(rows) == 21
+    assert len(gold) == 25 and len(rows) == 25
     compare_rows(gold, rows, inv.ncgmax)
     assert [r.ncg for r in rows] == [g[6] or 0 for g in gold]
-    assert inv.status == "fpi"  # lfphai: the reference resets the phase model here
+    # the final phase improvement starts at line 21 (lffhom: phases reset);
+    # with phase data of 0 its misfit is the floor 0.98 and it stops at once
+    assert inv.stage_start == 21 and inv.status == "81"
 
 
 def test_inversion_loop_reproduces_reference_trace_mixed_surf():

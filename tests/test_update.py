@@ -58,9 +58,13 @@ def _update_case(m, s, seed=11):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("ltri,lam,tol", [(0, 300.0, 1e-8), (1, 300.0, 1e-8), (0, 3000.0, 1e-8),
-                                          (1, 3000.0, 1e-8), (0, 30.0, 2e-5)])
-def test_update_matches_oracle(gpu_lib, grid1, ltri, lam, tol):
+@pytest.mark.parametrize("ltri,lam,tol,phase_only", [(0, 300.0, 1e-8, False), (1, 300.0, 1e-8, False),
+                                                     (0, 3000.0, 1e-8, False), (1, 3000.0, 1e-8, False),
+                                                     (0, 30.0, 2e-5, False), (0, 300.0, 1e-8, True),
+                                                     (1, 300.0, 1e-8, True), (1, 3000.0, 1e-8, True)])
+def test_update_matches_oracle(gpu_lib, grid1, ltri, lam, tol, phase_only):
+    """phase_only: the final phase improvement (crgpu_update_fpi against the
+    oracle's restatement of cjggdc); the update is purely imaginary."""
     from titatest_gb300 import PLAIN, CRMod
     s = grid1
     manz = s.grid.elanz
@@ -73,9 +77,12 @@ def test_update_matches_oracle(gpu_lib, grid1, ltri, lam, tol):
             nb = R.bnachbar(s.grid)
             sm = R.bsmatmtri(s.grid, nb)
         kw = dict(lam=lam, eps=1e-4, ncgmax=manz // 10, step=1.0)
-        pg, dg, cg, rg, ng = m.update(wmatd, wdfak, dat, sa, ltri, sm, nx=s.nx, nachbar=nb, par=par, **kw)
+        pg, dg, cg, rg, ng = m.update(wmatd, wdfak, dat, sa, ltri, sm, nx=s.nx, nachbar=nb, par=par,
+                                      phase_only=phase_only, **kw)
     po, do, co, ro, no = O.update(J, wmatd, wdfak, dat, sa, ltri, sm, nx=s.nx, nachbar=nb,
-                                  maxnk=s.grid.maxnk, par=par, **kw)
+                                  maxnk=s.grid.maxnk, par=par, phase_only=phase_only, **kw)
+    if phase_only:
+        assert np.all(dg.real == 0) and np.all(do.real == 0) and np.abs(do.imag).max() > 0
     assert ng == no
     assert relerr(cg, co) < 1e-12
     assert relerr(dg, do) < tol

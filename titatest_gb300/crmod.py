@@ -271,8 +271,9 @@ class CRMod:
 
     # -- inversion update ---------------------------------------------------
     def update(self, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx=0, nachbar=None, lam=1.0, eps=1e-4,
-               ncgmax=100, step=1.0, par=None):
-        """src/update.f90 + cjggra on the sensitivities of the last sens(1)."""
+               ncgmax=100, step=1.0, par=None, phase_only: bool = False):
+        """src/update.f90 + cjggra on the sensitivities of the last sens(1);
+        phase_only: the final phase improvement (crgpu_update_fpi, cjggdc)."""
         sv, g = self.survey, self.grid
         manz = g.elanz
         par = np.zeros(manz, np.complex128) if par is None else np.array(par, np.complex128)
@@ -281,7 +282,8 @@ class CRMod:
         cgres = np.zeros(ncgmax + 2, np.float32)
         ncg = C.c_int32(0)
         nb = np.ascontiguousarray(nachbar if nachbar is not None else np.zeros(1), np.int32)
-        code = lib().crgpu_update(
+        fn = lib().crgpu_update_fpi if phase_only else lib().crgpu_update
+        code = fn(
             self._h, ptr(np.ascontiguousarray(wmatd, np.float64), f64p),
             ptr(np.ascontiguousarray(wdfak, np.int32), i32p),
             ptr(np.ascontiguousarray(dat, np.complex128), f64p),

@@ -1247,10 +1247,10 @@ int crgpu_get_stats(const crgpu_ctx *c, crgpu_stats *s) {
     return 0;
 }
 
-int crgpu_update(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, const double *dat, const double *sigmaa,
-                 int32_t ltri, const double *smatm, int32_t nx, const int32_t *nachbar, double lam, double eps,
-                 int32_t ncgmax, double step, double *par, double *dpar, double *cgfac, float *cgres,
-                 int32_t *ncg) {
+static int update_common(crgpu_ctx *c, int phase_only, const double *wmatd, const int32_t *wdfak,
+                         const double *dat, const double *sigmaa, int32_t ltri, const double *smatm, int32_t nx,
+                         const int32_t *nachbar, double lam, double eps, int32_t ncgmax, double step, double *par,
+                         double *dpar, double *cgfac, float *cgres, int32_t *ncg) {
     if (!c || !wmatd || !wdfak || !dat || !sigmaa || !smatm || !par || !dpar || !cgfac || !cgres || !ncg ||
         ncgmax < 1)
         return ERR_ARG;
@@ -1316,6 +1316,7 @@ int crgpu_update(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, const 
     a.dpar = (double2 *)(base + o_dpar);
     a.cgfac = (double *)(base + o_cg);
     a.work = (double2 *)(base + o_work);
+    a.phase_only = phase_only;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -1335,6 +1336,22 @@ int crgpu_update(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, const 
     cudaEventDestroy(e1);
     *ncg = n_cg;
     return 0;
+}
+
+int crgpu_update(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, const double *dat, const double *sigmaa,
+                 int32_t ltri, const double *smatm, int32_t nx, const int32_t *nachbar, double lam, double eps,
+                 int32_t ncgmax, double step, double *par, double *dpar, double *cgfac, float *cgres,
+                 int32_t *ncg) {
+    return update_common(c, 0, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx, nachbar, lam, eps, ncgmax, step, par,
+                         dpar, cgfac, cgres, ncg);
+}
+
+int crgpu_update_fpi(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, const double *dat,
+                     const double *sigmaa, int32_t ltri, const double *smatm, int32_t nx, const int32_t *nachbar,
+                     double lam, double eps, int32_t ncgmax, double step, double *par, double *dpar, double *cgfac,
+                     float *cgres, int32_t *ncg) {
+    return update_common(c, 1, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx, nachbar, lam, eps, ncgmax, step, par,
+                         dpar, cgfac, cgres, ncg);
 }
 
 }  // extern "C"

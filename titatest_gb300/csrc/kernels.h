@@ -94,6 +94,7 @@ struct CGArgs {
     double2 *par, *dpar;    // in/out model, out update
     double *cgfac;          // out preconditioner
     double2 *work;          // update_work_bytes(nanz, manz)
+    int phase_only;         // final phase improvement (lfpi): Re(J), real CG on the phases
 };
 size_t update_work_bytes(int nanz, int manz);
 // runs update + cjggra; cgres (host, ncgmax+2 floats) receives the CG record

@@ -10,15 +10,15 @@ the Gauss-Newton update of src/update.f90 + src/cg_mod.f90.  DeviceBackend
 runs them through the C ABI (crgpu_forward, crgpu_sens, crgpu_update); the
 controller holds only O(nanz + manz) vectors.
 
-Covered: the complex inversion stage (CRI) with the error model of
-src/rdati.f90 (or individual errors), homogeneous or file start models
-(src/bsigm0.f90), structured (ltri 0) and triangular (ltri 1, 2)
-smoothness, a fixed lambda (llamf), the polarity checks (src/chkpol.f90,
-chkpo2 of src/dmisft.f90) and the stopping rules of src/inv.f90:560-640.
-The final phase improvement (lfphai, a real-valued phase-only CG) is not
-built: the run ends where the reference would switch to it, with
-status "fpi".  Robust inversion, difference inversion, prior models, data
-noise and DC inversion (ldc) raise NotImplementedError.
+Covered: the complex inversion stage (CRI) and the final phase improvement
+(lfphai: phase weights, a new lambda_0 from Re(J), the phase-only update of
+crgpu_update_fpi, the optional restart from the homogeneous phase, lffhom)
+with the error model of src/rdati.f90 (or individual errors), homogeneous or
+file start models (src/bsigm0.f90), structured (ltri 0) and triangular
+(ltri 1, 2) smoothness, a fixed lambda (llamf), the polarity checks
+(src/chkpol.f90, chkpo2 of src/dmisft.f90) and the stopping rules of
+src/inv.f90:560-640.  Robust inversion, difference inversion, prior models,
+data noise and DC inversion (ldc) raise NotImplementedError.
 """
 from __future__ import annotations
 
@@ -33,6 +33,13 @@ from . import formats
 from . import regularization as R
 
 _PI = math.acos(-1.0)
+
+
+def _q(a: float, b: float) -> float:
+    """a / b with IEEE semantics (0/0 is NaN and compares false, as in the
+    reference's tests on bdpar/bdalt when an update is zero)."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return float(np.float64(a) / np.float64(b))
 
 
 # ---------------------------------------------------------------------------
@@ -429,9 +436,11 @@ class DeviceBackend:
     def sensitivities(self):
         self.m.sens_on_device(1)
 
-    def update(self, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx, nachbar, lam, eps, ncgmax, step, par):
+    def update(self, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx, nachbar, lam, eps, ncgmax, step, par,
+               phase_only=False):
         p, dp, cgfac, cgres, ncg = self.m.update(wmatd, wdfak, dat, sigmaa, ltri, smatm, nx=nx, nachbar=nachbar,
-                                                 lam=lam, eps=eps, ncgmax=ncgmax, step=step, par=par)
+                                                 lam=lam, eps=eps, ncgmax=ncgmax, step=step, par=par,
+                                                 phase_only=phase_only)
         return dp, ncg
 
     def jacobian(self) -> np.ndarray:
@@ -468,7 +477,8 @@ def blam0(cfg: CRTomoConfig, lamnull_cri: float, lamnull_fpi: float, manz: int, 
 @dataclasses.dataclass
 class Row:
     """One line of inv.ctr (src/kont2.f90): kind 'IT' (an accepted model) or
-    'UP' (a trial of the lambda or step-length search)."""
+    'UP' (a trial of the lambda or step-length search); 'PIT' and 'PUP' in
+    the final phase improvement."""
     kind: str
     index: int
     nrmsd: float
@@ -503,7 +513,7 @@ class Inversion:
     lpol = False
 
     def __init__(self, grid, data: Data, cfg: CRTomoConfig, backend, sigma_start=None,
-                 lamnull: Optional[tuple] = None):
+                 lamnull: Optional[tuple] = None, phase_stage: bool = True):
         if cfg.lrobust or cfg.ldiff or cfg.ldc:
             raise NotImplementedError("robust, difference and DC inversion are not built")
         if cfg.ltri not in (0, 1, 2):
@@ -548,6 +558,8 @@ class Inversion:
         self.swapped = np.zeros(self.nanz, bool)
         self.rows: List[Row] = []
         self.status = ""
+        self.phase_stage = phase_stage  # run the final phase improvement (lfphai)
+        self.stage_start = None         # first row of the phase stage
 
     # -- pieces -----------------------------------------------------------------
     def _forward(self, sigma):
@@ -584,22 +596,24 @@ class Inversion:
         self.nrmsd, self.betrms, self.pharms, self.npol = m.nrmsd, m.betrms, m.pharms, m.npol
 
     def _kont2(self, lsetup: bool):
+        p = "P" if self.lfpi else ""
         if lsetup:
-            self.rows.append(Row("IT", self.it, self.nrmsd, betrms=self.betrms, pharms=self.pharms,
+            self.rows.append(Row(p + "IT", self.it, self.nrmsd, betrms=self.betrms, pharms=self.pharms,
                                  npol=self.npol, first=True))
         elif self.llam and not self.lstep:
-            self.rows.append(Row("IT", self.it, self.nrmsd, self.bdpar, self.lam, self.rough, self.ncg,
+            self.rows.append(Row(p + "IT", self.it, self.nrmsd, self.bdpar, self.lam, self.rough, self.ncg,
                                  self.betrms, self.pharms, self.npol, self.step))
         else:
-            self.rows.append(Row("UP", self.itr, self.nrmsd, self.bdpar, self.lam, self.rough, self.ncg,
+            self.rows.append(Row(p + "UP", self.itr, self.nrmsd, self.bdpar, self.lam, self.rough, self.ncg,
                                  step=self.step))
 
     # -- the loop ---------------------------------------------------------------
     def run(self, max_iterations: Optional[int] = None) -> List[Row]:
         """Runs until a stopping rule of src/inv.f90:560-640 holds; the rule
         is in self.status ('79' iteration limit, '80' target misfit, '81' no
-        misfit decrease, '92' minimal step twice, '109' minimal model change,
-        'fpi' where the final phase improvement would start).  With
+        misfit decrease, '92' minimal step twice, '109' minimal model change;
+        'fpi' where the final phase improvement starts, when the Inversion
+        was made with phase_stage=False).  With
         max_iterations the run also ends ('max_iterations') once that many
         models have been accepted."""
         cfg, b = self.cfg, self.b
@@ -618,6 +632,7 @@ class Inversion:
         sigma2 = self.sigma.copy()
         sgmaa2 = None
         self.wdfak = np.ones(self.nanz, np.int32)
+        lfphai = cfg.lfphai
         while True:
             self.it, self.itr = it, itr
             # modelling (src/inv.f90:342-503)
@@ -642,18 +657,38 @@ class Inversion:
                 err2 = 0
                 if stpalt == 0.0:
                     err2 = 92
-                if abs(1.0 - rmsalt / self.nrmsd) <= self.mqrms:
+                if abs(1.0 - _q(rmsalt, self.nrmsd)) <= self.mqrms:
                     err2 = 81
-                if abs(1.0 - self.nrmsd / self.nrmsdm) <= self.mqrms and ldlamf:
+                if abs(1.0 - _q(self.nrmsd, self.nrmsdm)) <= self.mqrms and ldlamf:
                     err2 = 80
                 if it >= cfg.itmax:
                     err2 = 79
-                if abs(1.0 - self.bdpar / bdalt) < self.bdmin:
+                if abs(1.0 - _q(self.bdpar, bdalt)) < self.bdmin:
                     err2 = 109
-                if err2 != 0:
-                    self.status = "fpi" if (cfg.lfphai and err2 != 79) else str(err2)
+                if err2 != 0 and not (lfphai and err2 != 79):
+                    self.status = str(err2)
                     break
-                lamalt = self.lam
+                if err2 != 0:
+                    # final phase improvement (src/inv.f90:600-660): phase
+                    # weights, a new lambda_0, the phase-only update
+                    if not self.phase_stage:
+                        self.status = "fpi"
+                        break
+                    self.wmatd = self.data.wmatdp.copy()
+                    self.lfpi, self.lsetip = True, True
+                    lfphai, self.llam, ldlami, lfstep, self.step = False, False, True, True, 1.0
+                    self.stage_start = len(self.rows)
+                    if cfg.lffhom:  # restart from the start phase, same magnitudes
+                        a = np.abs(self.sigma)
+                        self.sigma = a * complex(math.cos(cfg.pha0 / 1e3), -math.sin(cfg.pha0 / 1e3))
+                        self.lsetup = True
+                        continue
+                    self.lsetup = False
+                    self._misfit()
+                    self._kont2(True)
+                    setup = True
+                else:
+                    lamalt = self.lam
                 if max_iterations is not None and it >= max_iterations:
                     self.status = "max_iterations"
                     break
@@ -691,8 +726,8 @@ class Inversion:
                     nr = self.nrmsd
                     search = ((((nr < rmsreg and itr <= self.nlam) or (dlam > 1.0 and itr <= self.nlam))
                                and (not ldlamf or dlalt <= 1.0)
-                               and abs(1.0 - self.bdpar / bdalt) > self.bdmin
-                               and abs(1.0 - rmsreg / self.nrmsdm) > self.mqrms)
+                               and abs(1.0 - _q(self.bdpar, bdalt)) > self.bdmin
+                               and abs(1.0 - _q(rmsreg, self.nrmsdm)) > self.mqrms)
                               or rmsreg == 0.0)
                     if search:
                         if self.lsetup or self.lsetip:
@@ -739,7 +774,8 @@ class Inversion:
             if not self.llam:
                 dpar2, ncg2 = dpar, self.ncg
                 dpar, self.ncg = b.update(self.wmatd, self.wdfak, self.dat, self.sigmaa, cfg.ltri, self.smatm,
-                                          cfg.nx, self.nachbar, self.lam, self.eps, self.ncgmax, 1.0, par)
+                                          cfg.nx, self.nachbar, self.lam, self.eps, self.ncgmax, 1.0, par,
+                                          phase_only=self.lfpi)
                 dpar = np.array(dpar, np.complex128)
             else:
                 dpar, self.ncg = dpar2, ncg2
@@ -760,7 +796,7 @@ def format_rows(rows: List[Row]) -> str:
     for r in rows:
         if r.first:
             out.append(f"{r.kind:>3s}{r.index:4d}   {r.nrmsd:10.4g}{'':48s}{r.betrms:10.4g}  {r.pharms:10.4g}  {r.npol:4d}")
-        elif r.kind == "IT":
+        elif r.kind.endswith("IT"):
             out.append(f"{r.kind:>3s}{r.index:4d}   {r.nrmsd:10.4g}  {r.bdpar:10.4g} {r.lam:10.4g}  {r.rough:10.4g}  "
                        f"{r.ncg:6d}     {r.betrms:10.4g}  {r.pharms:10.4g}  {r.npol:4d}        {r.step:5.3f}")
         else:
