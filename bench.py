@@ -410,6 +410,97 @@ def run_ensemble(args):
     return 0
 
 
+def run_inversion(args):
+    """Config 4: the CRTomo Gauss-Newton complex inversion (structured
+    smoothness, lambda search) of synthetic data on the 400x100-quad,
+    192-electrode, 20000-quadrupole mesh: 8 iterations, CG capped at 100
+    steps, mixed precision.  value = seconds per GN iteration (all its lambda
+    and step trials: forward, Jacobian, update); RMS per iteration."""
+    import torch
+
+    from titatest_gb300 import MIXED, synth
+    from titatest_gb300 import inversion as I
+    from titatest_gb300.crmod import rwaven
+
+    torch.cuda.set_device(0)
+    s = synth.config4()
+    g, sv = s.grid, s.survey
+    kwn, kwnwi = rwaven(g, sv)
+    b = I.DeviceBackend(g, sv, kwn, kwnwi, 1, False, 0, MIXED, refinement=(args.refine_maxit, args.refine_tol))
+    try:
+        # data: the true model's response with 3% + 1e-4 ohm and 1 mrad noise
+        t0 = time.perf_counter()
+        V = np.exp(-b.forward(s.sigma))
+        t_first = time.perf_counter() - t0
+        rng = np.random.default_rng(4001)
+        bet, pha = np.abs(V), np.angle(V) * 1e3
+        noisy = bet + (0.03 * bet + 1e-4) * rng.standard_normal(len(bet))
+        while np.any(noisy <= 0):  # redraw the noise of a datum that would change sign
+            bad = noisy <= 0
+            noisy[bad] = bet[bad] + (0.03 * bet[bad] + 1e-4) * rng.standard_normal(int(bad.sum()))
+        pha_n = pha + rng.standard_normal(len(pha))
+        cfg = I.CRTomoConfig(mswitch=0, delem="", delectr="", dstrom="", ramd="", ldiff=False, dd0="", dm0="",
+                             dfm0="", nx=400, nz=100, alfx=1.0, alfz=1.0, itmax=8, ldc=False, lrobust=False,
+                             lfphai=False, stabw0=3.0, stabm0=1e-4, stabpA1=0.0, stabpB=0.0, stabpA2=0.0,
+                             stabp0=1.0, lrho0=True, bet0=100.0, pha0=-10.0, lagain=False, swrtr=1, lsink=False,
+                             nsink=0, lrandb2=False, drandb="", ltri=0)
+        data = I.make_data(sv.strnr, sv.vnr, noisy, pha_n, cfg)
+        inv = I.Inversion(g, data, cfg, b, ncgmax=100)
+        calls = {"forward": 0, "sens": 0, "update": 0}
+        times = {"forward": 0.0, "sens": 0.0, "update": 0.0}
+
+        def timed(name, fn):
+            def w(*a, **k):
+                t = time.perf_counter()
+                r = fn(*a, **k)
+                times[name] += time.perf_counter() - t
+                calls[name] += 1
+                return r
+            return w
+
+        b.forward = timed("forward", b.forward)
+        b.sensitivities = timed("sens", b.sensitivities)
+        b.update = timed("update", b.update)
+        torch.cuda.synchronize()
+        with ClockSampler(0) as clk:
+            t0 = time.perf_counter()
+            rows = inv.run()
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        kpot = b.m.forward(s.sigma, kpot=True)["kpot"] if args.cpu_baseline else None
+    finally:
+        b.close()
+    cpu = None
+    if kpot is not None:
+        # the oracle on a bounded sample of the forward's systems and of the
+        # Jacobian's rows, scaled to the forwards and Jacobians of one GN
+        # iteration as this run made them (the CPU CG is not included)
+        cb = cpu_baseline(s, kwn, kwnwi, kpot, target_s=args.ref_seconds)
+        n_it_ = max(1, sum(1 for r in rows if r.kind == "IT") - 1)
+        est = (calls["forward"] * cb["forward_s"] + calls["sens"] * cb["sens_s"]) / n_it_
+        cpu = {"value": est, "unit": "s/iteration (forwards + Jacobians only)", "cores": cb["cores"],
+               "kind": "port", "sample": cb["sample"], "forward_s": cb["forward_s"], "sens_s": cb["sens_s"]}
+    its = [r for r in rows if r.kind == "IT"]
+    n_it = max(1, len(its) - 1)
+    line = {
+        "metric": "config-4 CRTomo Gauss-Newton complex inversion: seconds per GN iteration (mixed precision)",
+        "value": wall / n_it, "unit": "s/iteration", "n_gpus": 1, "steps": n_it, "warmup": 0,
+        "ms_per_step": wall * 1e3 / n_it, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64 factor + f64 refinement; f64 Jacobian products and CG",
+        "data": "synthetic (config-4 model, its response with 3% + 1e-4 ohm and 1 mrad noise)",
+        "config": {"workload": workload_string(4, s, len(kwn)) + ", 8 GN iterations, CG <= 100 steps",
+                   "regularisation": "structured smoothness (ltri 0, 400 x 100), lambda search of src/inv.f90",
+                   "parallelism": "single GPU"},
+        "rms_per_iteration": [round(r.nrmsd, 4) for r in its], "lambda_per_iteration": [r.lam for r in its[1:]],
+        "status": inv.status, "trials": len(rows) - len(its), "calls": calls,
+        "seconds": {k: round(v, 3) for k, v in times.items()}, "first_forward_s": round(t_first, 3),
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -435,6 +526,8 @@ def main():
         return run_reference(args)
     if args.config == 5:
         return run_ensemble(args)
+    if args.config == 4:
+        return run_inversion(args)
     return run_gpu(args)
 
 

@@ -210,6 +210,15 @@ int crgpu_update_fpi(crgpu_ctx *ctx, const double *wmatd, const int32_t *wdfak, 
                      const int32_t *nachbar, double lam, double eps, int32_t ncgmax, double step,
                      double *par, double *dpar, double *cgfac, float *cgres, int32_t *ncg);
 
+/* The column sums of src/blam0.f90:60-130 for the first regularisation
+ * parameter: jtj[j] = |sum_i sum_k conj(J_ij) J_ik w_i| (w_i = wmatd_i
+ * wdfak_i; phase_only: Re(J), the final phase improvement) on the
+ * sensitivities of the last crgpu_sens(ctx, 1, ...), computed as two
+ * products with J (J 1, then J^H W (J 1)).  lam_0 = 5 sum_j jtj[j] / manz *
+ * 2 / (alfx + alfz).  jtj: manz doubles. */
+int crgpu_blam0_jtj(crgpu_ctx *ctx, const double *wmatd, const int32_t *wdfak, int32_t phase_only,
+                    double *jtj);
+
 /* ------------------------------------------------------------------ */
 /* host-side set-up routines                                            */
 /* ------------------------------------------------------------------ */

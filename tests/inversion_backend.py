@@ -37,8 +37,11 @@ class OracleBackend:
                                       phase_only=phase_only)
         return dpar, ncg
 
-    def jacobian(self):
-        return self.J
+    def jtj(self, wmatd, wdfak, phase_only):
+        """|(J^H W J 1)_j| of src/blam0.f90 from the host Jacobian."""
+        w = np.asarray(wmatd) * np.asarray(wdfak, np.float64)
+        J = self.J.real if phase_only else self.J
+        return np.abs(np.conj(J).T @ (w * (J @ np.ones(J.shape[1]))))
 
 
 def golden_rows(case):

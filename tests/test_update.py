@@ -88,3 +88,19 @@ def test_update_matches_oracle(gpu_lib, grid1, ltri, lam, tol, phase_only):
     assert relerr(dg, do) < tol
     assert relerr(pg, po) < tol
     assert int(rg[0]) == ng
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("phase_only", [False, True])
+def test_blam0_column_sums_match_host(gpu_lib, grid1, phase_only):
+    """crgpu_blam0_jtj: |(J^H W J 1)_j| of src/blam0.f90 on the device
+    sensitivities against the same sums from the host copy of J."""
+    from titatest_gb300 import PLAIN, CRMod
+    s = grid1
+    with CRMod(s.grid, s.survey, precision=PLAIN) as m:
+        J, dat, sa, wmatd, wdfak, par = _update_case(m, s)
+        got = m.blam0_jtj(wmatd, wdfak, phase_only)
+    Jx = J.real if phase_only else J
+    w = wmatd * wdfak
+    ref = np.abs(np.conj(Jx).T @ (w * (Jx @ np.ones(Jx.shape[1]))))
+    assert relerr(got, ref) < 1e-12

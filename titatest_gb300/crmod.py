@@ -191,6 +191,14 @@ class CRMod:
         _check(self._h, lib().crgpu_sens(self._h, int(mode), ptr(buf, f64p)))
         return buf.T
 
+    def blam0_jtj(self, wmatd, wdfak, phase_only: bool = False) -> np.ndarray:
+        """|(J^H W J 1)_j| of src/blam0.f90 on the device sensitivities."""
+        out = np.zeros(self.grid.elanz)
+        _check(self._h, lib().crgpu_blam0_jtj(self._h, ptr(np.ascontiguousarray(wmatd, np.float64), f64p),
+                                              ptr(np.ascontiguousarray(wdfak, np.int32), i32p),
+                                              int(bool(phase_only)), ptr(out, f64p)))
+        return out
+
     def sens_on_device(self, mode: int = 1):
         """The sensitivities of the last forward into the context's device
         array only (for update), with no host copy."""

@@ -1338,6 +1338,43 @@ static int update_common(crgpu_ctx *c, int phase_only, const double *wmatd, cons
     return 0;
 }
 
+int crgpu_blam0_jtj(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, int32_t phase_only, double *jtj) {
+    if (!c || !wmatd || !wdfak || !jtj) return ERR_ARG;
+    if (!c->last_sens) return fail(c, ERR_ARG, "crgpu_blam0_jtj needs the sensitivities (crgpu_sens mode 1) first");
+    const int nanz = c->nanz, manz = c->hg.elanz;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off += (bytes + 255) & ~(size_t)255;
+        return o;
+    };
+    const size_t o_w = take(sizeof(double) * nanz), o_wd = take(sizeof(int32_t) * nanz);
+    const size_t o_cg = take(sizeof(double) * manz), o_work = take(update_work_bytes(nanz, manz));
+    if (c->upd_bytes < off) {
+        if (c->d_upd) cudaFreeAsync(c->d_upd, c->st);
+        c->d_upd = nullptr;
+        c->upd_bytes = 0;
+        cudaError_t e = cudaMallocAsync(&c->d_upd, off, c->st);
+        if (e != cudaSuccess) return fail(c, 94, std::string("blam0 work space: ") + cudaGetErrorString(e));
+        c->upd_bytes = off;
+    }
+    char *base = (char *)c->d_upd;
+    CUCHECK(c, cudaMemcpyAsync(base + o_w, wmatd, sizeof(double) * nanz, cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemcpyAsync(base + o_wd, wdfak, sizeof(int32_t) * nanz, cudaMemcpyHostToDevice, c->st));
+    CGArgs a{};
+    a.nanz = nanz;
+    a.manz = manz;
+    a.sens = c->last_sens;
+    a.wmatd = (const double *)(base + o_w);
+    a.wdfak = (const int32_t *)(base + o_wd);
+    a.cgfac = (double *)(base + o_cg);
+    a.work = (double2 *)(base + o_work);
+    a.phase_only = phase_only ? 1 : 0;
+    int rc = run_jhwj1(a, c->st, jtj);
+    if (rc) return fail(c, rc, "blam0 kernels failed");
+    return 0;
+}
+
 int crgpu_update(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, const double *dat, const double *sigmaa,
                  int32_t ltri, const double *smatm, int32_t nx, const int32_t *nachbar, double lam, double eps,
                  int32_t ncgmax, double step, double *par, double *dpar, double *cgfac, float *cgres,

@@ -102,9 +102,9 @@ __global__ __launch_bounds__(kRedThreads) void k_colred(CGArgs a, int mode, cons
             gi += red[1][q];
             dg += red[2][q];
         }
-        double diagR = a.ltri == 0 ? a.smatm[j] : a.smatm[(size_t)a.maxnk * a.manz + j];
         double cf;
         if (mode == 0) {
+            const double diagR = a.ltri == 0 ? a.smatm[j] : a.smatm[(size_t)a.maxnk * a.manz + j];
             cf = 1.0 / sqrt(dg + a.lam * diagR);
             cgfac[j] = cf;
             out[j] = cz((gr - a.lam * rm[j].x) * cf, (gi - a.lam * rm[j].y) * cf);
@@ -215,6 +215,19 @@ __global__ void k_final(int n, double2 *dpar, const double *__restrict__ cgfac, 
 
 inline unsigned nblk(int n, int t) { return (unsigned)((n + t - 1) / t); }
 
+__global__ void k_fill_one(int n, double2 *v, double *f) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    v[i] = cz(1.0, 0.0);
+    f[i] = 1.0;
+}
+
+__global__ void k_abs(int n, const double2 *__restrict__ v, double *out) {  // out may not alias v
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = hypot(v[i].x, v[i].y);
+}
+
 }  // namespace
 
 // work layout (double2 units): bvec, rvec, pvec, dpar(out) | ap, dmf (nanz) |
@@ -285,6 +298,31 @@ int run_update(const CGArgs &a, cudaStream_t st, int *ncg_out, float *cgres_host
     cudaError_t e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaGetLastError();
     *ncg_out = ncg;
+    return e == cudaSuccess ? 0 : ERR_CUDA;
+}
+
+// |(J^H W J 1)_j| of src/blam0.f90:60-130 (phase only: Re(J)): the double
+// sum over data and model cells as two products with J.  Reads a.sens,
+// a.wmatd, a.wdfak and the work space; a.smatm, a.nachbar, a.par, a.dpar,
+// a.dat and a.sigmaa are not used (k_colred reads smatm in mode 0 only).
+int run_jhwj1(CGArgs a, cudaStream_t st, double *jtj_host) {
+    const int manz = a.manz, nanz = a.nanz;
+    const int nchunk = (manz + kColChunk - 1) / kColChunk;
+    double2 *bvec = a.work, *ones = bvec + manz, *pvec = ones + manz;
+    double2 *ap = pvec + manz, *dmf = ap + nanz, *partial = dmf + nanz;
+    (void)dmf;
+    const int T = 256;
+    k_fill_one<<<nblk(manz, T), T, 0, st>>>(manz, ones, a.cgfac);
+    cudaMemsetAsync(bvec, 0, sizeof(double2) * manz, st);
+    dim3 g1(nblk(nanz, kRowTile), nchunk);
+    k_jp_partial<<<g1, kRowTile, 0, st>>>(a, ones, partial);
+    k_jp_reduce<<<nblk(nanz, T), T, 0, st>>>(a, nchunk, partial, ap);
+    a.lam = 0.0;
+    k_colred<<<manz, kRedThreads, 0, st>>>(a, 1, ap, bvec, a.cgfac, pvec);
+    k_abs<<<nblk(manz, T), T, 0, st>>>(manz, pvec, (double *)bvec);
+    cudaMemcpyAsync(jtj_host, bvec, sizeof(double) * manz, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
     return e == cudaSuccess ? 0 : ERR_CUDA;
 }
 

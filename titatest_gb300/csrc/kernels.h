@@ -99,5 +99,7 @@ struct CGArgs {
 size_t update_work_bytes(int nanz, int manz);
 // runs update + cjggra; cgres (host, ncgmax+2 floats) receives the CG record
 int run_update(const CGArgs &a, cudaStream_t st, int *ncg_out, float *cgres_host);
+// |(J^H W J 1)_j| for the first regularisation parameter (src/blam0.f90); jtj_host: manz doubles
+int run_jhwj1(CGArgs a, cudaStream_t st, double *jtj_host);
 
 }  // namespace crgpu

@@ -202,6 +202,23 @@ class Data:
     wmatd_cri: np.ndarray  # 1/(eps_r^2 + eps_p^2)
 
 
+def make_data(strnr, vnr, bet, pha, cfg: CRTomoConfig) -> Data:
+    """Data from arrays with the error model of src/rdati.f90:234-255 (bet:
+    |R| in ohm, pha: phase in mrad)."""
+    bet = np.asarray(bet, np.float64)
+    pha = np.zeros_like(bet) if cfg.ldc else np.asarray(pha, np.float64)
+    if np.any(bet <= 0.0):
+        raise formats.CRError(94, "resistance not positive")
+    stabw = 1e-2 * cfg.stabw0 + cfg.stabm0 / bet
+    stabwp = (cfg.stabpA1 * bet ** cfg.stabpB + 1e-2 * cfg.stabpA2 * np.abs(pha) + cfg.stabp0) * 1e-3
+    dat = -np.log(bet) - 1j * pha / 1e3
+    wr = 1.0 / stabw ** 2
+    wp = np.zeros_like(bet) if cfg.ldc else 1.0 / stabwp ** 2
+    wc = np.zeros_like(bet) if cfg.ldc else 1.0 / (stabw ** 2 + stabwp ** 2)
+    return Data(strnr=np.asarray(strnr, np.int32), vnr=np.asarray(vnr, np.int32), dat=dat, wmatdr=wr,
+                wmatdp=wp, wmatd_cri=wc)
+
+
 def read_data(path: str, cfg: CRTomoConfig, eanz: int) -> Data:
     """Measurements and their weights.  Without individual errors the error
     model err(R) = A1 |R| + A2 (as an error of ln R: 1e-2 A1 + A2/|R|) and
@@ -443,30 +460,24 @@ class DeviceBackend:
                                                  phase_only=phase_only)
         return dp, ncg
 
-    def jacobian(self) -> np.ndarray:
-        return self.m.sens(1)
+    def jtj(self, wmatd, wdfak, phase_only: bool) -> np.ndarray:
+        return self.m.blam0_jtj(wmatd, wdfak, phase_only)
 
     def close(self):
         self.m.close()
 
 
 def blam0(cfg: CRTomoConfig, lamnull_cri: float, lamnull_fpi: float, manz: int, nanz: int, lfpi: bool,
-          jacobian, wmatd, wdfak) -> float:
+          jtj_fn, wmatd, wdfak) -> float:
     """src/blam0.f90: a preset lambda_0 (nz = -1: max(manz, nanz); nz < -1:
     |nz|; crt.lamnull), else 5 mean_j |(J^H W J 1)_j| 2/(alfx + alfz) --
-    the double sum of the reference factorises into two products with J."""
+    jtj_fn(wmatd, wdfak, lfpi) gives |(J^H W J 1)_j| (Re(J) when lfpi)."""
     eps = np.finfo(np.float64).eps
     if ((cfg.llamf & 1) or lamnull_cri > eps) and not lfpi:
         return float(max(manz, nanz)) if cfg.nz == -1 else float(lamnull_cri)
     if (cfg.llamf & 1) or lamnull_fpi > eps:
         return float(lamnull_fpi)
-    J = jacobian()
-    w = np.asarray(wmatd) * np.asarray(wdfak, np.float64)
-    if lfpi:
-        Jr = J.real
-        jtj = np.abs(Jr.T @ (w * (Jr @ np.ones(manz))))
-    else:
-        jtj = np.abs(np.conj(J).T @ (w * (J @ np.ones(manz))))
+    jtj = np.asarray(jtj_fn(wmatd, wdfak, lfpi))
     lam = float(np.sum(jtj)) / manz
     return lam * 2.0 / (cfg.alfx + cfg.alfz) * 5.0
 
@@ -498,8 +509,10 @@ class Inversion:
 
     grid, enr: the mesh and electrodes; data: read_data(); cfg:
     read_crtomo_cfg().  backend: an object with forward(sigma) -> sigmaa,
-    sensitivities(), update(...) -> (dpar, ncg) and jacobian(), as
-    DeviceBackend.  sigma_start: the start model when cfg.lrho0 is off."""
+    sensitivities(), update(...) -> (dpar, ncg) and jtj(wmatd, wdfak,
+    phase_only) -> |(J^H W J 1)_j|, as DeviceBackend.  sigma_start: the start
+    model when cfg.lrho0 is off; ncgmax: a cap on the CG steps other than
+    the reference's manz/10."""
 
     # src/rall.f90:196-222 defaults
     nrmsdm = 1.0
@@ -513,7 +526,7 @@ class Inversion:
     lpol = False
 
     def __init__(self, grid, data: Data, cfg: CRTomoConfig, backend, sigma_start=None,
-                 lamnull: Optional[tuple] = None, phase_stage: bool = True):
+                 lamnull: Optional[tuple] = None, phase_stage: bool = True, ncgmax: Optional[int] = None):
         if cfg.lrobust or cfg.ldiff or cfg.ldc:
             raise NotImplementedError("robust, difference and DC inversion are not built")
         if cfg.ltri not in (0, 1, 2):
@@ -524,6 +537,8 @@ class Inversion:
             raise formats.CRError(50, "manz /= elanz is not implemented")
         self.nanz = len(data.dat)
         self.ncgmax = self.manz // 10 if cfg.ltri < 5 else self.manz  # src/rall.f90:745-746
+        if ncgmax is not None:
+            self.ncgmax = int(ncgmax)
         # first lambda (src/rall.f90:768-796; lamnull = the crt.lamnull file)
         if lamnull is not None:
             self.lamnull_cri, self.lamnull_fpi = lamnull
@@ -732,7 +747,7 @@ class Inversion:
                     if search:
                         if self.lsetup or self.lsetip:
                             self.lam = blam0(cfg, self.lamnull_cri, self.lamnull_fpi, self.manz, self.nanz,
-                                             self.lfpi, b.jacobian, self.wmatd, self.wdfak)
+                                             self.lfpi, b.jtj, self.wmatd, self.wdfak)
                             lamalt = self.lam
                         else:
                             dlalt = dlam
