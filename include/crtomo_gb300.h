@@ -109,6 +109,16 @@ int crgpu_set_stream(crgpu_ctx *ctx, void *stream);
  * the values.  A node outside 1..sanz returns 30. */
 int crgpu_set_boundary_values(crgpu_ctx *ctx, int32_t rwdanz, const int32_t *rwdnr, const double *rwd);
 
+/* DC mode (CRTomo ldc): the DC twins of the hot path (src/kompadc.f90,
+ * src/scaldc.f90, src/choldc.f90, src/vredc.f90, src/bsendc.f90) on the
+ * complex path: the real parts of sigma, an error 28 for a pivot <= 0
+ * (src/choldc.f90:66-70, where src/chol.f90 stops only on 0), the real
+ * voltage with a +0 imaginary part for -log V (src/bvolti.f90:56-62).  With
+ * real conductivities every other complex operation of the path keeps its
+ * imaginary parts 0, so the values are those of the real routines.
+ * ldc: 0 or 1. */
+int crgpu_set_dc(crgpu_ctx *ctx, int32_t ldc);
+
 /* Upper bound of device memory for the per-system band factors; systems are
  * processed in batches that fit.  Default: 60% of free device memory. */
 int crgpu_set_memory_budget(crgpu_ctx *ctx, int64_t bytes);
@@ -209,6 +219,13 @@ int crgpu_update_fpi(crgpu_ctx *ctx, const double *wmatd, const int32_t *wdfak, 
                      const double *sigmaa, int32_t ltri, const double *smatm, int32_t nx,
                      const int32_t *nachbar, double lam, double eps, int32_t ncgmax, double step,
                      double *par, double *dpar, double *cgfac, float *cgres, int32_t *ncg);
+
+/* The same for DC inversion (ldc, src/update.f90 with sensdc and cjggdc):
+ * the real CG on the real part of the right-hand side; the update real. */
+int crgpu_update_dc(crgpu_ctx *ctx, const double *wmatd, const int32_t *wdfak, const double *dat,
+                    const double *sigmaa, int32_t ltri, const double *smatm, int32_t nx,
+                    const int32_t *nachbar, double lam, double eps, int32_t ncgmax, double step,
+                    double *par, double *dpar, double *cgfac, float *cgres, int32_t *ncg);
 
 /* The column sums of src/blam0.f90:60-130 for the first regularisation
  * parameter: jtj[j] = |sum_i sum_k conj(J_ij) J_ik w_i| (w_i = wmatd_i

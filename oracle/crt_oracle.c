@@ -554,6 +554,8 @@ typedef struct {
     int rwdanz;
     const int *rwdnr;
     const cx *rwd;
+    int ldc;
+    cx *sigma_dc; /* owned: the real parts of sigma (DC) */
 } fe_ctx;
 
 /* src/kompab.f90:11-194 */
@@ -694,7 +696,9 @@ static int scalab(int sanz, int mb, cx *a, cx *b, double *fak) {
 }
 
 /* src/chol.f90:7-88: in-place complex-symmetric L L^T (no conjugation) */
-static int chol(int sanz, int mb, cx *a) {
+/* ldc: src/choldc.f90:66-70 stops on a pivot <= 0 (the complex routine only
+ * on 0); with real data every other step is the same arithmetic */
+static int chol(int sanz, int mb, cx *a, int ldc) {
     int m1 = mb + 1;
     for (int i = 1; i <= sanz; i++) {
         long idi = (long)i * m1;
@@ -707,7 +711,7 @@ static int chol(int sanz, int mb, cx *a) {
             if (j < i) {
                 a[ij - 1] = cdiv(s, a[(long)j * m1 - 1]);
             } else {
-                if (cabs_(s) <= 0.0) return 28;
+                if (cabs_(s) <= 0.0 || (ldc && !(s.re > 0.0))) return 28;
                 a[idi - 1] = csqrt_(s);
             }
         }
@@ -741,6 +745,7 @@ static int setup_ctx(const or_mesh *m, const or_opts *o, int kwnanz, const doubl
                      int *lbeta, int *lsr_eff) {
     or_counts(m, &c->elanz, &c->relanz, &c->maxnk);
     c->m = m;
+    c->sigma_dc = NULL;
     c->kwnanz = kwnanz;
     *elbg = (double *)calloc((size_t)c->elanz * 10 * kwnanz + 1, sizeof(double));
     *relbg = (double *)calloc((size_t)c->relanz * 10 + 1, sizeof(double));
@@ -763,6 +768,13 @@ static int setup_ctx(const or_mesh *m, const or_opts *o, int kwnanz, const doubl
     c->rwdanz = o->rwdanz;
     c->rwdnr = o->rwdnr;
     c->rwd = (const cx *)o->rwd;
+    c->ldc = o->ldc;
+    c->sigma_dc = NULL;
+    if (o->ldc) { /* src/kompadc.f90:114-119: DBLE(sigma) */
+        c->sigma_dc = (cx *)malloc(sizeof(cx) * (size_t)c->elanz + 1);
+        for (int i = 0; i < c->elanz; i++) c->sigma_dc[i] = cmk(((const cx *)sigma)[i].re, 0.0);
+        c->sigma = c->sigma_dc;
+    }
     for (int ir = 0; ir < c->rwdanz; ir++)  /* src/rrandb.f90 (error 30) */
         if (c->rwdnr[ir] < 1 || c->rwdnr[ir] > m->sanz) return 30;
     *lsr_eff = lsr;
@@ -794,7 +806,7 @@ static int forward_k(const fe_ctx *c, int lbeta, int lana, int k, const double *
             if (!e && c->lrandb) randb(m, a, b);
             if (!e && c->rwdanz) randb2(c, a, b);
             if (!e) e = scalab(sanz, mb, a, b, fak);
-            if (!e) e = chol(sanz, mb, a);
+            if (!e) e = chol(sanz, mb, a, c->ldc);
             if (e) { err = e; break; }
             have_factor = 1;
         } else if (!lana) {
@@ -842,7 +854,7 @@ int or_forward(const or_mesh *m, const or_opts *o, int kwnanz, const double *kwn
         }
         e = err;
     }
-    free(elbg); free(relbg); free(kg);
+    free(elbg); free(relbg); free(kg); free(c.sigma_dc);
     return e;
 }
 
@@ -876,7 +888,7 @@ int or_forward_pairs(const or_mesh *m, const or_opts *o, int kwnanz, const doubl
         }
         e = err;
     }
-    free(elbg); free(relbg); free(kg);
+    free(elbg); free(relbg); free(kg); free(c.sigma_dc);
     return e;
 }
 
@@ -942,6 +954,7 @@ int or_bvolt(const or_mesh *m, int mode, const double *hpot, const double *kfak,
         cx d4 = (e3 > 0 && e1 > 0) ? HP(e3, e1) : cmk(0, 0);
 #undef HP
         cx v = csub(csub(d1, d2), csub(d3, d4));
+        if (mode == 2) v.im = 0.0; /* DC: dcmplx of the real voltage, src/bvolti.f90:56-62 */
         CX(volt, i) = v;
         if (mode == 0) {
             CX(sigmaa, i) = cmul(cmk(kfak ? kfak[i] : 1.0, 0.0), v);
@@ -1351,13 +1364,14 @@ static void rmul_tri(int manz, int maxnk, const int *nachbar, const double *smat
     }
 }
 
-/* src/update.f90 with lfpi and cjggdc (src/cg_mod.f90:136-260, bapdc, bpdc,
- * bpdctri, bbdc): Re(J) in the preconditioner, the right-hand side and the
- * products; the real CG runs on Im(bvec); the update goes into the phases. */
-static int update_fpi(int nanz, int manz, const cx *sens, const double *wmatd, const int *wdfak,
-                      const cx *dat, const cx *sigmaa, int ltri, const double *smatm, int nx,
-                      const int *nachbar, int maxnk, double lam, double eps, int ncgmax, double step,
-                      cx *par, cx *dpar, double *cgfac, float *cgres) {
+/* src/update.f90 with lfpi or ldc and cjggdc (src/cg_mod.f90:136-260, bapdc,
+ * bpdc, bpdctri, bbdc): Re(J) in the preconditioner, the right-hand side and
+ * the products; the real CG runs on Im(bvec) (part 1, lfpi: the update goes
+ * into the phases) or Re(bvec) (part 2, ldc: the update is real). */
+static int update_real(int part, int nanz, int manz, const cx *sens, const double *wmatd, const int *wdfak,
+                       const cx *dat, const cx *sigmaa, int ltri, const double *smatm, int nx,
+                       const int *nachbar, int maxnk, double lam, double eps, int ncgmax, double step,
+                       cx *par, cx *dpar, double *cgfac, float *cgres) {
     cx *bvec = (cx *)calloc((size_t)manz, sizeof(cx));
     cx *tmp = (cx *)calloc((size_t)manz, sizeof(cx));
     double *bdc = (double *)calloc((size_t)manz, sizeof(double));
@@ -1379,7 +1393,7 @@ static int update_fpi(int nanz, int manz, const cx *sens, const double *wmatd, c
         for (int i = 0; i < nanz; i++)
             cdum = cadd(cdum, cmul(cmk(RS(i, j) * wmatd[i] * (double)wdfak[i], 0.0), csub(dat[i], sigmaa[i])));
         bvec[j] = cmul(csub(cdum, cmul(cmk(lam, 0.0), bvec[j])), cmk(cgfac[j], 0.0));
-        bdc[j] = bvec[j].im;
+        bdc[j] = part == 1 ? bvec[j].im : bvec[j].re; /* src/cg_mod.f90:160-164 */
         rdc[j] = bdc[j];
     }
     double dr = 0, dr0 = 0, dr1 = 0, beta = 0, alpha;
@@ -1422,7 +1436,7 @@ static int update_fpi(int nanz, int manz, const cx *sens, const double *wmatd, c
     if (k > ncgmax) ncg = ncgmax;
     cgres[0] = (float)ncg;
     for (int j = 0; j < manz; j++) {
-        dpar[j] = cmk(0.0, dp[j] * cgfac[j]);
+        dpar[j] = part == 1 ? cmk(0.0, dp[j] * cgfac[j]) : cmk(dp[j] * cgfac[j], 0.0);
         par[j] = cadd(par[j], cmul(cmk(step, 0.0), dpar[j]));
     }
 #undef RS
@@ -1434,8 +1448,18 @@ int or_update_fpi(int nanz, int manz, const double *sens, const double *wmatd, c
                   const double *dat, const double *sigmaa, int ltri, const double *smatm, int nx,
                   const int *nachbar, int maxnk, double lam, double eps, int ncgmax, double step,
                   double *par, double *dpar, double *cgfac, float *cgres) {
-    return update_fpi(nanz, manz, (const cx *)sens, wmatd, wdfak, (const cx *)dat, (const cx *)sigmaa, ltri,
-                      smatm, nx, nachbar, maxnk, lam, eps, ncgmax, step, (cx *)par, (cx *)dpar, cgfac, cgres);
+    return update_real(1, nanz, manz, (const cx *)sens, wmatd, wdfak, (const cx *)dat, (const cx *)sigmaa, ltri,
+                       smatm, nx, nachbar, maxnk, lam, eps, ncgmax, step, (cx *)par, (cx *)dpar, cgfac, cgres);
+}
+
+/* DC inversion (ldc: src/update.f90 with sensdc, cjggdc on Re(bvec)); the
+ * real Jacobian is Re(sens) */
+int or_update_dc(int nanz, int manz, const double *sens, const double *wmatd, const int *wdfak,
+                 const double *dat, const double *sigmaa, int ltri, const double *smatm, int nx,
+                 const int *nachbar, int maxnk, double lam, double eps, int ncgmax, double step,
+                 double *par, double *dpar, double *cgfac, float *cgres) {
+    return update_real(2, nanz, manz, (const cx *)sens, wmatd, wdfak, (const cx *)dat, (const cx *)sigmaa, ltri,
+                       smatm, nx, nachbar, maxnk, lam, eps, ncgmax, step, (cx *)par, (cx *)dpar, cgfac, cgres);
 }
 
 int or_update(int nanz, int manz, const double *sens_, const double *wmatd, const int *wdfak,
@@ -1541,10 +1565,10 @@ int or_factor(const or_mesh *m, const or_opts *o, int kwnanz, const double *kwn,
         if (!e && c.lrandb) randb(m, (cx *)a_out, b);
         if (!e && c.rwdanz) randb2(&c, (cx *)a_out, b);
         if (!e) e = scalab(sanz, mb, (cx *)a_out, b, fak_out);
-        if (!e) e = chol(sanz, mb, (cx *)a_out);
+        if (!e) e = chol(sanz, mb, (cx *)a_out, c.ldc);
         free(b);
         free(pota);
     }
-    free(elbg); free(relbg); free(kg);
+    free(elbg); free(relbg); free(kg); free(c.sigma_dc);
     return e;
 }

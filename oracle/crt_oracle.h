@@ -54,6 +54,7 @@ typedef struct {
     int rwdanz;     /* Dirichlet boundary values of src/randb2.f90 (lrandb2); 0: none */
     const int *rwdnr;   /* rwdanz node numbers, 1-based */
     const double *rwd;  /* rwdanz complex values (re, im pairs) */
+    int ldc;            /* DC twins (src/kompadc.f90 ... src/choldc.f90): Re(sigma), pivots > 0 */
 } or_opts;
 
 /* derived mesh counts */
@@ -101,7 +102,8 @@ void or_rtrafo(const or_mesh *m, int swrtr, int kwnanz, const double *kwnwi,
 int or_bkfak(const or_mesh *m, double *kfak);
 
 /* src/bvolt.f90 (mode 0: sigmaa = kfak*V) and src/bvolti.f90 (mode 1:
- * sigmaa = -log V).  kfak may be NULL (= 1).  Returns errnr. */
+ * sigmaa = -log V; mode 2: DC, V = dcmplx(Re V)).  kfak may be NULL (= 1).
+ * Returns errnr. */
 int or_bvolt(const or_mesh *m, int mode, const double *hpot, const double *kfak,
              double *volt, double *sigmaa);
 
@@ -155,7 +157,13 @@ int or_update(int nanz, int manz, const double *sens, const double *wmatd,
               int maxnk, double lam, double eps, int ncgmax, double step,
               double *par, double *dpar, double *cgfac, float *cgres);
 
-/* the same in the final phase improvement (lfpi; cjggdc on Re(J)) */
+/* the same in the final phase improvement (lfpi; cjggdc on Re(J)); and for
+ * DC inversion (ldc; cjggdc on Re(J) and Re(bvec)) */
+int or_update_dc(int nanz, int manz, const double *sens, const double *wmatd,
+                 const int *wdfak, const double *dat, const double *sigmaa,
+                 int ltri, const double *smatm, int nx, const int *nachbar,
+                 int maxnk, double lam, double eps, int ncgmax, double step,
+                 double *par, double *dpar, double *cgfac, float *cgres);
 int or_update_fpi(int nanz, int manz, const double *sens, const double *wmatd,
                   const int *wdfak, const double *dat, const double *sigmaa,
                   int ltri, const double *smatm, int nx, const int *nachbar,

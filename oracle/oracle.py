@@ -43,7 +43,7 @@ class OrMesh(C.Structure):
 class OrOpts(C.Structure):
     _fields_ = [("swrtr", C.c_int), ("lsr", C.c_int), ("lana", C.c_int), ("lsink", C.c_int),
                 ("nsink", C.c_int), ("lsytop", C.c_int), ("nthreads", C.c_int),
-                ("rwdanz", C.c_int), ("rwdnr", i32p), ("rwd", f64p)]
+                ("rwdanz", C.c_int), ("rwdnr", i32p), ("rwd", f64p), ("ldc", C.c_int)]
 
 
 def lib():
@@ -96,6 +96,7 @@ class Problem:
             strom=np.ascontiguousarray(survey.strom, np.float64),
         )
         self._rwd = None
+        self._ldc = 0
         k = self._keep
         self.m = OrMesh(
             grid.sanz, grid.typanz, grid.mb, _p(k["typ"], i32p), _p(k["nelanz"], i32p),
@@ -147,8 +148,14 @@ class Problem:
         assert nr.shape == vv.shape
         self._rwd = (nr, vv)
 
+    def set_dc(self, ldc=True):
+        """DC twins (CRTomo ldc): Re(sigma) in the assembly, the pivot test of
+        src/choldc.f90; bvolt(..., mode=2) and update(..., dc=True) go with it."""
+        self._ldc = int(bool(ldc))
+
     def _opts(self, *args):
         o = OrOpts(*args)
+        o.ldc = self._ldc
         if self._rwd is not None:
             nr, vv = self._rwd
             o.rwdanz = len(nr)
@@ -301,7 +308,7 @@ def cutmck(grid, enr):
 
 
 def update(sens, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx=0, nachbar=None, maxnk=4, lam=1.0,
-           eps=1e-4, ncgmax=100, step=1.0, par=None, phase_only=False):
+           eps=1e-4, ncgmax=100, step=1.0, par=None, phase_only=False, dc=False):
     """src/update.f90 + cjggra (phase_only: the final phase improvement with
     cjggdc); sens (nanz, manz) complex.  Returns (par_new, dpar, cgfac,
     cgres, ncg)."""
@@ -317,7 +324,7 @@ def update(sens, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx=0, nachbar=None, max
     sa = np.ascontiguousarray(sigmaa, np.complex128)
     sm = np.ascontiguousarray(smatm, np.float64)
     nb = np.ascontiguousarray(nachbar if nachbar is not None else np.zeros(1), np.int32)
-    fn = lib().or_update_fpi if phase_only else lib().or_update
+    fn = lib().or_update_fpi if phase_only else lib().or_update_dc if dc else lib().or_update
     ncg = fn(nanz, manz, _p(s, f64p), _p(wm, f64p), _p(wd, i32p), _p(d, f64p),
                           _p(sa, f64p), ltri, _p(sm, f64p), nx, _p(nb, i32p), maxnk,
                           C.c_double(lam), C.c_double(eps), ncgmax, C.c_double(step),

@@ -36,6 +36,11 @@ INVERSION = {
     "mixed_surf": "tests/2.5D_mixed_surf/Reference",
 }
 
+# DC_Problem: one mesh and data set inverted twice by the reference, as a
+# complex problem (crtomo.cfg, inv.ctr) and with the DC routines (ldc:
+# crtomo_dc.cfg, inv_dc.ctr, a run that the DC factor ended with errnr 28)
+DC_PROBLEM = "tests/DC_Problem"
+
 CUTMCK = {
     "minimal": "tests/minimal/Reference/grid",
     "mixed_surf": "tests/2.5D_mixed_surf/Reference/grid",
@@ -61,6 +66,16 @@ def main(ref: str):
         src = os.path.join(ref, d)
         for f in ("exe/crtomo.cfg", "inv/inv.ctr"):
             shutil.copyfile(os.path.join(src, f), os.path.join(out, os.path.basename(f)))
+    out = os.path.join(here, "dc_problem")
+    os.makedirs(out, exist_ok=True)
+    src = os.path.join(ref, DC_PROBLEM)
+    for f, dst in (("Complex/grid/elem.dat", "elem.dat"), ("Complex/grid/elec.dat", "elec.dat"),
+                   ("Complex/mod/volt.dat", "volt.dat"), ("Complex/exe/crtomo.cfg", "crtomo.cfg"),
+                   ("Complex/inv/inv.ctr", "inv.ctr"), ("DC/exe/crtomo.cfg", "crtomo_dc.cfg"),
+                   ("DC/inv/inv.ctr", "inv_dc.ctr")):
+        shutil.copyfile(os.path.join(src, f), os.path.join(out, dst))
+    with open(os.path.join(out, "SOURCE"), "w") as fh:
+        fh.write(DC_PROBLEM + "/{Complex,DC}\n")
     for name, d in CUTMCK.items():
         out = os.path.join(here, "cutmck_" + name)
         os.makedirs(out, exist_ok=True)

@@ -14,16 +14,23 @@ class OracleBackend:
     """forward + src/bvolti.f90, src/bsensi.f90 and src/update.f90 by the
     oracle (complex128)."""
 
-    def __init__(self, grid, survey, kwn, kwnwi, swrtr=1, lsink=False, nsink=0):
+    def __init__(self, grid, survey, kwn, kwnwi, swrtr=1, lsink=False, nsink=0, ldc=False):
         self.P = O.Problem(grid, survey)
         self.grid, self.kwn, self.kwnwi = grid, kwn, kwnwi
         self.kw = dict(swrtr=swrtr, lsink=lsink, nsink=nsink)
+        self.ldc = ldc
+        self.P.set_dc(ldc)
 
     def forward(self, sigma):
-        self.sigma = np.array(sigma, np.complex128)
-        self.kp = self.P.forward(self.sigma, self.kwn, self.kwnwi, **self.kw)
-        hp = self.P.rtrafo(self.kp, self.kwnwi, self.kw["swrtr"])
-        self.volt, sa = self.P.bvolt(hp, 1, None)
+        # DC: the real routines read DBLE(sigma) (src/kompadc.f90, src/bsendc.f90)
+        self.sigma = np.array(sigma.real if self.ldc else sigma, np.complex128)
+        try:
+            self.kp = self.P.forward(self.sigma, self.kwn, self.kwnwi, **self.kw)
+            hp = self.P.rtrafo(self.kp, self.kwnwi, self.kw["swrtr"])
+            self.volt, sa = self.P.bvolt(hp, 2 if self.ldc else 1, None)
+        except RuntimeError as e:  # "... errnr N" of the oracle, as the library's errors carry it
+            from titatest_gb300.formats import CRError
+            raise CRError(int(str(e).split()[-1]), str(e)) from e
         return sa
 
     def sensitivities(self):
@@ -31,10 +38,10 @@ class OracleBackend:
                               swrtr=self.kw["swrtr"])
 
     def update(self, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx, nachbar, lam, eps, ncgmax, step, par,
-               phase_only=False):
+               phase_only=False, dc=False):
         _, dpar, _, _, ncg = O.update(self.J, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx=nx, nachbar=nachbar,
                                       maxnk=self.grid.maxnk, lam=lam, eps=eps, ncgmax=ncgmax, step=step, par=par,
-                                      phase_only=phase_only)
+                                      phase_only=phase_only, dc=dc)
         return dpar, ncg
 
     def jtj(self, wmatd, wdfak, phase_only):
@@ -113,3 +120,26 @@ def compare_rows(gold, rows, ncgmax):
         assert _close(r.rough, g[5], t["rough"]), (where, r.rough, g[5])
         assert abs(r.ncg - g[6]) <= t["ncg"], (where, r.ncg, g[6])
         assert r.step == g[7], (where, r.step, g[7])
+
+
+def dc_problem(ldc):
+    """The DC_Problem tomodir: (grid, survey, data, cfg, kwn, kwnwi) for the
+    complex inversion (ldc False) or the DC one (crtomo_dc.cfg)."""
+    from titatest_gb300 import inversion as I
+    g, sv, data, cfg, kwn, kwnwi = inversion_case("dc_problem")
+    if ldc:
+        d = os.path.join(GOLDEN, "dc_problem")
+        cfg = I.read_crtomo_cfg(os.path.join(d, "crtomo_dc.cfg"))
+        data = I.read_data(os.path.join(d, "volt.dat"), cfg, sv.eanz)
+    return g, sv, data, cfg, kwn, kwnwi
+
+
+def golden_rows_file(case, name):
+    """golden_rows of another inv.ctr of a case"""
+    rows = []
+    with open(os.path.join(GOLDEN, case, name)) as fh:
+        for line in fh:
+            t = line.split()
+            if t and t[0] == "IT" and len(t) == 6:
+                rows.append((t[0], int(t[1]), float(t[2]), float(t[3]), t[4], int(t[5])))
+    return rows

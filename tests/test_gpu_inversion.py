@@ -63,3 +63,41 @@ def test_run_crtomo_on_a_tomodir(gpu_lib, tmp_path):
     assert len(lines) == 25 and lines[0].split()[:3] == ["IT", "0", "111.9"]
     sig = F.read_rho(str(tmp_path / "inv" / "rho.dat"), inv.grid.elanz)
     assert np.max(np.abs(sig / inv.sigma - 1)) < 1e-8
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_gpu_dc_twin_stops_like_the_reference(gpu_lib, prec):
+    """DC mode (crgpu_set_dc): IT 0 of the reference's DC run (37.02, 10 data
+    of changed polarity), then errnr 28 from the DC pivot test in the first
+    trial's factor -- in the complex128 factor and in the complex64 ones."""
+    from titatest_gb300 import inversion as I
+    from titatest_gb300._lib import CRGPUError
+    from inversion_backend import dc_problem, golden_rows_file
+    g, sv, data, cfg, kwn, kwnwi = dc_problem(True)
+    b = I.DeviceBackend(g, sv, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink, prec, refinement=(8, 1e-10), ldc=True)
+    try:
+        inv = I.Inversion(g, data, cfg, b)
+        with pytest.raises(CRGPUError) as ei:
+            inv.run()
+    finally:
+        b.close()
+    assert ei.value.errnr == 28
+    (kind, it, rms, betrms, pharms, npol), = golden_rows_file("dc_problem", "inv_dc.ctr")
+    assert len(inv.rows) == 1 and inv.rows[0].npol == npol and abs(inv.rows[0].nrmsd / rms - 1) < 2e-3
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_gpu_complex_twin_of_the_dc_problem(gpu_lib, prec):
+    import math
+
+    from titatest_gb300 import inversion as I
+    from inversion_backend import dc_problem
+    g, sv, data, cfg, kwn, kwnwi = dc_problem(False)
+    b = I.DeviceBackend(g, sv, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink, prec, refinement=(8, 1e-10))
+    try:
+        inv = I.Inversion(g, data, cfg, b)
+        rows = inv.run(max_iterations=2)
+    finally:
+        b.close()
+    compare_rows(golden_rows("dc_problem")[:7], rows, inv.ncgmax)
+    assert math.isnan(rows[0].pharms) and rows[4].npol == 389

@@ -16,7 +16,10 @@ line are those of tests/inversion_backend.py."""
 import numpy as np
 import pytest
 
-from inversion_backend import OracleBackend, compare_rows, golden_rows, inversion_case
+import math
+
+from inversion_backend import (OracleBackend, compare_rows, dc_problem, golden_rows, golden_rows_file,
+                               inversion_case)
 
 
 def _run(case, max_iterations=None):
@@ -65,3 +68,36 @@ def test_parfit_cases():
     # fb below fmin: linear interpolation to fmin between 0 and 0.5
     assert abs(parfit(3.0, 0.5, 2.0, 1.0, 1e-3, 0.5) - 0.5 * (1.0 - 3.0) / (0.5 - 3.0)) < 1e-15
     assert parfit(1.0, 1.0, 1.0, 1.0, 1e-3, 0.5) == 1e-3
+
+
+def test_dc_twin_stops_on_the_indefinite_matrix_like_the_reference():
+    """DC_Problem with ldc: the DC routines of the reference (src/choldc.f90
+    stops on a pivot <= 0) print IT 0 -- misfit 37.02, phase RMS 0, 10 data
+    of changed polarity -- and end with errnr 28 ("FE matrix indefinite") in
+    the forward of the first trial model."""
+    from titatest_gb300 import formats as F
+    from titatest_gb300 import inversion as I
+    g, sv, data, cfg, kwn, kwnwi = dc_problem(True)
+    assert cfg.ldc
+    inv = I.Inversion(g, data, cfg, OracleBackend(g, sv, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink, ldc=True))
+    with pytest.raises(F.CRError) as ei:
+        inv.run()
+    assert ei.value.errnr == 28
+    (kind, it, rms, betrms, pharms, npol), = golden_rows_file("dc_problem", "inv_dc.ctr")
+    assert len(inv.rows) == 1 and inv.rows[0].kind == "IT" and inv.rows[0].npol == npol == 10
+    assert abs(inv.rows[0].nrmsd / rms - 1) < 2e-3 and float(pharms) == inv.rows[0].pharms == 0.0
+
+
+def test_complex_twin_of_the_dc_problem_runs_on():
+    """The same mesh and data inverted as a complex problem: the complex
+    factor (src/chol.f90) stops only on a zero pivot, so the run goes on; the
+    phase errors of 0 give infinite phase weights and a NaN phase RMS, as in
+    the reference's trace.  Lines 0-6 (to the second iteration's UP 1; 389
+    data excluded for polarity at IT 1) against inv.ctr."""
+    from titatest_gb300 import inversion as I
+    g, sv, data, cfg, kwn, kwnwi = dc_problem(False)
+    inv = I.Inversion(g, data, cfg, OracleBackend(g, sv, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink))
+    rows = inv.run(max_iterations=2)
+    gold = golden_rows("dc_problem")[:7]
+    compare_rows(gold, rows, inv.ncgmax)
+    assert math.isnan(rows[0].pharms) and rows[4].npol == 389

@@ -58,13 +58,19 @@ def _update_case(m, s, seed=11):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("ltri,lam,tol,phase_only", [(0, 300.0, 1e-8, False), (1, 300.0, 1e-8, False),
-                                                     (0, 3000.0, 1e-8, False), (1, 3000.0, 1e-8, False),
-                                                     (0, 30.0, 2e-5, False), (0, 300.0, 1e-8, True),
-                                                     (1, 300.0, 1e-8, True), (1, 3000.0, 1e-8, True)])
-def test_update_matches_oracle(gpu_lib, grid1, ltri, lam, tol, phase_only):
+@pytest.mark.parametrize("ltri,lam,tol,phase_only,dc", [(0, 300.0, 1e-8, False, False),
+                                                        (1, 300.0, 1e-8, False, False),
+                                                        (0, 3000.0, 1e-8, False, False),
+                                                        (1, 3000.0, 1e-8, False, False),
+                                                        (0, 30.0, 2e-5, False, False),
+                                                        (0, 300.0, 1e-8, True, False),
+                                                        (1, 300.0, 1e-8, True, False),
+                                                        (1, 3000.0, 1e-8, True, False),
+                                                        (1, 300.0, 1e-8, False, True)])
+def test_update_matches_oracle(gpu_lib, grid1, ltri, lam, tol, phase_only, dc):
     """phase_only: the final phase improvement (crgpu_update_fpi against the
-    oracle's restatement of cjggdc); the update is purely imaginary."""
+    oracle's restatement of cjggdc); the update is purely imaginary.  dc: the
+    DC update (crgpu_update_dc, cjggdc on Re(bvec)); the update is real."""
     from titatest_gb300 import PLAIN, CRMod
     s = grid1
     manz = s.grid.elanz
@@ -78,11 +84,13 @@ def test_update_matches_oracle(gpu_lib, grid1, ltri, lam, tol, phase_only):
             sm = R.bsmatmtri(s.grid, nb)
         kw = dict(lam=lam, eps=1e-4, ncgmax=manz // 10, step=1.0)
         pg, dg, cg, rg, ng = m.update(wmatd, wdfak, dat, sa, ltri, sm, nx=s.nx, nachbar=nb, par=par,
-                                      phase_only=phase_only, **kw)
+                                      phase_only=phase_only, dc=dc, **kw)
     po, do, co, ro, no = O.update(J, wmatd, wdfak, dat, sa, ltri, sm, nx=s.nx, nachbar=nb,
-                                  maxnk=s.grid.maxnk, par=par, phase_only=phase_only, **kw)
+                                  maxnk=s.grid.maxnk, par=par, phase_only=phase_only, dc=dc, **kw)
     if phase_only:
         assert np.all(dg.real == 0) and np.all(do.real == 0) and np.abs(do.imag).max() > 0
+    if dc:
+        assert np.all(dg.imag == 0) and np.all(do.imag == 0) and np.abs(do.real).max() > 0
     assert ng == no
     assert relerr(cg, co) < 1e-12
     assert relerr(dg, do) < tol

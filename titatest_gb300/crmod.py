@@ -139,6 +139,10 @@ class CRMod:
             raise ValueError("nodes and values differ in length")
         _check(self._h, lib().crgpu_set_boundary_values(self._h, len(nr), ptr(nr, i32p), ptr(vv, f64p)))
 
+    def set_dc(self, ldc: bool = True):
+        """DC mode (crgpu_set_dc): the real routines of CRTomo's ldc."""
+        _check(self._h, lib().crgpu_set_dc(self._h, int(bool(ldc))))
+
     def set_stream(self, stream_handle: int):
         """Issue the work on a caller-owned cudaStream_t (e.g.
         torch.cuda.current_stream().cuda_stream); 0 restores the own stream."""
@@ -279,9 +283,10 @@ class CRMod:
 
     # -- inversion update ---------------------------------------------------
     def update(self, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx=0, nachbar=None, lam=1.0, eps=1e-4,
-               ncgmax=100, step=1.0, par=None, phase_only: bool = False):
+               ncgmax=100, step=1.0, par=None, phase_only: bool = False, dc: bool = False):
         """src/update.f90 + cjggra on the sensitivities of the last sens(1);
-        phase_only: the final phase improvement (crgpu_update_fpi, cjggdc)."""
+        phase_only: the final phase improvement (crgpu_update_fpi, cjggdc);
+        dc: DC inversion (crgpu_update_dc, cjggdc)."""
         sv, g = self.survey, self.grid
         manz = g.elanz
         par = np.zeros(manz, np.complex128) if par is None else np.array(par, np.complex128)
@@ -290,7 +295,7 @@ class CRMod:
         cgres = np.zeros(ncgmax + 2, np.float32)
         ncg = C.c_int32(0)
         nb = np.ascontiguousarray(nachbar if nachbar is not None else np.zeros(1), np.int32)
-        fn = lib().crgpu_update_fpi if phase_only else lib().crgpu_update
+        fn = lib().crgpu_update_fpi if phase_only else lib().crgpu_update_dc if dc else lib().crgpu_update
         code = fn(
             self._h, ptr(np.ascontiguousarray(wmatd, np.float64), f64p),
             ptr(np.ascontiguousarray(wdfak, np.int32), i32p),

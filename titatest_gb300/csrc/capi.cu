@@ -339,6 +339,10 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
     if (d_sigma != c->d_sigma)  // keep the model of this forward (adjoint, refactorisation)
         CUCHECK(c, cudaMemcpyAsync(c->d_sigma, d_sigma, sizeof(double2) * c->hg.elanz, cudaMemcpyDeviceToDevice, c->st));
     d_sigma = c->d_sigma;
+    if (P.ldc) {  // the DC routines take DBLE(sigma) (src/kompadc.f90:114-119, src/bsendc.f90:172)
+        launch_real_part(c->d_sigma, c->hg.elanz, c->st);
+        c->stats.kernel_launches += 1;
+    }
     launch_adom(P, d_sigma, c->d_adom, c->st);
     c->stats.kernel_launches += 1;
     if (c->lsr) {
@@ -799,6 +803,14 @@ int crgpu_set_boundary_values(crgpu_ctx *c, int32_t rwdanz, const int32_t *rwdnr
     return 0;
 }
 
+int crgpu_set_dc(crgpu_ctx *c, int32_t ldc) {
+    if (!c || (ldc != 0 && ldc != 1)) return ERR_ARG;
+    drop_graph(c);
+    c->factors_resident = false;
+    c->P.ldc = ldc;
+    return 0;
+}
+
 int crgpu_set_stream(crgpu_ctx *c, void *stream) {
     if (!c) return ERR_ARG;
     c->st = stream ? (cudaStream_t)stream : c->own_st;
@@ -1247,7 +1259,7 @@ int crgpu_get_stats(const crgpu_ctx *c, crgpu_stats *s) {
     return 0;
 }
 
-static int update_common(crgpu_ctx *c, int phase_only, const double *wmatd, const int32_t *wdfak,
+static int update_common(crgpu_ctx *c, int part, const double *wmatd, const int32_t *wdfak,
                          const double *dat, const double *sigmaa, int32_t ltri, const double *smatm, int32_t nx,
                          const int32_t *nachbar, double lam, double eps, int32_t ncgmax, double step, double *par,
                          double *dpar, double *cgfac, float *cgres, int32_t *ncg) {
@@ -1316,7 +1328,7 @@ static int update_common(crgpu_ctx *c, int phase_only, const double *wmatd, cons
     a.dpar = (double2 *)(base + o_dpar);
     a.cgfac = (double *)(base + o_cg);
     a.work = (double2 *)(base + o_work);
-    a.phase_only = phase_only;
+    a.part = part;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -1369,7 +1381,7 @@ int crgpu_blam0_jtj(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, int
     a.wdfak = (const int32_t *)(base + o_wd);
     a.cgfac = (double *)(base + o_cg);
     a.work = (double2 *)(base + o_work);
-    a.phase_only = phase_only ? 1 : 0;
+    a.part = phase_only ? 1 : 0;  // Re(J) for the final phase improvement and for DC
     int rc = run_jhwj1(a, c->st, jtj);
     if (rc) return fail(c, rc, "blam0 kernels failed");
     return 0;
@@ -1388,6 +1400,14 @@ int crgpu_update_fpi(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, co
                      double lam, double eps, int32_t ncgmax, double step, double *par, double *dpar, double *cgfac,
                      float *cgres, int32_t *ncg) {
     return update_common(c, 1, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx, nachbar, lam, eps, ncgmax, step, par,
+                         dpar, cgfac, cgres, ncg);
+}
+
+int crgpu_update_dc(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, const double *dat,
+                    const double *sigmaa, int32_t ltri, const double *smatm, int32_t nx, const int32_t *nachbar,
+                    double lam, double eps, int32_t ncgmax, double step, double *par, double *dpar, double *cgfac,
+                    float *cgres, int32_t *ncg) {
+    return update_common(c, 2, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx, nachbar, lam, eps, ncgmax, step, par,
                          dpar, cgfac, cgres, ncg);
 }
 

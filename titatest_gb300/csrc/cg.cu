@@ -73,7 +73,7 @@ __global__ __launch_bounds__(kRedThreads) void k_colred(CGArgs a, int mode, cons
     double gr = 0.0, gi = 0.0, dg = 0.0;
     for (int i = threadIdx.x; i < a.nanz; i += kRedThreads) {
         double2 s = col[i];
-        if (a.phase_only) s.y = 0.0;  // DBLE(sens) of src/update.f90:187-192, 248-252
+        if (a.part) s.y = 0.0;  // DBLE(sens) / sensdc of src/update.f90:182-192, 243-252
         const double w = a.wmatd[i] * (double)a.wdfak[i];
         if (mode == 0) dg = fma(s.x * s.x + s.y * s.y, w, dg);
         const double2 v = vec[i];
@@ -132,7 +132,7 @@ __global__ __launch_bounds__(kRowTile) void k_jp_partial(CGArgs a, const double2
     double ar = 0.0, ai = 0.0;
     for (int j = j0; j < j1; j++) {
         double2 s = a.sens[(size_t)j * a.nanz + i];
-        if (a.phase_only) s.y = 0.0;  // bapdc, src/cg_mod.f90:226-230
+        if (a.part) s.y = 0.0;  // bapdc, src/cg_mod.f90:222-230
         const double2 v = q[j - j0];
         ar = fma(s.x, v.x, ar);
         ar = fma(-s.y, v.y, ar);
@@ -193,21 +193,23 @@ __global__ void k_sub(int n, const double2 *__restrict__ a, const double2 *__res
     out[i] = csub(a[i], b[i]);
 }
 
-// the phase-only CG runs on Im(bvec) (cjggdc, src/cg_mod.f90:160-164)
-__global__ void k_take_imag(int n, double2 *v) {
+// the real CG runs on Im(bvec) (part 1) or Re(bvec) (part 2) (cjggdc,
+// src/cg_mod.f90:160-164)
+__global__ void k_take_part(int n, double2 *v, int part) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    v[i] = cz(v[i].y, 0.0);
+    v[i] = cz(part == 1 ? v[i].y : v[i].x, 0.0);
 }
 
-// dpar = cgfac o dpar (phase only: i Re(dpar), src/update.f90:299-302), par += step dpar
+// dpar = cgfac o dpar (part 1: i Re(dpar), src/update.f90:299-302; part 2:
+// Re(dpar)), par += step dpar
 __global__ void k_final(int n, double2 *dpar, const double *__restrict__ cgfac, double step, double2 *par,
-                        int phase_only) {
+                        int part) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double2 d = dpar[i];
     double f = cgfac[i];
-    d = phase_only ? cz(0.0, d.x * f) : cz(d.x * f, d.y * f);
+    d = part == 1 ? cz(0.0, d.x * f) : part == 2 ? cz(d.x * f, 0.0) : cz(d.x * f, d.y * f);
     dpar[i] = d;
     double2 p = par[i];
     par[i] = cz(p.x + step * d.x, p.y + step * d.y);
@@ -259,8 +261,8 @@ int run_update(const CGArgs &a, cudaStream_t st, int *ncg_out, float *cgres_host
     k_rmul<<<nblk(manz, T), T, 0, st>>>(a, a.par, nullptr, bvec);
     k_sub<<<nblk(nanz, T), T, 0, st>>>(nanz, a.dat, a.sigmaa, dmf);
     k_colred<<<manz, kRedThreads, 0, st>>>(a, 0, dmf, bvec, a.cgfac, bvec);
-    if (a.phase_only) k_take_imag<<<nblk(manz, T), T, 0, st>>>(manz, bvec);
-    // cjggra (complex) or cjggdc (phase only: the same recursion on real vectors)
+    if (a.part) k_take_part<<<nblk(manz, T), T, 0, st>>>(manz, bvec, a.part);
+    // cjggra (complex) or cjggdc (parts 1, 2: the same recursion on real vectors)
     cudaMemsetAsync(a.dpar, 0, sizeof(double2) * manz, st);
     cudaMemcpyAsync(rvec, bvec, sizeof(double2) * manz, cudaMemcpyDeviceToDevice, st);
     cudaMemsetAsync(pvec, 0, sizeof(double2) * manz, st);
@@ -273,7 +275,7 @@ int run_update(const CGArgs &a, cudaStream_t st, int *ncg_out, float *cgres_host
         if (k == 1) {
             dr0 = dr * a.eps;
             beta = 0.0;
-            if (a.phase_only && dr <= dr0) break;  // cjggdc tests the first step too
+            if (a.part && dr <= dr0) break;  // cjggdc tests the first step too
         } else {
             if (dr <= dr0) break;
             beta = dr / dr1;
@@ -293,7 +295,7 @@ int run_update(const CGArgs &a, cudaStream_t st, int *ncg_out, float *cgres_host
     }
     if (k > a.ncgmax) ncg = a.ncgmax;
     cgres[0] = (float)ncg;
-    k_final<<<nblk(manz, T), T, 0, st>>>(manz, a.dpar, a.cgfac, a.step, a.par, a.phase_only);
+    k_final<<<nblk(manz, T), T, 0, st>>>(manz, a.dpar, a.cgfac, a.step, a.par, a.part);
     for (size_t q = 0; q < cgres.size(); q++) cgres_host[q] = cgres[q];
     cudaError_t e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaGetLastError();

@@ -12,6 +12,7 @@ struct DevProblem {
     int rw;               // padded row width of the lower pattern (row i at i*rw)
     int swrtr;
     int lsr;              // singularity removal
+    int ldc;              // DC (src/kompadc.f90 ... src/bsendc.f90): Re(sigma), pivots > 0 (src/choldc.f90)
     // launch choices of the autotuner (0: the built-in default)
     int tune_factor;      // mixed factor: 1 tensor cores, 2 SIMT register tiles, 3 SIMT shared-memory tiles
     int tune_ctas;        // SIMT factor: blocks per SM

@@ -70,7 +70,7 @@ __global__ __launch_bounds__(kPlainThreads) void k_factor_plain(DevProblem P, De
         for (int j = 0; j < n; j++) {
             if (tid == 0) {
                 double2 a = L[(size_t)j * W + mb];
-                if (!(cabsd(a) > 0.0)) bad = 28;  // src/chol.f90:67-71
+                if (!(cabsd(a) > 0.0) || (P.ldc && !(a.x > 0.0))) bad = 28;  // src/chol.f90:67-71, choldc.f90:66-70
                 double2 d = csqrtd(a);
                 L[(size_t)j * W + mb] = d;
                 double2 dinv = crecip(d);
@@ -146,13 +146,13 @@ struct MixCfg {
 // In-place L L^T of the 4x4 diagonal tile held in registers (rows j0..j0+3);
 // rows beyond n get a unit pivot.  Publishes L and 1/diag to shared memory.
 __device__ __forceinline__ void factor_diag4(float2 (&w)[4][4], int j0, int n, float2 (*Ld)[4], float2 *dinv,
-                                             int *bad) {
+                                             int *bad, int ldc) {
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         float2 d;
         if (j0 + q < n) {
             const float2 v = w[q][q];
-            if (!(cabsf_(v) > 0.f) || !isfinite(v.x) || !isfinite(v.y)) *bad = 28;
+            if (!(cabsf_(v) > 0.f) || !isfinite(v.x) || !isfinite(v.y) || (ldc && !(v.x > 0.f))) *bad = 28;
             d = csqrt_fast(v);
         } else {
             d = cf(1.f, 0.f);
@@ -242,7 +242,7 @@ __global__ __launch_bounds__(MixCfg<WP>::NT, 1) void k_factor_mixed(DevProblem P
             }
         }
         __syncthreads();
-        if (has && bi == 0 && bj == 0) factor_diag4(w, 0, n, Ldsh, dinvsh, &bad);
+        if (has && bi == 0 && bj == 0) factor_diag4(w, 0, n, Ldsh, dinvsh, &bad, P.ldc);
         if (ln >= 0) {
             // rows WP..WP+3 enter at block step 0: staged directly
             const int r = ln >> 3, e0 = ln & 7, rr = WP + r;
@@ -361,7 +361,7 @@ __global__ __launch_bounds__(MixCfg<WP>::NT, 1) void k_factor_mixed(DevProblem P
                 }
                 // the next pivot block: factor it now, off the critical path
                 const int Bn = (Bk + 1 == NB) ? 0 : Bk + 1;
-                if (bi == Bn && bj == Bn) factor_diag4(w, j + 4, n, Ldsh, dinvsh, &bad);
+                if (bi == Bn && bj == Bn) factor_diag4(w, j + 4, n, Ldsh, dinvsh, &bad, P.ldc);
             }
             if (ln >= 0) {
                 // staging warp: right-hand side update, clearing of the buffer

@@ -68,14 +68,14 @@ __device__ __forceinline__ void store_tile(float2 (*tl)[T], int t, const float2 
 // In-place L L^T of a 4x4 diagonal tile (rows j0..j0+3; rows beyond n get a
 // unit pivot); publishes L and 1/diag
 __device__ __forceinline__ void factor_diag4_s(float2 (&w)[4][4], int j0, int n, float2 (*Ld)[4], float2 *dinv,
-                                               int *bad) {
+                                               int *bad, int ldc) {
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         float2 d;
         if (j0 + q < n) {
             const float2 v = w[q][q];
             const float r2 = v.x * v.x + v.y * v.y;
-            if (!(r2 > 0.f) || !isfinite(r2)) *bad = 28;
+            if (!(r2 > 0.f) || !isfinite(r2) || (ldc && !(v.x > 0.f))) *bad = 28;
             d = csqrt_fast(v);
         } else {
             d = cf(1.f, 0.f);
@@ -161,7 +161,7 @@ __global__ __launch_bounds__(kSmemThreads, 1) void k_factor_mixed_smem(DevProble
         if (tid == 0) {  // tile (0, 0) is tile 0
             float2 w[4][4];
             load_tile(S.tiles, 0, w);
-            factor_diag4_s(w, 0, n, S.Ldsh, S.dinvsh, &S.bad);
+            factor_diag4_s(w, 0, n, S.Ldsh, S.dinvsh, &S.bad, P.ldc);
             store_tile(S.tiles, 0, w);
         }
         if (ln >= 0) {
@@ -282,7 +282,7 @@ __global__ __launch_bounds__(kSmemThreads, 1) void k_factor_mixed_smem(DevProble
 #pragma unroll
                         for (int b = 0; b < 4; b++) w[a][b] = cfmsf(w[a][b], la[a], lb[b]);
                 }
-                if (bi == Bn && bj == Bn) factor_diag4_s(w, j + 4, n, S.Ldsh, S.dinvsh, &S.bad);
+                if (bi == Bn && bj == Bn) factor_diag4_s(w, j + 4, n, S.Ldsh, S.dinvsh, &S.bad, P.ldc);
                 store_tile(S.tiles, t, w);
             }
             if (ln >= 0) {

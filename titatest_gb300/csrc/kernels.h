@@ -81,6 +81,9 @@ void launch_adjoint_lambda(const DevProblem &P, const DevBatch &B, int nrhs, dou
 void launch_adjoint_grad(const DevProblem &P, const double2 *kpot, const double2 *lambda, const int32_t *ebnd_ptr,
                          const int32_t *ebnd_list, double2 *grad, cudaStream_t st);
 
+// v.y = 0 (DC: the real parts of the conductivities)
+void launch_real_part(double2 *v, int n, cudaStream_t st);
+
 // update / CG (src/update.f90, src/cg_mod.f90); all pointers device memory
 struct CGArgs {
     int nanz, manz, ltri, nx, maxnk, ncgmax;
@@ -94,7 +97,8 @@ struct CGArgs {
     double2 *par, *dpar;    // in/out model, out update
     double *cgfac;          // out preconditioner
     double2 *work;          // update_work_bytes(nanz, manz)
-    int phase_only;         // final phase improvement (lfpi): Re(J), real CG on the phases
+    int part;               // 0 complex CG; real CG of cjggdc on Re(J): 1 the phases (final phase
+                            // improvement, lfpi), 2 the real parts (DC, ldc)
 };
 size_t update_work_bytes(int nanz, int manz);
 // runs update + cjggra; cgres (host, ncgmax+2 floats) receives the CG record

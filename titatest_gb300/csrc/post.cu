@@ -44,6 +44,7 @@ __global__ void k_bvolt(DevProblem P, const double2 *__restrict__ hpot, int mode
     };
     double2 d1 = hp(e4, e2), d2 = hp(e4, e1), d3 = hp(e3, e2), d4 = hp(e3, e1);
     double2 v = csub(csub(d1, d2), csub(d3, d4));
+    if (P.ldc) v.y = 0.0;  // dcmplx of the real DC voltage (src/bvolti.f90:56-62): -log(V < 0) = -ln|V| - i pi
     if (volt) volt[i] = v;
     if (mode == 0) {
         double kf = kfak ? kfak[i] : 1.0;
@@ -57,6 +58,15 @@ __global__ void k_bvolt(DevProblem P, const double2 *__restrict__ hpot, int mode
         }
         if (sigmaa) sigmaa[i] = cz(-log(a), -atan2(v.y, v.x));
     }
+}
+
+__global__ void k_real_part(double2 *v, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i].y = 0.0;
+}
+
+void launch_real_part(double2 *v, int n, cudaStream_t st) {
+    if (n > 0) k_real_part<<<(n + 127) / 128, 128, 0, st>>>(v, n);
 }
 
 void launch_bvolt(const DevProblem &P, const double2 *hpot, int mode, const double *kfak, double2 *volt,

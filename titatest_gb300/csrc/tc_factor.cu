@@ -125,7 +125,7 @@ __device__ __forceinline__ void handoff_sync() { asm volatile("bar.sync 2, 192;\
 // operations on the step's critical path; the square roots for the stored
 // Cholesky factor Lc = Lu D^{1/2} come after the MMAs are issued.
 __device__ __forceinline__ void pivot_ldlt(const float2 (&a)[4][4], int j, int n, float2 (&Lu)[4][4],
-                                           float2 (&dv)[4], float2 (&dinv)[4], int &bad) {
+                                           float2 (&dv)[4], float2 (&dinv)[4], int &bad, int ldc) {
     float2 dm[4][4];
 #pragma unroll
     for (int r = 0; r < 4; r++)
@@ -138,7 +138,7 @@ __device__ __forceinline__ void pivot_ldlt(const float2 (&a)[4][4], int j, int n
             d = cf(1.f, 0.f);
         } else {
             const float r2 = d.x * d.x + d.y * d.y;
-            if (!(r2 > 0.f) || !isfinite(r2)) bad = 28;
+            if (!(r2 > 0.f) || !isfinite(r2) || (ldc && !(d.x > 0.f))) bad = 28;
         }
         const float2 di = crecip_fast(d);
         dv[q] = d;
@@ -320,7 +320,7 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
                     for (int r = 0; r < 4; r++)
 #pragma unroll
                         for (int q = 0; q < 4; q++) d0[r][q] = S.dm[ob][r][q];
-                    pivot_ldlt(d0, j, n, Lu, dv, dinv, bad);
+                    pivot_ldlt(d0, j, n, Lu, dv, dinv, bad, P.ldc);
                 }
                 // ---- m = a Lu^{-T} and l = m D^{-1} of this slot's row (zero for the pivot rows)
                 float2 m[4], l[4];
@@ -505,7 +505,7 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
 #pragma unroll
                         for (int c = 0; c < 4; c++) d0[r][c] = S.dm[ob][r][c];
                     int bad_m = 0;  // reported by the panel, which factors the same block
-                    pivot_ldlt(d0, j, n, Lu, dv, dinv, bad_m);
+                    pivot_ldlt(d0, j, n, Lu, dv, dinv, bad_m, P.ldc);
                     // right-hand side of the pivot rows with the last step's update, then Lu^{-1}
                     float2 w[4];
 #pragma unroll

@@ -16,9 +16,10 @@ crgpu_update_fpi, the optional restart from the homogeneous phase, lffhom)
 with the error model of src/rdati.f90 (or individual errors), homogeneous or
 file start models (src/bsigm0.f90), structured (ltri 0) and triangular
 (ltri 1, 2) smoothness, a fixed lambda (llamf), the polarity checks
-(src/chkpol.f90, chkpo2 of src/dmisft.f90) and the stopping rules of
-src/inv.f90:560-640.  Robust inversion, difference inversion, prior models,
-data noise and DC inversion (ldc) raise NotImplementedError.
+(src/chkpol.f90, chkpo2 of src/dmisft.f90), the stopping rules of
+src/inv.f90:560-640, and DC inversion (ldc: the backends in DC mode,
+crgpu_set_dc, and the real update crgpu_update_dc).  Robust inversion,
+difference inversion, prior models and data noise raise NotImplementedError.
 """
 from __future__ import annotations
 
@@ -212,9 +213,10 @@ def make_data(strnr, vnr, bet, pha, cfg: CRTomoConfig) -> Data:
     stabw = 1e-2 * cfg.stabw0 + cfg.stabm0 / bet
     stabwp = (cfg.stabpA1 * bet ** cfg.stabpB + 1e-2 * cfg.stabpA2 * np.abs(pha) + cfg.stabp0) * 1e-3
     dat = -np.log(bet) - 1j * pha / 1e3
-    wr = 1.0 / stabw ** 2
-    wp = np.zeros_like(bet) if cfg.ldc else 1.0 / stabwp ** 2
-    wc = np.zeros_like(bet) if cfg.ldc else 1.0 / (stabw ** 2 + stabwp ** 2)
+    with np.errstate(divide="ignore"):
+        wr = 1.0 / stabw ** 2
+        wp = np.zeros_like(bet) if cfg.ldc else 1.0 / stabwp ** 2
+        wc = np.zeros_like(bet) if cfg.ldc else 1.0 / (stabw ** 2 + stabwp ** 2)
     return Data(strnr=np.asarray(strnr, np.int32), vnr=np.asarray(vnr, np.int32), dat=dat, wmatdr=wr,
                 wmatdp=wp, wmatd_cri=wc)
 
@@ -270,10 +272,10 @@ def read_data(path: str, cfg: CRTomoConfig, eanz: int) -> Data:
             raise formats.CRError(46, f"datum {i + 1}: electrode number")
         strnr[i], vnr[i] = s, v
         dat[i] = complex(-math.log(bet), -pha / 1e3)
-        wr[i] = 1.0 / stabw ** 2
-        if not cfg.ldc:
-            wc[i] = 1.0 / (stabw ** 2 + stabwp ** 2)
-            wp[i] = 1.0 / stabwp ** 2
+        wr[i] = _q(1.0, stabw ** 2)
+        if not cfg.ldc:  # a phase error of 0 gives an infinite weight, as in the reference
+            wc[i] = _q(1.0, stabw ** 2 + stabwp ** 2)
+            wp[i] = _q(1.0, stabwp ** 2)
     if lindiv:
         t = rec._tokens(rec.read_line())
         sw = formats._f(t[0])
@@ -339,8 +341,9 @@ def dmisft(dat, sigmaa, wmatd, wmatdr, wmatdp, lfpi: bool = False, lpol: bool = 
         psi = math.sqrt(wmatd[i]) * (abs(cdum.imag) if lfpi else abs(cdum))
         idum += wdlok
         nrmsd += psi * psi * wdlok
-        betrms += wmatdr[i] * wdlok * cdum.real * cdum.real
-        pharms += wmatdp[i] * wdlok * cdum.imag * cdum.imag
+        with np.errstate(invalid="ignore"):  # an infinite weight times 0 is NaN, as in the reference
+            betrms += float(np.float64(wmatdr[i]) * wdlok * cdum.real * cdum.real)
+            pharms += float(np.float64(wmatdp[i]) * wdlok * cdum.imag * cdum.imag)
     if idum == 0:
         raise formats.CRError(99, "no datum left for the misfit")
     return Misfit(math.sqrt(nrmsd / idum), math.sqrt(betrms / idum), math.sqrt(pharms / idum), len(dat) - idum)
@@ -441,11 +444,13 @@ class DeviceBackend:
     """The heavy steps on the GPU through the C ABI (one context)."""
 
     def __init__(self, grid, survey, kwn, kwnwi, swrtr: int, lsink: bool, nsink: int, precision: int,
-                 refinement: Optional[tuple] = None):
+                 refinement: Optional[tuple] = None, ldc: bool = False):
         from .crmod import CRMod
         self.m = CRMod(grid, survey, kwn, kwnwi, swrtr=swrtr, lsink=lsink, nsink=nsink, precision=precision)
         if refinement is not None:
             self.m.set_refinement(*refinement)
+        if ldc:
+            self.m.set_dc(True)
 
     def forward(self, sigma: np.ndarray) -> np.ndarray:
         return self.m.forward(sigma, volt_mode=1)["sigmaa"]
@@ -454,10 +459,10 @@ class DeviceBackend:
         self.m.sens_on_device(1)
 
     def update(self, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx, nachbar, lam, eps, ncgmax, step, par,
-               phase_only=False):
+               phase_only=False, dc=False):
         p, dp, cgfac, cgres, ncg = self.m.update(wmatd, wdfak, dat, sigmaa, ltri, smatm, nx=nx, nachbar=nachbar,
                                                  lam=lam, eps=eps, ncgmax=ncgmax, step=step, par=par,
-                                                 phase_only=phase_only)
+                                                 phase_only=phase_only, dc=dc)
         return dp, ncg
 
     def jtj(self, wmatd, wdfak, phase_only: bool) -> np.ndarray:
@@ -527,8 +532,8 @@ class Inversion:
 
     def __init__(self, grid, data: Data, cfg: CRTomoConfig, backend, sigma_start=None,
                  lamnull: Optional[tuple] = None, phase_stage: bool = True, ncgmax: Optional[int] = None):
-        if cfg.lrobust or cfg.ldiff or cfg.ldc:
-            raise NotImplementedError("robust, difference and DC inversion are not built")
+        if cfg.lrobust or cfg.ldiff:
+            raise NotImplementedError("robust and difference inversion are not built")
         if cfg.ltri not in (0, 1, 2):
             raise NotImplementedError(f"regularisation ltri = {cfg.ltri} is not built")
         self.grid, self.data, self.cfg, self.b = grid, data, cfg, backend
@@ -653,11 +658,14 @@ class Inversion:
             # modelling (src/inv.f90:342-503)
             try:
                 self.sigmaa = self._forward(self.sigma)
-            except Exception:
-                if sgmaa2 is None:
+            except Exception as e:
+                # a zero voltage (src/bvolti.f90, errnr 82) ends the run with the
+                # last model (src/inv.f90:495-503); any other error -- e.g. a
+                # non-positive DC pivot, errnr 28 -- aborts it, as in the reference
+                if getattr(e, "errnr", None) != 82 or sgmaa2 is None:
                     raise
                 self.sigma, self.sigmaa = sigma2, sgmaa2
-                self.status = "forward"
+                self.status = "82"
                 break
             setup = self.lsetup or self.lsetip
             if setup:
@@ -747,7 +755,8 @@ class Inversion:
                     if search:
                         if self.lsetup or self.lsetip:
                             self.lam = blam0(cfg, self.lamnull_cri, self.lamnull_fpi, self.manz, self.nanz,
-                                             self.lfpi, b.jtj, self.wmatd, self.wdfak)
+                                             self.lfpi, lambda w, d, p: b.jtj(w, d, p or cfg.ldc), self.wmatd,
+                                             self.wdfak)
                             lamalt = self.lam
                         else:
                             dlalt = dlam
@@ -790,7 +799,7 @@ class Inversion:
                 dpar2, ncg2 = dpar, self.ncg
                 dpar, self.ncg = b.update(self.wmatd, self.wdfak, self.dat, self.sigmaa, cfg.ltri, self.smatm,
                                           cfg.nx, self.nachbar, self.lam, self.eps, self.ncgmax, 1.0, par,
-                                          phase_only=self.lfpi)
+                                          phase_only=self.lfpi, dc=cfg.ldc)
                 dpar = np.array(dpar, np.complex128)
             else:
                 dpar, self.ncg = dpar2, ncg2
@@ -846,7 +855,7 @@ def run_crtomo(exe_dir: str, precision: int = 1, refinement=(8, 1e-10), write: b
     sigma_start = None
     if not cfg.lrho0 and cfg.dm0:
         sigma_start = formats.read_rho(p(cfg.dm0), grid.elanz)
-    b = DeviceBackend(grid, survey, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink, precision, refinement)
+    b = DeviceBackend(grid, survey, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink, precision, refinement, cfg.ldc)
     try:
         if cfg.lrandb2:
             b.m.set_boundary_values(*formats.read_boundary_values(p(cfg.drandb), grid.sanz))
