@@ -8,7 +8,9 @@ Run in a container where the reference checkout is present:
 Forward cases (<case>/): the CRMod inputs (elem.dat, elec.dat, rho.dat,
 crmod.cfg) and the CRMod output volt.dat of a reference tomodir.  The
 measurement configurations are the (strnr, vnr) columns of volt.dat.
-Inversion cases add the tomodir's crtomo.cfg and CRTomo's inv.ctr.
+Inversion cases add the tomodir's crtomo.cfg, CRTomo's inv.ctr and the
+model and data files written after iteration 1 (rho01.mag, rho01.pha,
+volt01.dat; minimal also rho02.mag).
 
 CutMcK cases (cutmck_<case>/): the grid before (elem.dat.orig, elec.dat.orig)
 and after (elem.dat, elec.dat) the reference's Cuthill-McKee renumbering.
@@ -64,8 +66,10 @@ def main(ref: str):
     for name, d in INVERSION.items():
         out = os.path.join(here, name)
         src = os.path.join(ref, d)
-        for f in ("exe/crtomo.cfg", "inv/inv.ctr"):
+        for f in ("exe/crtomo.cfg", "inv/inv.ctr", "inv/rho01.mag", "inv/rho01.pha", "inv/volt01.dat"):
             shutil.copyfile(os.path.join(src, f), os.path.join(out, os.path.basename(f)))
+        if name == "minimal":
+            shutil.copyfile(os.path.join(src, "inv/rho02.mag"), os.path.join(out, "rho02.mag"))
     out = os.path.join(here, "dc_problem")
     os.makedirs(out, exist_ok=True)
     src = os.path.join(ref, DC_PROBLEM)

@@ -143,3 +143,31 @@ def golden_rows_file(case, name):
             if t and t[0] == "IT" and len(t) == 6:
                 rows.append((t[0], int(t[1]), float(t[2]), float(t[3]), t[4], int(t[5])))
     return rows
+
+
+def check_models(case, inv, log10_tol=5e-4, pha_tol_mrad=0.05, volt_tol=1e-3):
+    """The accepted models against the reference's rhoNN.mag (log10 |rho|
+    per element; the files print 9 digits), rhoNN.pha (phase of rho, mrad)
+    and volt01.dat (|R| of the model after iteration 1) of the case."""
+    from titatest_gb300 import inversion as I
+    d = os.path.join(GOLDEN, case)
+    checked = 0
+    for nn in (1, 2):
+        path = os.path.join(d, f"rho{nn:02d}.mag")
+        if not os.path.exists(path):
+            continue
+        m = [mm for mm in inv.models if mm["it"] == nn][0]
+        rho = 1.0 / m["sigma"]
+        n, rms, x, y, lg = I.read_model_mag(path)
+        assert n == len(rho)
+        assert np.abs(np.log10(np.abs(rho)) - lg).max() < log10_tol, (case, nn)
+        pha_path = os.path.join(d, f"rho{nn:02d}.pha")
+        if os.path.exists(pha_path):
+            _, _, _, _, ph = I.read_model_mag(pha_path)
+            assert np.abs(1e3 * np.angle(rho) - ph).max() < pha_tol_mrad, (case, nn)
+        checked += 1
+    m1 = [mm for mm in inv.models if mm["it"] == 1][0]
+    vals = np.loadtxt(os.path.join(d, "volt01.dat"), skiprows=1)
+    ours = np.exp(-m1["sigmaa"].real)
+    assert np.abs(ours / vals[:, 2] - 1).max() < volt_tol
+    return checked

@@ -7,7 +7,7 @@ trials whose CG stops on its residual test the most (mixed_surf UP 9: 1.4% in
 misfit, 6 CG steps), inside the tolerances for such trials."""
 import pytest
 
-from inversion_backend import compare_rows, golden_rows, inversion_case
+from inversion_backend import check_models, compare_rows, golden_rows, inversion_case
 
 pytestmark = pytest.mark.gpu
 
@@ -31,6 +31,7 @@ def test_gpu_inversion_reproduces_reference_trace_minimal(gpu_lib, prec):
     assert len(rows) == len(gold) == 25
     compare_rows(gold, rows, inv.ncgmax)
     assert inv.stage_start == 21 and inv.status == "81"
+    assert check_models("minimal", inv) == 2
 
 
 @pytest.mark.parametrize("prec", [0, 1])
@@ -39,6 +40,7 @@ def test_gpu_inversion_reproduces_reference_trace_mixed_surf(gpu_lib, prec):
     gold = golden_rows("mixed_surf")[:15]
     assert len(rows) == 15 and inv.status == "max_iterations"
     compare_rows(gold, rows, inv.ncgmax)
+    assert check_models("mixed_surf", inv) == 1
 
 
 def test_run_crtomo_on_a_tomodir(gpu_lib, tmp_path):
@@ -63,6 +65,9 @@ def test_run_crtomo_on_a_tomodir(gpu_lib, tmp_path):
     assert len(lines) == 25 and lines[0].split()[:3] == ["IT", "0", "111.9"]
     sig = F.read_rho(str(tmp_path / "inv" / "rho.dat"), inv.grid.elanz)
     assert np.max(np.abs(sig / inv.sigma - 1)) < 1e-8
+    mine = I.read_model_mag(str(tmp_path / "inv" / "rho02.mag"))
+    ref = I.read_model_mag(os.path.join(src, "rho02.mag"))
+    assert np.abs(mine[4] - ref[4]).max() < 5e-4
 
 
 @pytest.mark.parametrize("prec", [0, 1])

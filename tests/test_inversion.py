@@ -3,6 +3,9 @@ src/dmisft.f90, src/blam0.f90, src/parfit.f90, src/brough_mod.f90) on the
 oracle's forward, Jacobian and update, against the reference's own control
 output inv.ctr (src/kont2.f90).
 
+Where the reference's rhoNN.mag / rhoNN.pha / volt01.dat are in the
+fixtures, the accepted models are compared element by element as well.
+
 minimal: the whole run -- 21 lines of the complex stage over two accepted
 models (the lambda search, a failed trial, the half step and the parabolic
 step fit), then the final phase improvement with its restart from the
@@ -18,8 +21,8 @@ import pytest
 
 import math
 
-from inversion_backend import (OracleBackend, compare_rows, dc_problem, golden_rows, golden_rows_file,
-                               inversion_case)
+from inversion_backend import (OracleBackend, check_models, compare_rows, dc_problem, golden_rows,
+                               golden_rows_file, inversion_case)
 
 
 def _run(case, max_iterations=None):
@@ -30,7 +33,7 @@ def _run(case, max_iterations=None):
     return inv, rows
 
 
-def test_inversion_loop_reproduces_reference_trace_minimal():
+def test_inversion_loop_reproduces_reference_trace_minimal(tmp_path):
     inv, rows = _run("minimal")
     gold = golden_rows("minimal")
     assert len(gold) == 25 and len(rows) == 25
@@ -39,6 +42,18 @@ def test_inversion_loop_reproduces_reference_trace_minimal():
     # the final phase improvement starts at line 21 (lffhom: phases reset);
     # with phase data of 0 its misfit is the floor 0.98 and it stops at once
     assert inv.stage_start == 21 and inv.status == "81"
+    # the models after iterations 1 and 2 element by element (rho01/02.mag)
+    assert check_models("minimal", inv) == 2
+    # the files of src/wout.f90, read back against the reference's
+    from conftest import GOLDEN
+    from titatest_gb300 import inversion as I
+    I.write_models(inv, str(tmp_path))
+    mine = I.read_model_mag(str(tmp_path / "rho01.mag"))
+    ref = I.read_model_mag(f"{GOLDEN}/minimal/rho01.mag")
+    assert mine[0] == ref[0] and abs(mine[1] / ref[1] - 1) < 2e-3
+    assert np.array_equal(mine[2], ref[2]) and np.array_equal(mine[3], ref[3])
+    assert np.abs(mine[4] - ref[4]).max() < 5e-4
+    assert sorted(p.name for p in tmp_path.iterdir())[:3] == ["rho00.mag", "rho00.modl", "rho00.pha"]
 
 
 def test_inversion_loop_reproduces_reference_trace_mixed_surf():
@@ -46,6 +61,7 @@ def test_inversion_loop_reproduces_reference_trace_mixed_surf():
     gold = golden_rows("mixed_surf")[:15]
     assert len(rows) == 15 and inv.status == "max_iterations"
     compare_rows(gold, rows, inv.ncgmax)
+    assert check_models("mixed_surf", inv) == 1  # magnitude and phase of the model after iteration 1
 
 
 def test_crtomo_cfg_and_error_model():

@@ -580,6 +580,7 @@ class Inversion:
         self.status = ""
         self.phase_stage = phase_stage  # run the final phase improvement (lfphai)
         self.stage_start = None         # first row of the phase stage
+        self.models: List[dict] = []    # every accepted model (an IT / PIT line), for write_models
 
     # -- pieces -----------------------------------------------------------------
     def _forward(self, sigma):
@@ -617,6 +618,9 @@ class Inversion:
 
     def _kont2(self, lsetup: bool):
         p = "P" if self.lfpi else ""
+        if lsetup or (self.llam and not self.lstep):
+            self.models.append(dict(it=self.it, sigma=self.sigma.copy(), sigmaa=self.sigmaa.copy(),
+                                    wdfak=self.wdfak.copy(), betrms=self.betrms, pharms=self.pharms))
         if lsetup:
             self.rows.append(Row(p + "IT", self.it, self.nrmsd, betrms=self.betrms, pharms=self.pharms,
                                  npol=self.npol, first=True))
@@ -829,12 +833,67 @@ def format_rows(rows: List[Row]) -> str:
     return "\n".join(out) + "\n"
 
 
+def _f4(x) -> str:
+    """A REAL*4 value as list-directed output prints it: 9 significant digits."""
+    x = float(np.float32(x))
+    if x == 0.0 or 1e-1 <= abs(x) < 1e8:
+        return f"{x:.9g}"
+    return f"{x:.8E}"
+
+
+def write_models(inv: "Inversion", ramd: str, ldc: bool = False):
+    """The files src/wout.f90 writes for every accepted model NN: rhoNN.mag
+    (centroid x, y, log10 |rho|; header elanz and the magnitude RMS),
+    rhoNN.pha (phase of rho in mrad; header the phase RMS), rhoNN.modl
+    (|rho|-like 1/Re(sigma) and the phase), rhoNN.sig (sigma) and voltNN.dat
+    (strnr, vnr, |R|, phase in mrad, wdfak).  Numbers in list-directed
+    REAL*4 style; the layout, not the bytes, of the reference's files."""
+    os.makedirs(ramd, exist_ok=True)
+    g = inv.grid
+    cx, cy = R._centroids(g)
+    for m in inv.models:
+        nn = f"{m['it']:02d}"
+        rho = 1.0 / m["sigma"]
+        with open(os.path.join(ramd, f"rho{nn}.mag"), "w") as fh:
+            fh.write(f"{g.elanz:12d} \t {m['betrms']!r}\n")
+            for i in range(g.elanz):
+                fh.write(f"  {_f4(cx[i])}  {_f4(cy[i])}  {_f4(math.log10(abs(rho[i])))}\n")
+        with open(os.path.join(ramd, f"rho{nn}.modl"), "w") as fh:
+            fh.write(f"{g.elanz:7d}\n")
+            for i in range(g.elanz):
+                fh.write(f" {1.0 / m['sigma'][i].real:12.4G} {1e3 * math.atan2(rho[i].imag, rho[i].real):12.4G}\n")
+        if not ldc:
+            with open(os.path.join(ramd, f"rho{nn}.pha"), "w") as fh:
+                fh.write(f"{g.elanz:12d} \t {m['pharms']!r}\n")
+                for i in range(g.elanz):
+                    fh.write(f"  {_f4(cx[i])}  {_f4(cy[i])}  {_f4(1e3 * math.atan2(rho[i].imag, rho[i].real))}\n")
+            with open(os.path.join(ramd, f"rho{nn}.sig"), "w") as fh:
+                fh.write(f"{g.elanz:12d} {m['betrms']!r} {m['pharms']!r}\n")
+                for s in m["sigma"]:
+                    fh.write(f"  {_f4(s.real)}  {_f4(s.imag)}\n")
+        with open(os.path.join(ramd, f"volt{nn}.dat"), "w") as fh:
+            fh.write(f"{len(m['sigmaa']):12d}\n")
+            for i, sa in enumerate(m["sigmaa"]):
+                cols = [_f4(1.0 / math.exp(sa.real))] + ([] if ldc else [_f4(-1e3 * sa.imag)])
+                fh.write(f"{int(inv.data.strnr[i]):12d}{int(inv.data.vnr[i]):12d}  " + "  ".join(cols)
+                         + f"{int(m['wdfak'][i]):12d}\n")
+
+
+def read_model_mag(path: str):
+    """(elanz, rms, x, y, log10 |rho|) of a rhoNN.mag file."""
+    with open(path) as fh:
+        head = fh.readline().split()
+        vals = np.loadtxt(fh)
+    return int(head[0]), float(head[1]), vals[:, 0], vals[:, 1], vals[:, 2]
+
+
 def run_crtomo(exe_dir: str, precision: int = 1, refinement=(8, 1e-10), write: bool = True):
     """CRTomo's complex stage on a tomodir: reads exe_dir/crtomo.cfg and its
     inputs, inverts on the GPU and (write) puts the IT/UP lines into
-    <ramd>/inv.ctr and the final model into <ramd>/rho.dat (magnitude in
-    ohm m and phase in mrad, as src/rsigma.f90 reads a model).  Returns the
-    Inversion."""
+    <ramd>/inv.ctr, the final model into <ramd>/rho.dat (magnitude in ohm m
+    and phase in mrad, as src/rsigma.f90 reads a model) and every accepted
+    model with its data into rhoNN.* / voltNN.dat (write_models).  Returns
+    the Inversion."""
     cfg = read_crtomo_cfg(os.path.join(exe_dir, "crtomo.cfg"))
 
     def p(x):
@@ -871,4 +930,5 @@ def run_crtomo(exe_dir: str, precision: int = 1, refinement=(8, 1e-10), write: b
         mag = 1.0 / np.abs(inv.sigma)
         pha = -1e3 * np.angle(inv.sigma)  # resistivity phase in mrad
         formats.write_rho(os.path.join(ramd, "rho.dat"), mag, pha)
+        write_models(inv, ramd, cfg.ldc)
     return inv
