@@ -115,6 +115,51 @@ __global__ __launch_bounds__(kRedThreads) void k_colred(CGArgs a, int mode, cons
     }
 }
 
+// wv_i = w_i v_i (w_i = wmatd_i wdfak_i), once per CG step for k_colred_bb
+__global__ void k_weight(CGArgs a, const double2 *__restrict__ v, double2 *__restrict__ wv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nanz) return;
+    const double w = a.wmatd[i] * (double)a.wdfak[i];
+    wv[i] = cz(w * v[i].x, w * v[i].y);
+}
+
+// k_colred mode 1 (src/cg_mod.f90 bb) on a weighted vector: four FP64 FMAs
+// per element of J, the FP64 pipe's minimum for a complex product
+//   out_j = (sum_i conj(s_ij) wv_i + lam rm_j) cgfac_j
+__global__ __launch_bounds__(kRedThreads) void k_colred_bb(CGArgs a, const double2 *__restrict__ wv,
+                                                           const double2 *rm, double2 *out) {  // out may alias rm
+    const int j = blockIdx.x;
+    const double2 *col = a.sens + (size_t)j * a.nanz;
+    double gr = 0.0, gi = 0.0;
+    for (int i = threadIdx.x; i < a.nanz; i += kRedThreads) {
+        double2 s = col[i];
+        if (a.part) s.y = 0.0;
+        const double2 v = wv[i];
+        gr = fma(s.x, v.x, gr);
+        gr = fma(s.y, v.y, gr);
+        gi = fma(s.x, v.y, gi);
+        gi = fma(-s.y, v.x, gi);
+    }
+    __shared__ double red[2][kRedThreads / 32];
+    gr = warp_sum(gr);
+    gi = warp_sum(gi);
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    if (lane == 0) {
+        red[0][wl] = gr;
+        red[1][wl] = gi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        gr = gi = 0.0;
+        for (int q = 0; q < kRedThreads / 32; q++) {
+            gr += red[0][q];
+            gi += red[1][q];
+        }
+        const double cf = a.cgfac[j];
+        out[j] = cz((gr + a.lam * rm[j].x) * cf, (gi + a.lam * rm[j].y) * cf);
+    }
+}
+
 // partial[chunk][i] = sum_{j in chunk} s_ij (cgfac_j p_j)   (src/cg_mod.f90:520-545)
 __global__ __launch_bounds__(kRowTile) void k_jp_partial(CGArgs a, const double2 *__restrict__ p,
                                                          double2 *__restrict__ partial) {
@@ -285,7 +330,8 @@ int run_update(const CGArgs &a, cudaStream_t st, int *ncg_out, float *cgres_host
         k_jp_partial<<<g1, kRowTile, 0, st>>>(a, pvec, partial);
         k_jp_reduce<<<nblk(nanz, T), T, 0, st>>>(a, nchunk, partial, ap);
         k_rmul<<<nblk(manz, T), T, 0, st>>>(a, pvec, a.cgfac, bvec);
-        k_colred<<<manz, kRedThreads, 0, st>>>(a, 1, ap, bvec, a.cgfac, bvec);
+        k_weight<<<nblk(nanz, T), T, 0, st>>>(a, ap, dmf);  // d - f is not needed after the right-hand side
+        k_colred_bb<<<manz, kRedThreads, 0, st>>>(a, dmf, bvec, bvec);
         dr1 = dot(pvec, bvec);
         const double alpha = dr / dr1;
         k_axpy<<<nblk(manz, T), T, 0, st>>>(manz, a.dpar, a.dpar, alpha, pvec);

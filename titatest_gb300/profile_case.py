@@ -7,6 +7,9 @@ A small driver for profilers (ncu) and quick timing:
 
 --batch limits the number of band systems per batch (one factor launch per
 batch), so a profiler can capture a single launch of known size.
+--update-steps N adds the CRTomo Jacobian (bsensi, kept on the device) and one
+Gauss-Newton update with at most N CG steps (structured smoothness) on data
+that are the model's response times 1.03: the CG kernels for a profiler.
 """
 from __future__ import annotations
 
@@ -26,6 +29,7 @@ def main(argv=None):
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--sens", action="store_true")
     ap.add_argument("--refine-tol", type=float, default=1e-8)
+    ap.add_argument("--update-steps", type=int, default=0)
     a = ap.parse_args(argv)
     s = synth.make(a.config)
     prec = MIXED if a.precision == "mixed" else PLAIN
@@ -47,6 +51,18 @@ def main(argv=None):
                 msg += f", sens {m.stats()['ms_sens']:.1f} ms, |J|max {np.abs(J).max():.3e}"
             print(msg, flush=True)
         assert np.all(np.isfinite(out["volt"]))
+        if a.update_steps:
+            from . import regularization as R
+            sa = m.forward(s.sigma, volt_mode=1)["sigmaa"]
+            m.sens_on_device(1)
+            dat = sa - np.log(1.03)
+            w = np.full(len(sa), 1.0 / 0.03 ** 2)
+            sm = R.bsmatmreg(s.grid, s.nx, s.nz)
+            t = time.time()
+            _, dpar, _, _, ncg = m.update(w, np.ones(len(sa), np.int32), dat, sa, 0, sm, nx=s.nx, lam=300.0,
+                                          eps=1e-4, ncgmax=a.update_steps, par=np.log(s.sigma))
+            print(f"update {1e3 * (time.time() - t):.1f} ms, {ncg} CG steps, |dpar|max {np.abs(dpar).max():.3e}",
+                  flush=True)
 
 
 if __name__ == "__main__":
