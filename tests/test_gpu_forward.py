@@ -230,3 +230,38 @@ def test_wide_band_mixed_factor_shared_memory_window(gpu_lib):
         lo = max(0, g.mb - i)
         assert relerr(a[i, lo:], a_ref[i, lo:]) < 1e-3, i
     assert relerr(vm, vp) < MIXED_VOLT_TOL
+
+
+def test_run_tomodir_writes_crmod_outputs(gpu_lib, tmp_path):
+    """CRMod on a tomodir (crmod.run_tomodir): volt.dat against the reference's
+    golden, and with potentials and sensitivities switched on, one pot and one
+    sens file per measurement (src/bpot.f90, src/wpot.f90, src/wsens.f90)."""
+    import os
+    import shutil
+
+    from conftest import GOLDEN
+    from titatest_gb300 import PLAIN
+    from titatest_gb300 import formats as F
+    from titatest_gb300.crmod import run_tomodir
+    src = os.path.join(GOLDEN, "minimal")
+    for sub in ("exe", "grid", "rho", "config", "mod"):
+        os.makedirs(tmp_path / sub)
+    shutil.copyfile(os.path.join(src, "elem.dat"), tmp_path / "grid" / "elem.dat")
+    shutil.copyfile(os.path.join(src, "elec.dat"), tmp_path / "grid" / "elec.dat")
+    shutil.copyfile(os.path.join(src, "rho.dat"), tmp_path / "rho" / "rho.dat")
+    s, v, bet, pha = F.read_volt(os.path.join(src, "volt.dat"))
+    F.write_config(str(tmp_path / "config" / "config.dat"), s, v)
+    cfg = open(os.path.join(src, "crmod.cfg")).read().splitlines()
+    cfg[5] = "T                ! potentials ?"
+    cfg[9] = "T               ! sensitivities ?"
+    (tmp_path / "exe" / "crmod.cfg").write_text("\n".join(cfg) + "\n")
+    out = run_tomodir(str(tmp_path / "exe"), precision=PLAIN)
+    s2, v2, bet2, pha2 = F.read_volt(str(tmp_path / "mod" / "volt.dat"))
+    assert np.array_equal(s2, s) and np.array_equal(v2, v)
+    assert np.max(np.abs(bet2 / bet - 1)) < 1e-6  # real*4 files on both sides
+    pots = sorted(os.listdir(tmp_path / "mod" / "pot"))
+    sens = sorted(os.listdir(tmp_path / "mod" / "sens"))
+    assert len(pots) == len(sens) == len(s) and pots[0] == "pot01.dat" and sens[-1] == "sens12.dat"
+    J = out["sens"]
+    body = np.loadtxt(tmp_path / "mod" / "sens" / "sens12.dat", skiprows=1)
+    assert np.allclose(body[:, 2] + 1j * body[:, 3], J[11], rtol=1e-6, atol=1e-7 * np.abs(J[11]).max())

@@ -129,3 +129,35 @@ def test_boundary_values_file(tmp_path):
     with pytest.raises(F.CRError) as ei:
         F.read_boundary_values(str(p), 8)
     assert ei.value.errnr == 30
+
+
+def test_potential_and_sensitivity_files(tmp_path):
+    """src/wpot.f90 / src/wsens.f90 layouts: numbered names, x y Re Im lines
+    (the potential of each measurement's current pair; J per element with
+    the |sum| / phase header), read back against the arrays written."""
+    from conftest import load_case
+    from oracle import oracle as O
+    from titatest_gb300 import regularization as R
+    assert F.numbered_path("../mod/pot/pot.dat", 7, 12) == "../mod/pot/pot07.dat"
+    assert F.numbered_path("sens/sens.dat", 7, 1199) == "sens/sens0007.dat"
+    g, sv, sig, cfg, _ = load_case("minimal")
+    P = O.Problem(g, sv)
+    kwn, kwnwi = P.rwaven()
+    hp = P.rtrafo(P.forward(sig, kwn, kwnwi), kwnwi)
+    F.write_potentials(str(tmp_path / "pot" / "pot.dat"), hp, sv.strnr, np.ones(sv.nanz), g)
+    vals = np.loadtxt(tmp_path / "pot" / "pot03.dat")
+    e1, e2 = sv.strnr[2] % 10000, sv.strnr[2] // 10000
+    want = hp[e2 - 1] - hp[e1 - 1]
+    x, y = g.node_xy()
+    assert vals.shape == (g.sanz, 4) and np.allclose(vals[:, 0], x.astype(np.float32))
+    assert np.allclose(vals[:, 2] + 1j * vals[:, 3], want, rtol=1e-6, atol=1e-7 * np.abs(want).max())
+    rng = np.random.default_rng(1)
+    J = rng.normal(size=(sv.nanz, g.elanz)) + 1j * rng.normal(size=(sv.nanz, g.elanz))
+    cx, cy = R._centroids(g)
+    F.write_sensitivities(str(tmp_path / "sens" / "sens.dat"), J, cx, cy)
+    with open(tmp_path / "sens" / "sens05.dat") as fh:
+        head = [float(t) for t in fh.readline().split()]
+        body = np.loadtxt(fh)
+    s = J[4].sum()
+    assert abs(head[0] / abs(s) - 1) < 1e-6 and abs(head[1] - 1e3 * np.angle(s)) < 1e-3
+    assert np.allclose(body[:, 2] + 1j * body[:, 3], J[4], rtol=1e-6)

@@ -320,12 +320,19 @@ def run_tomodir(exe_dir: str, precision: int = PLAIN, write: bool = True):
         if td.boundary_values is not None:
             m.set_boundary_values(*td.boundary_values)
         kfak = m.bkfak() if (cfg.wkfak and td.grid.relanz and 11 in set(td.grid.typ.tolist())) else None
-        out = m.forward(td.sigma, kfak=kfak)
+        out = m.forward(td.sigma, kfak=kfak, hpot=bool(write and cfg.lpot))
+        if write and cfg.lpot:  # src/fem.f90:409-412
+            formats.write_potentials(os.path.normpath(os.path.join(exe_dir, cfg.dpot)), out["hpot"],
+                                     td.survey.strnr, np.asarray(td.survey.strom), td.grid)
         if write and cfg.lvolt:
             formats.write_volt(os.path.normpath(os.path.join(exe_dir, cfg.dvolt)), td.survey.strnr,
                                td.survey.vnr, out["sigmaa"])
         if cfg.lsens:
             out["sens"] = m.bsens()
+            if write:  # src/fem.f90:436-467
+                from .regularization import _centroids
+                cx, cy = _centroids(td.grid)
+                formats.write_sensitivities(os.path.normpath(os.path.join(exe_dir, cfg.dsens)), out["sens"], cx, cy)
         return out
     finally:
         m.close()

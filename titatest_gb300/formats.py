@@ -11,6 +11,8 @@ discards the rest of its last record):
 * ``crmod.cfg`` -- src/fem.f90:163-205
 * ``volt.dat``  -- src/wdatm.f90 (written by CRMod)
 * boundary values -- src/rrandb.f90 (lrandb2)
+* potentials and sensitivities -- src/wpot.f90, src/wsens.f90 (one file per
+  measurement)
 
 Node, element and electrode numbers are kept 1-based, exactly as in the
 files, so that the arrays can be handed to the C ABI unchanged.
@@ -525,6 +527,61 @@ def write_boundary_values(path: str, nodes, values):
             v = complex(v)
             fh.write(f"{int(k)} ({v.real!r},{v.imag!r})\n")
         fh.write("0\n")
+
+
+def f4(x) -> str:
+    """A REAL*4 value as list-directed output prints it: 9 significant digits."""
+    x = float(np.float32(x))
+    if x == 0.0 or 1e-1 <= abs(x) < 1e8:
+        return f"{x:.9g}"
+    return f"{x:.8E}"
+
+
+def numbered_path(datei: str, i: int, count: int) -> str:
+    """The file name of measurement i (1-based) of count, as src/wpot.f90 and
+    src/wsens.f90 form it: the number, zero-padded to the digits of count,
+    before the extension of datei ("pot.dat" -> "pot0001.dat")."""
+    head, tail = os.path.split(datei)
+    lnanz = int(math.log10(count)) + 1
+    stem, dot, ext = tail.partition(".")
+    return os.path.join(head, f"{stem}{i:0{lnanz}d}{dot}{ext[:3]}")
+
+
+def write_potentials(datei: str, hpot: np.ndarray, strnr, strom, grid: "Grid"):
+    """src/bpot.f90 + src/wpot.f90: for every measurement the potential of its
+    current pair (hpot(e2) - hpot(e1), times strom) at every node, as
+    x y Re Im lines, node by node in band order.  hpot: (eanz, sanz)."""
+    x, y = grid.node_xy()
+    nanz = len(strnr)
+    os.makedirs(os.path.dirname(datei) or ".", exist_ok=True)
+    for i in range(nanz):
+        e1, e2 = int(strnr[i]) % 10000, int(strnr[i]) // 10000
+        if e1 == 0:
+            pot = hpot[e2 - 1] * strom[i]
+        elif e2 == 0:
+            pot = -hpot[e1 - 1] * strom[i]
+        else:
+            pot = (hpot[e2 - 1] - hpot[e1 - 1]) * strom[i]
+        with open(numbered_path(datei, i + 1, nanz), "w") as fh:
+            for j in range(len(pot)):
+                fh.write(f"  {f4(x[j])}  {f4(y[j])}  {f4(pot[j].real)}  {f4(pot[j].imag)}\n")
+
+
+def write_sensitivities(datei: str, sens: np.ndarray, cx: np.ndarray, cy: np.ndarray):
+    """src/wsens.f90: one file per measurement i: |sum_j J_ij| and its phase
+    (mrad), then x y Re Im of J_ij for every element j (centroids cx, cy).
+    sens: (nanz, manz)."""
+    nanz = sens.shape[0]
+    os.makedirs(os.path.dirname(datei) or ".", exist_ok=True)
+    for i in range(nanz):
+        summe = complex(np.sum(sens[i]))
+        with open(numbered_path(datei, i + 1, nanz), "w") as fh:
+            if abs(summe) > 0.0:
+                fh.write(f"  {f4(abs(summe))}  {f4(1e3 * math.atan2(summe.imag, summe.real))}\n")
+            else:
+                fh.write("   0.00000000       0.00000000\n")
+            for j in range(sens.shape[1]):
+                fh.write(f"  {f4(cx[j])}  {f4(cy[j])}  {f4(sens[i, j].real)}  {f4(sens[i, j].imag)}\n")
 
 
 @dataclasses.dataclass

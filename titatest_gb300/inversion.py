@@ -833,14 +833,6 @@ def format_rows(rows: List[Row]) -> str:
     return "\n".join(out) + "\n"
 
 
-def _f4(x) -> str:
-    """A REAL*4 value as list-directed output prints it: 9 significant digits."""
-    x = float(np.float32(x))
-    if x == 0.0 or 1e-1 <= abs(x) < 1e8:
-        return f"{x:.9g}"
-    return f"{x:.8E}"
-
-
 def write_models(inv: "Inversion", ramd: str, ldc: bool = False):
     """The files src/wout.f90 writes for every accepted model NN: rhoNN.mag
     (centroid x, y, log10 |rho|; header elanz and the magnitude RMS),
@@ -857,7 +849,7 @@ def write_models(inv: "Inversion", ramd: str, ldc: bool = False):
         with open(os.path.join(ramd, f"rho{nn}.mag"), "w") as fh:
             fh.write(f"{g.elanz:12d} \t {m['betrms']!r}\n")
             for i in range(g.elanz):
-                fh.write(f"  {_f4(cx[i])}  {_f4(cy[i])}  {_f4(math.log10(abs(rho[i])))}\n")
+                fh.write(f"  {formats.f4(cx[i])}  {formats.f4(cy[i])}  {formats.f4(math.log10(abs(rho[i])))}\n")
         with open(os.path.join(ramd, f"rho{nn}.modl"), "w") as fh:
             fh.write(f"{g.elanz:7d}\n")
             for i in range(g.elanz):
@@ -866,15 +858,15 @@ def write_models(inv: "Inversion", ramd: str, ldc: bool = False):
             with open(os.path.join(ramd, f"rho{nn}.pha"), "w") as fh:
                 fh.write(f"{g.elanz:12d} \t {m['pharms']!r}\n")
                 for i in range(g.elanz):
-                    fh.write(f"  {_f4(cx[i])}  {_f4(cy[i])}  {_f4(1e3 * math.atan2(rho[i].imag, rho[i].real))}\n")
+                    fh.write(f"  {formats.f4(cx[i])}  {formats.f4(cy[i])}  {formats.f4(1e3 * math.atan2(rho[i].imag, rho[i].real))}\n")
             with open(os.path.join(ramd, f"rho{nn}.sig"), "w") as fh:
                 fh.write(f"{g.elanz:12d} {m['betrms']!r} {m['pharms']!r}\n")
                 for s in m["sigma"]:
-                    fh.write(f"  {_f4(s.real)}  {_f4(s.imag)}\n")
+                    fh.write(f"  {formats.f4(s.real)}  {formats.f4(s.imag)}\n")
         with open(os.path.join(ramd, f"volt{nn}.dat"), "w") as fh:
             fh.write(f"{len(m['sigmaa']):12d}\n")
             for i, sa in enumerate(m["sigmaa"]):
-                cols = [_f4(1.0 / math.exp(sa.real))] + ([] if ldc else [_f4(-1e3 * sa.imag)])
+                cols = [formats.f4(1.0 / math.exp(sa.real))] + ([] if ldc else [formats.f4(-1e3 * sa.imag)])
                 fh.write(f"{int(inv.data.strnr[i]):12d}{int(inv.data.vnr[i]):12d}  " + "  ".join(cols)
                          + f"{int(m['wdfak'][i]):12d}\n")
 
