@@ -236,6 +236,25 @@ int crgpu_update_dc(crgpu_ctx *ctx, const double *wmatd, const int32_t *wdfak, c
 int crgpu_blam0_jtj(crgpu_ctx *ctx, const double *wmatd, const int32_t *wdfak, int32_t phase_only,
                     double *jtj);
 
+/* Model uncertainty and resolution of src/bmcm_mod.f90 (buncert) on the
+ * sensitivities of the last crgpu_sens(ctx, 1, ...):
+ *   ata = Re(J^H W J) (bata), ata_reg = ata + lam R (bata_reg; ltri 1, 2 as
+ *   the reference builds it; ltri 0 the 5-point stencil of src/update.f90),
+ *   cov = ata_reg^-1 (bmcm, Cholesky), res = cov ata (bres, flags bit 0),
+ *   cov2 = cov ata cov (bmcm2, flags bits 0 and 1).
+ * Outputs the diagonals, manz doubles each (diag_res / diag_cov2 may be NULL
+ * when not asked for).  A non positive definite ata_reg returns 108. */
+int crgpu_mcm(crgpu_ctx *ctx, const double *wmatd, const int32_t *wdfak, int32_t ltri, const double *smatm,
+              int32_t nx, const int32_t *nachbar, double lam, int32_t flags, double *diag_ata,
+              double *diag_reg, double *diag_cov1, double *diag_res, double *diag_cov2);
+
+/* Column sums of the sensitivities for the coverage (src/bbsens.f90) and
+ * the FPI diagonal of bata: c1_j = sum_i |J_ij| wa_i, c2_j = sum_i
+ * |Re J_ij| wb_i, c3_j = sum_i Re(J_ij)^2 wc_i (nanz weights in, manz sums
+ * out). */
+int crgpu_column_sums(crgpu_ctx *ctx, const double *wa, const double *wb, const double *wc, double *c1,
+                      double *c2, double *c3);
+
 /* ------------------------------------------------------------------ */
 /* host-side set-up routines                                            */
 /* ------------------------------------------------------------------ */

@@ -1572,3 +1572,114 @@ int or_factor(const or_mesh *m, const or_opts *o, int kwnanz, const double *kwn,
     free(elbg); free(relbg); free(kg); free(c.sigma_dc);
     return e;
 }
+
+/* src/bmcm_mod.f90 buncert on a host Jacobian (column-major (nanz, manz)):
+ * bata (ata = Re(J^H W J)), bata_reg (ltri 1, 2: column by column, the
+ * diagonal, then the first nachbar(j, nk+1) slots, mirrored; ltri 0: the
+ * 5-point stencil of src/update.f90), bmcm (Cholesky inverse), bres
+ * (diag(cov ata)) and bmcm2 (diag(cov ata cov)).  Returns 108 when ata_reg
+ * is not positive definite. */
+int or_mcm(int nanz, int manz, const double *sens_, const double *wmatd, const int *wdfak, int ltri,
+           const double *smatm, int nx, const int *nachbar, int maxnk, double lam, double *d_ata,
+           double *d_reg, double *d_cov1, double *d_res, double *d_cov2) {
+    const cx *sens = (const cx *)sens_;
+    size_t n = (size_t)manz;
+    double *ata = (double *)calloc(n * n, sizeof(double));
+    double *reg = (double *)calloc(n * n, sizeof(double));
+    double *L = (double *)calloc(n * n, sizeof(double));
+    double *cov = (double *)calloc(n * n, sizeof(double));
+#define M(a, i, j) a[(size_t)(j) * n + (i)]
+    for (int k = 0; k < manz; k++)
+        for (int j = k; j < manz; j++) {
+            double s = 0.0;
+            for (int i = 0; i < nanz; i++) {
+                cx a = sens[(size_t)k * nanz + i], b = sens[(size_t)j * nanz + i];
+                s += (a.re * b.re + a.im * b.im) * wmatd[i] * (double)wdfak[i];
+            }
+            M(ata, k, j) = s;
+            M(ata, j, k) = s;
+        }
+    for (int k = 0; k < manz; k++) d_ata[k] = M(ata, k, k);
+    memcpy(reg, ata, sizeof(double) * n * n);
+    if (ltri == 0) {
+        for (int i = 0; i < manz; i++) {
+            M(reg, i, i) += lam * smatm[i];
+            if (i + 1 < manz) {
+                M(reg, i, i + 1) += lam * smatm[n + i];
+                M(reg, i + 1, i) += lam * smatm[n + i];
+            }
+            if (i + nx < manz) {
+                M(reg, i, i + nx) += lam * smatm[2 * n + i];
+                M(reg, i + nx, i) += lam * smatm[2 * n + i];
+            }
+        }
+    } else {
+        for (int j = 0; j < manz; j++) {
+            M(reg, j, j) = M(ata, j, j) + lam * smatm[(size_t)maxnk * n + j];
+            int cnt = nachbar[(size_t)maxnk * n + j];
+            for (int k = 0; k < cnt && k < maxnk; k++) {
+                int ik = nachbar[(size_t)k * n + j];
+                if (ik == 0) continue;
+                double v = M(ata, ik - 1, j) + lam * smatm[(size_t)k * n + j];
+                M(reg, ik - 1, j) = v;
+                M(reg, j, ik - 1) = v;
+            }
+        }
+    }
+    for (int k = 0; k < manz; k++) d_reg[k] = M(reg, k, k);
+    int err = 0;
+    /* Cholesky reg = L L^T */
+    for (int j = 0; j < manz && !err; j++) {
+        double s = M(reg, j, j);
+        for (int k = 0; k < j; k++) s -= M(L, j, k) * M(L, j, k);
+        if (!(s > 0.0)) { err = 108; break; }
+        double d = sqrt(s);
+        M(L, j, j) = d;
+        for (int i = j + 1; i < manz; i++) {
+            double t = M(reg, i, j);
+            for (int k = 0; k < j; k++) t -= M(L, i, k) * M(L, j, k);
+            M(L, i, j) = t / d;
+        }
+    }
+    if (!err) {
+        /* cov = L^-T L^-1: columns of L^-1 by forward substitution */
+        double *Li = (double *)calloc(n * n, sizeof(double));
+        for (int c = 0; c < manz; c++)
+            for (int i = c; i < manz; i++) {
+                double t = (i == c) ? 1.0 : 0.0;
+                for (int k = c; k < i; k++) t -= M(L, i, k) * M(Li, k, c);
+                M(Li, i, c) = t / M(L, i, i);
+            }
+        for (int i = 0; i < manz; i++)
+            for (int j = 0; j <= i; j++) {
+                double t = 0.0;
+                for (int k = i; k < manz; k++) t += M(Li, k, i) * M(Li, k, j);
+                M(cov, i, j) = t;
+                M(cov, j, i) = t;
+            }
+        free(Li);
+        for (int k = 0; k < manz; k++) d_cov1[k] = M(cov, k, k);
+        if (d_res || d_cov2) {
+            /* res = cov ata (src/bmcm_mod.f90 bres), cov2 = res cov (bmcm2) */
+            double *res = (double *)calloc(n * n, sizeof(double));
+            for (int j = 0; j < manz; j++)
+                for (int k = 0; k < manz; k++) {
+                    double a = M(ata, k, j);
+                    if (a == 0.0) continue;
+                    for (int i = 0; i < manz; i++) M(res, i, j) += M(cov, i, k) * a;
+                }
+            if (d_res)
+                for (int k = 0; k < manz; k++) d_res[k] = M(res, k, k);
+            if (d_cov2)
+                for (int i = 0; i < manz; i++) {
+                    double t = 0.0;
+                    for (int k = 0; k < manz; k++) t += M(res, i, k) * M(cov, k, i);
+                    d_cov2[i] = t;
+                }
+            free(res);
+        }
+    }
+#undef M
+    free(ata); free(reg); free(L); free(cov);
+    return err;
+}

@@ -157,6 +157,14 @@ int or_update(int nanz, int manz, const double *sens, const double *wmatd,
               int maxnk, double lam, double eps, int ncgmax, double step,
               double *par, double *dpar, double *cgfac, float *cgres);
 
+/* src/bmcm_mod.f90 buncert (bata, bata_reg, bmcm, bres, bmcm2) on a host
+ * Jacobian: the diagonals of ata, ata_reg, cov, cov ata and cov ata cov
+ * (d_res / d_cov2 may be NULL).  Returns 108 if ata_reg is not positive
+ * definite. */
+int or_mcm(int nanz, int manz, const double *sens, const double *wmatd, const int *wdfak, int ltri,
+           const double *smatm, int nx, const int *nachbar, int maxnk, double lam, double *d_ata,
+           double *d_reg, double *d_cov1, double *d_res, double *d_cov2);
+
 /* the same in the final phase improvement (lfpi; cjggdc on Re(J)); and for
  * DC inversion (ldc; cjggdc on Re(J) and Re(bvec)) */
 int or_update_dc(int nanz, int manz, const double *sens, const double *wmatd,

@@ -331,3 +331,31 @@ def update(sens, wmatd, wdfak, dat, sigmaa, ltri, smatm, nx=0, nachbar=None, max
                           _p(par, f64p), _p(dpar, f64p), _p(cgfac, f64p),
                           cgres.ctypes.data_as(C.POINTER(C.c_float)))
     return par, dpar, cgfac, cgres, ncg
+
+
+def mcm(sens, wmatd, wdfak, ltri, smatm, nx=0, nachbar=None, maxnk=4, lam=1.0, res=True, cov2=True):
+    """src/bmcm_mod.f90 buncert on the host Jacobian sens (nanz, manz):
+    dict of the diagonals 'ata', 'reg', 'cov1' and (if asked) 'res', 'cov2'."""
+    nanz, manz = sens.shape
+    s = np.ascontiguousarray(np.asarray(sens, np.complex128).T)  # column-major
+    out = {k: np.zeros(manz) for k in ("ata", "reg", "cov1", "res", "cov2")}
+    nb = np.ascontiguousarray(nachbar if nachbar is not None else np.zeros(1), np.int32)
+    e = lib().or_mcm(nanz, manz, _p(s, f64p), _p(np.ascontiguousarray(wmatd, np.float64), f64p),
+                     _p(np.ascontiguousarray(wdfak, np.int32), i32p), int(ltri),
+                     _p(np.ascontiguousarray(smatm, np.float64), f64p), int(nx), _p(nb, i32p), int(maxnk),
+                     C.c_double(lam), _p(out["ata"], f64p), _p(out["reg"], f64p), _p(out["cov1"], f64p),
+                     _p(out["res"], f64p) if res else None, _p(out["cov2"], f64p) if (res and cov2) else None)
+    if e:
+        raise RuntimeError(f"mcm errnr {e}")
+    if not res:
+        del out["res"]
+    if not (res and cov2):
+        del out["cov2"]
+    return out
+
+
+def column_sums(sens, wa, wb, wc):
+    """src/bbsens.f90 / bata column sums: sum_i |J_ij| wa_i, sum_i |Re J_ij|
+    wb_i, sum_i Re(J_ij)^2 wc_i."""
+    J = np.asarray(sens)
+    return (np.abs(J).T @ wa, np.abs(J.real).T @ wb, (J.real ** 2).T @ wc)

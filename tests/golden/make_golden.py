@@ -10,7 +10,8 @@ crmod.cfg) and the CRMod output volt.dat of a reference tomodir.  The
 measurement configurations are the (strnr, vnr) columns of volt.dat.
 Inversion cases add the tomodir's crtomo.cfg, CRTomo's inv.ctr and the
 model and data files written after iteration 1 (rho01.mag, rho01.pha,
-volt01.dat; minimal also rho02.mag).
+volt01.dat; minimal also rho02.mag and the coverage and uncertainty files
+of src/bbsens.f90 and src/bmcm_mod.f90).
 
 CutMcK cases (cutmck_<case>/): the grid before (elem.dat.orig, elec.dat.orig)
 and after (elem.dat, elec.dat) the reference's Cuthill-McKee renumbering.
@@ -69,7 +70,10 @@ def main(ref: str):
         for f in ("exe/crtomo.cfg", "inv/inv.ctr", "inv/rho01.mag", "inv/rho01.pha", "inv/volt01.dat"):
             shutil.copyfile(os.path.join(src, f), os.path.join(out, os.path.basename(f)))
         if name == "minimal":
-            shutil.copyfile(os.path.join(src, "inv/rho02.mag"), os.path.join(out, "rho02.mag"))
+            # rho02.mag, the coverage and the uncertainty files (mswitch 15)
+            for f in ("rho02.mag", "coverage.mag", "coverage.mag_fpi", "ata.diag", "ata.diag_fpi",
+                      "ata_reg.diag", "cov1_m.diag", "res_m.diag", "cov2_m.diag"):
+                shutil.copyfile(os.path.join(src, "inv", f), os.path.join(out, f))
     out = os.path.join(here, "dc_problem")
     os.makedirs(out, exist_ok=True)
     src = os.path.join(ref, DC_PROBLEM)

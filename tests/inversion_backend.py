@@ -44,6 +44,13 @@ class OracleBackend:
                                       phase_only=phase_only, dc=dc)
         return dpar, ncg
 
+    def mcm(self, wmatd, wdfak, ltri, smatm, nx, nachbar, lam, res, cov2):
+        return O.mcm(self.J, wmatd, wdfak, ltri, smatm, nx=nx, nachbar=nachbar, maxnk=self.grid.maxnk, lam=lam,
+                     res=res, cov2=cov2)
+
+    def column_sums(self, wa, wb, wc):
+        return O.column_sums(self.J, wa, wb, wc)
+
     def jtj(self, wmatd, wdfak, phase_only):
         """|(J^H W J 1)_j| of src/blam0.f90 from the host Jacobian."""
         w = np.asarray(wmatd) * np.asarray(wdfak, np.float64)
@@ -175,3 +182,28 @@ def check_models(case, inv, log10_tol=5e-4, pha_tol_mrad=0.5, volt_tol=1e-3):
     ours = np.exp(-m1["sigmaa"].real)
     assert np.abs(ours / vals[:, 2] - 1).max() < volt_tol
     return checked
+
+
+def check_uncertainty(inv, backend, tmpdir, rel=5e-3):
+    """titatest_gb300.uncertainty.write_all against the reference's
+    coverage and uncertainty files of minimal (mswitch 15; the reference
+    files come from the 2014 build, whose headers differ, the columns not):
+    ata, ata + lam R, cov and cov ata cov diagonals relative, the resolution
+    diagonal against its largest entry, the coverage in log10."""
+    from titatest_gb300 import uncertainty as U
+    U.write_all(inv, backend, str(tmpdir))
+    d = os.path.join(GOLDEN, "minimal")
+    for name, nc, col, kind, tol in (("ata.diag", 2, 0, "rel", rel), ("ata_reg.diag", 2, 0, "rel", rel),
+                                     ("cov1_m.diag", 3, 0, "rel", rel), ("cov2_m.diag", 3, 0, "rel", rel),
+                                     ("ata.diag_fpi", 2, 0, "rel", rel), ("res_m.diag", 2, 0, "max", 1e-3),
+                                     ("coverage.mag", 3, 2, "abs", 5e-3), ("coverage.mag_fpi", 3, 2, "abs", 5e-3)):
+        a = U.read_columns(os.path.join(str(tmpdir), name), nc)[:, col]
+        r = U.read_columns(os.path.join(d, name), nc)[:, col]
+        assert a.shape == r.shape, name
+        if kind == "rel":
+            err = np.max(np.abs(a / r - 1))
+        elif kind == "max":
+            err = np.max(np.abs(a - r)) / np.max(np.abs(r))
+        else:
+            err = np.max(np.abs(a - r))
+        assert err < tol, (name, err)

@@ -7,26 +7,29 @@ trials whose CG stops on its residual test the most (mixed_surf UP 9: 1.4% in
 misfit, 6 CG steps), inside the tolerances for such trials."""
 import pytest
 
-from inversion_backend import check_models, compare_rows, golden_rows, inversion_case
+from inversion_backend import check_models, check_uncertainty, compare_rows, golden_rows, inversion_case
 
 pytestmark = pytest.mark.gpu
 
 
-def _run(case, precision, max_iterations=None):
+def _run(case, precision, max_iterations=None, after=None):
     from titatest_gb300 import inversion as I
     g, sv, data, cfg, kwn, kwnwi = inversion_case(case)
     b = I.DeviceBackend(g, sv, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink, precision, refinement=(8, 1e-10))
     try:
         inv = I.Inversion(g, data, cfg, b)
         rows = inv.run(max_iterations=max_iterations)
+        if after is not None:
+            after(inv, b)
     finally:
         b.close()
     return inv, rows
 
 
 @pytest.mark.parametrize("prec", [0, 1])
-def test_gpu_inversion_reproduces_reference_trace_minimal(gpu_lib, prec):
-    inv, rows = _run("minimal", prec)
+def test_gpu_inversion_reproduces_reference_trace_minimal(gpu_lib, prec, tmp_path):
+    # coverage and uncertainty on the device (crgpu_column_sums, crgpu_mcm)
+    inv, rows = _run("minimal", prec, after=lambda inv, b: check_uncertainty(inv, b, tmp_path))
     gold = golden_rows("minimal")
     assert len(rows) == len(gold) == 25
     compare_rows(gold, rows, inv.ncgmax)

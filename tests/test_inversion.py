@@ -21,20 +21,21 @@ import pytest
 
 import math
 
-from inversion_backend import (OracleBackend, check_models, compare_rows, dc_problem, golden_rows,
-                               golden_rows_file, inversion_case)
+from inversion_backend import (OracleBackend, check_models, check_uncertainty, compare_rows, dc_problem,
+                               golden_rows, golden_rows_file, inversion_case)
 
 
-def _run(case, max_iterations=None):
+def _run(case, max_iterations=None, with_backend=False):
     from titatest_gb300 import inversion as I
     g, sv, data, cfg, kwn, kwnwi = inversion_case(case)
-    inv = I.Inversion(g, data, cfg, OracleBackend(g, sv, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink))
+    b = OracleBackend(g, sv, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink)
+    inv = I.Inversion(g, data, cfg, b)
     rows = inv.run(max_iterations=max_iterations)
-    return inv, rows
+    return (inv, rows, b) if with_backend else (inv, rows)
 
 
 def test_inversion_loop_reproduces_reference_trace_minimal(tmp_path):
-    inv, rows = _run("minimal")
+    inv, rows, backend = _run("minimal", with_backend=True)
     gold = golden_rows("minimal")
     assert len(gold) == 25 and len(rows) == 25
     compare_rows(gold, rows, inv.ncgmax)
@@ -54,6 +55,8 @@ def test_inversion_loop_reproduces_reference_trace_minimal(tmp_path):
     assert np.array_equal(mine[2], ref[2]) and np.array_equal(mine[3], ref[3])
     assert np.abs(mine[4] - ref[4]).max() < 5e-4
     assert sorted(p.name for p in tmp_path.iterdir())[:3] == ["rho00.mag", "rho00.modl", "rho00.pha"]
+    # coverage and uncertainty (src/bbsens.f90, src/bmcm_mod.f90) against the reference's files
+    check_uncertainty(inv, backend, tmp_path / "mcm")
 
 
 def test_inversion_loop_reproduces_reference_trace_mixed_surf():

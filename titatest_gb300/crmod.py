@@ -203,6 +203,34 @@ class CRMod:
                                               int(bool(phase_only)), ptr(out, f64p)))
         return out
 
+    def mcm(self, wmatd, wdfak, ltri, smatm, nx=0, nachbar=None, lam=1.0, res=True, cov2=True) -> dict:
+        """crgpu_mcm: the diagonals of src/bmcm_mod.f90 (ata, ata_reg, cov and,
+        if asked, cov ata and cov ata cov) on the device sensitivities."""
+        manz = self.grid.elanz
+        out = {k: np.zeros(manz) for k in ("ata", "reg", "cov1", "res", "cov2")}
+        nb = np.ascontiguousarray(nachbar if nachbar is not None else np.zeros(1), np.int32)
+        flags = (1 if res else 0) | (2 if (res and cov2) else 0)
+        _check(self._h, lib().crgpu_mcm(
+            self._h, ptr(np.ascontiguousarray(wmatd, np.float64), f64p),
+            ptr(np.ascontiguousarray(wdfak, np.int32), i32p), int(ltri),
+            ptr(np.ascontiguousarray(smatm, np.float64), f64p), int(nx), ptr(nb, i32p), C.c_double(lam),
+            int(flags), ptr(out["ata"], f64p), ptr(out["reg"], f64p), ptr(out["cov1"], f64p),
+            ptr(out["res"], f64p), ptr(out["cov2"], f64p)))
+        if not res:
+            del out["res"]
+        if not (res and cov2):
+            del out["cov2"]
+        return out
+
+    def column_sums(self, wa, wb, wc):
+        """crgpu_column_sums: sum_i |J_ij| wa_i, sum_i |Re J_ij| wb_i,
+        sum_i Re(J_ij)^2 wc_i on the device sensitivities."""
+        manz = self.grid.elanz
+        c = [np.zeros(manz) for _ in range(3)]
+        ws = [np.ascontiguousarray(w, np.float64) for w in (wa, wb, wc)]
+        _check(self._h, lib().crgpu_column_sums(self._h, *(ptr(w, f64p) for w in ws), *(ptr(x, f64p) for x in c)))
+        return tuple(c)
+
     def sens_on_device(self, mode: int = 1):
         """The sensitivities of the last forward into the context's device
         array only (for update), with no host copy."""

@@ -1387,6 +1387,89 @@ int crgpu_blam0_jtj(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, int
     return 0;
 }
 
+int crgpu_mcm(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, int32_t ltri, const double *smatm,
+              int32_t nx, const int32_t *nachbar, double lam, int32_t flags, double *diag_ata, double *diag_reg,
+              double *diag_cov1, double *diag_res, double *diag_cov2) {
+    if (!c || !wmatd || !wdfak || !smatm || !diag_ata || !diag_reg || !diag_cov1) return ERR_ARG;
+    if (!c->last_sens) return fail(c, ERR_ARG, "crgpu_mcm needs the sensitivities (crgpu_sens mode 1) first");
+    if (ltri != 0 && ltri != 1 && ltri != 2)
+        return fail(c, ERR_UNSUPPORTED, "crgpu_mcm: regularisation types 0, 1 and 2 only");
+    if (ltri != 0 && !nachbar) return ERR_ARG;
+    if ((flags & 1) && !diag_res) return ERR_ARG;
+    if ((flags & 2) && !diag_cov2) return ERR_ARG;
+    const int nanz = c->nanz, manz = c->hg.elanz;
+    int nk = 0;
+    for (int e = 0; e < manz; e++) nk = std::max(nk, c->hg.etype[e] == 3 ? 3 : 4);
+    const int ncol = ltri == 0 ? 3 : nk + 1;
+    double *d_w = nullptr, *d_sm = nullptr;
+    int32_t *d_wd = nullptr, *d_nb = nullptr;
+    int e = dalloc(c, &d_w, nanz);
+    if (!e) e = dalloc(c, &d_wd, nanz);
+    if (!e) e = dalloc(c, &d_sm, (size_t)manz * ncol);
+    if (!e && ltri != 0) e = dalloc(c, &d_nb, (size_t)manz * (nk + 1));
+    if (e) return e;
+    CUCHECK(c, cudaMemcpyAsync(d_w, wmatd, sizeof(double) * nanz, cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemcpyAsync(d_wd, wdfak, sizeof(int32_t) * nanz, cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemcpyAsync(d_sm, smatm, sizeof(double) * (size_t)manz * ncol, cudaMemcpyHostToDevice, c->st));
+    if (ltri != 0)
+        CUCHECK(c, cudaMemcpyAsync(d_nb, nachbar, sizeof(int32_t) * (size_t)manz * (nk + 1), cudaMemcpyHostToDevice,
+                                   c->st));
+    McmArgs a{};
+    a.nanz = nanz;
+    a.manz = manz;
+    a.ltri = ltri;
+    a.nx = nx;
+    a.nk = nk;
+    a.lam = lam;
+    a.sens = c->last_sens;
+    a.wmatd = d_w;
+    a.wdfak = d_wd;
+    a.smatm = d_sm;
+    a.nachbar = d_nb;
+    a.want_res = (flags & 1) != 0;
+    a.want_cov2 = (flags & 2) != 0;
+    a.diag_ata = diag_ata;
+    a.diag_reg = diag_reg;
+    a.diag_cov1 = diag_cov1;
+    a.diag_res = diag_res;
+    a.diag_cov2 = diag_cov2;
+    std::string msg;
+    const int rc = run_mcm(a, c->st, msg);
+    for (void *p : {(void *)d_w, (void *)d_wd, (void *)d_sm, (void *)d_nb}) {
+        if (!p) continue;
+        cudaFreeAsync(p, c->st);
+        c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), p), c->allocs.end());
+    }
+    if (rc) return fail(c, rc, msg);
+    return 0;
+}
+
+int crgpu_column_sums(crgpu_ctx *c, const double *wa, const double *wb, const double *wc, double *c1, double *c2,
+                      double *c3) {
+    if (!c || !wa || !wb || !wc || !c1 || !c2 || !c3) return ERR_ARG;
+    if (!c->last_sens) return fail(c, ERR_ARG, "crgpu_column_sums needs the sensitivities first");
+    const int nanz = c->nanz, manz = c->hg.elanz;
+    double *w = nullptr, *out = nullptr;
+    int e = dalloc(c, &w, (size_t)3 * nanz);
+    if (!e) e = dalloc(c, &out, (size_t)3 * manz);
+    if (e) return e;
+    CUCHECK(c, cudaMemcpyAsync(w, wa, sizeof(double) * nanz, cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemcpyAsync(w + nanz, wb, sizeof(double) * nanz, cudaMemcpyHostToDevice, c->st));
+    CUCHECK(c, cudaMemcpyAsync(w + 2 * (size_t)nanz, wc, sizeof(double) * nanz, cudaMemcpyHostToDevice, c->st));
+    launch_column_sums(nanz, manz, c->last_sens, w, w + nanz, w + 2 * (size_t)nanz, out, out + manz,
+                       out + 2 * (size_t)manz, c->st);
+    CUCHECK(c, cudaMemcpyAsync(c1, out, sizeof(double) * manz, cudaMemcpyDeviceToHost, c->st));
+    CUCHECK(c, cudaMemcpyAsync(c2, out + manz, sizeof(double) * manz, cudaMemcpyDeviceToHost, c->st));
+    CUCHECK(c, cudaMemcpyAsync(c3, out + 2 * (size_t)manz, sizeof(double) * manz, cudaMemcpyDeviceToHost, c->st));
+    CUCHECK(c, cudaStreamSynchronize(c->st));
+    for (void *p : {(void *)w, (void *)out}) {
+        cudaFreeAsync(p, c->st);
+        c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), p), c->allocs.end());
+    }
+    CUCHECK(c, cudaGetLastError());
+    return 0;
+}
+
 int crgpu_update(crgpu_ctx *c, const double *wmatd, const int32_t *wdfak, const double *dat, const double *sigmaa,
                  int32_t ltri, const double *smatm, int32_t nx, const int32_t *nachbar, double lam, double eps,
                  int32_t ncgmax, double step, double *par, double *dpar, double *cgfac, float *cgres,

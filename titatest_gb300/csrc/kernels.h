@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "device.cuh"
 
 namespace crgpu {
@@ -80,6 +82,24 @@ void launch_adjoint_rhs(const DevProblem &P, const DevBatch &B, int nrhs, const 
 void launch_adjoint_lambda(const DevProblem &P, const DevBatch &B, int nrhs, double2 *lambda, cudaStream_t st);
 void launch_adjoint_grad(const DevProblem &P, const double2 *kpot, const double2 *lambda, const int32_t *ebnd_ptr,
                          const int32_t *ebnd_list, double2 *grad, cudaStream_t st);
+
+// model uncertainty and resolution (mcm.cu, src/bmcm_mod.f90); device
+// inputs, host outputs (manz doubles each; diag_res / diag_cov2 only when
+// wanted)
+struct McmArgs {
+    int nanz, manz, ltri, nx, nk;
+    double lam;
+    const double2 *sens;     // column-major (nanz, manz)
+    const double *wmatd;     // nanz
+    const int32_t *wdfak;    // nanz
+    const double *smatm;     // column-major (manz, 3) or (manz, nk+1)
+    const int32_t *nachbar;  // column-major (manz, nk+1)
+    int want_res, want_cov2;
+    double *diag_ata, *diag_reg, *diag_cov1, *diag_res, *diag_cov2;
+};
+int run_mcm(const McmArgs &a, cudaStream_t st, std::string &msg);
+void launch_column_sums(int nanz, int manz, const double2 *sens, const double *wa, const double *wb,
+                        const double *wc, double *c1, double *c2, double *c3, cudaStream_t st);
 
 // v.y = 0 (DC: the real parts of the conductivities)
 void launch_real_part(double2 *v, int n, cudaStream_t st);

@@ -468,6 +468,12 @@ class DeviceBackend:
     def jtj(self, wmatd, wdfak, phase_only: bool) -> np.ndarray:
         return self.m.blam0_jtj(wmatd, wdfak, phase_only)
 
+    def mcm(self, wmatd, wdfak, ltri, smatm, nx, nachbar, lam, res, cov2) -> dict:
+        return self.m.mcm(wmatd, wdfak, ltri, smatm, nx=nx, nachbar=nachbar, lam=lam, res=res, cov2=cov2)
+
+    def column_sums(self, wa, wb, wc):
+        return self.m.column_sums(wa, wb, wc)
+
     def close(self):
         self.m.close()
 
@@ -581,6 +587,8 @@ class Inversion:
         self.phase_stage = phase_stage  # run the final phase improvement (lfphai)
         self.stage_start = None         # first row of the phase stage
         self.models: List[dict] = []    # every accepted model (an IT / PIT line), for write_models
+        self.lam_cri = None             # lambda when the final phase improvement started
+        self.lamalt = None              # the last good lambda after run()
 
     # -- pieces -----------------------------------------------------------------
     def _forward(self, sigma):
@@ -702,6 +710,7 @@ class Inversion:
                         self.status = "fpi"
                         break
                     self.wmatd = self.data.wmatdp.copy()
+                    self.lam_cri = lamalt  # src/inv.f90:634: the lambda of the complex stage
                     self.lfpi, self.lsetip = True, True
                     lfphai, self.llam, ldlami, lfstep, self.step = False, False, True, True, 1.0
                     self.stage_start = len(self.rows)
@@ -814,6 +823,7 @@ class Inversion:
             if cfg.llamf & 1:
                 self.llam = True
         self.it, self.itr = it, itr
+        self.lamalt = lamalt  # the last good lambda (src/inv.f90:1065, buncert)
         return self.rows
 
 
