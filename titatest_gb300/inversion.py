@@ -922,6 +922,9 @@ def run_crtomo(exe_dir: str, precision: int = 1, refinement=(8, 1e-10), write: b
             b.m.set_boundary_values(*formats.read_boundary_values(p(cfg.drandb), grid.sanz))
         inv = Inversion(grid, data, cfg, b, sigma_start=sigma_start)
         inv.run()
+        if write:  # coverage and, by mswitch, uncertainty (src/inv.f90:1050-1065)
+            from . import uncertainty
+            uncertainty.write_all(inv, b, p(cfg.ramd))
     finally:
         b.close()
     if write:
