@@ -9,7 +9,8 @@ A small driver for profilers (ncu) and quick timing:
 batch), so a profiler can capture a single launch of known size.
 --update-steps N adds the CRTomo Jacobian (bsensi, kept on the device) and one
 Gauss-Newton update with at most N CG steps (structured smoothness) on data
-that are the model's response times 1.03: the CG kernels for a profiler.
+that are the model's response times 1.03: the CG kernels for a profiler;
+--mcm then also times the model uncertainty (crgpu_mcm).
 """
 from __future__ import annotations
 
@@ -30,6 +31,7 @@ def main(argv=None):
     ap.add_argument("--sens", action="store_true")
     ap.add_argument("--refine-tol", type=float, default=1e-8)
     ap.add_argument("--update-steps", type=int, default=0)
+    ap.add_argument("--mcm", action="store_true", help="with --update-steps: time crgpu_mcm (uncertainty)")
     a = ap.parse_args(argv)
     s = synth.make(a.config)
     prec = MIXED if a.precision == "mixed" else PLAIN
@@ -63,6 +65,11 @@ def main(argv=None):
                                           eps=1e-4, ncgmax=a.update_steps, par=np.log(s.sigma))
             print(f"update {1e3 * (time.time() - t):.1f} ms, {ncg} CG steps, |dpar|max {np.abs(dpar).max():.3e}",
                   flush=True)
+            if a.mcm:
+                t = time.time()
+                d = m.mcm(w, np.ones(len(sa), np.int32), 0, sm, nx=s.nx, lam=300.0)
+                print(f"mcm {1e3 * (time.time() - t):.1f} ms for manz {len(d['cov1'])} (ata, ata_reg, Cholesky "
+                      f"inverse, resolution, cov2), min cov1 {d['cov1'].min():.3e}", flush=True)
 
 
 if __name__ == "__main__":
