@@ -331,19 +331,45 @@ class Misfit:
     npol: int
 
 
+def _phase_classes(im: np.ndarray) -> np.ndarray:
+    """_phase_class of every element."""
+    return np.where(im > _PI / 2.0, -1, np.where(im <= -_PI / 2.0, 1, 0))
+
+
+def _seqsum(v: np.ndarray) -> float:
+    """A sum in index order, as the reference's loops add (cumsum is sequential)."""
+    return float(np.cumsum(v)[-1]) if len(v) else 0.0
+
+
 def dmisft(dat, sigmaa, wmatd, wmatdr, wmatdp, lfpi: bool = False, lpol: bool = False) -> Misfit:
-    """src/dmisft.f90:60-125 (without robust reweighting or difference data)."""
-    nrmsd = betrms = pharms = 0.0
-    idum = 0
-    for i in range(len(dat)):
-        cdat, csig, wdlok = chkpo2(complex(dat[i]), complex(sigmaa[i]), lpol)
-        cdum = cdat - csig
-        psi = math.sqrt(wmatd[i]) * (abs(cdum.imag) if lfpi else abs(cdum))
-        idum += wdlok
-        nrmsd += psi * psi * wdlok
-        with np.errstate(invalid="ignore"):  # an infinite weight times 0 is NaN, as in the reference
-            betrms += float(np.float64(wmatdr[i]) * wdlok * cdum.real * cdum.real)
-            pharms += float(np.float64(wmatdp[i]) * wdlok * cdum.imag * cdum.imag)
+    """src/dmisft.f90:60-125 (without robust reweighting or difference data),
+    the polarity cases of chkpo2 applied element-wise and the sums taken in
+    index order."""
+    dat = np.asarray(dat, np.complex128)
+    sigmaa = np.asarray(sigmaa, np.complex128)
+    redat, imdat = dat.real.copy(), dat.imag.copy()
+    resig, imsig = sigmaa.real.copy(), sigmaa.imag.copy()
+    idat, isig = _phase_classes(imdat), _phase_classes(imsig)
+    wdlok = np.ones(len(dat), np.int64)
+    c1 = (idat == 0) & (isig != 0)
+    c2 = (idat != 0) & (isig == 0)
+    c3 = (idat != 0) & (isig != 0)
+    imsig[c1] = imsig[c1] + isig[c1] * _PI
+    if not lpol:
+        imdat[c1] = imdat[c1] - np.copysign(_PI, imdat[c1])
+    wdlok[c1] = 0
+    if lpol:
+        imdat[c2] = imdat[c2] + idat[c2] * _PI
+    wdlok[c2] = 0
+    imsig[c3] = imsig[c3] + isig[c3] * _PI
+    imdat[c3] = imdat[c3] + idat[c3] * _PI
+    dre, dim = redat - resig, imdat - imsig
+    psi = np.sqrt(np.asarray(wmatd, np.float64)) * (np.abs(dim) if lfpi else np.hypot(dre, dim))
+    idum = int(wdlok.sum())
+    with np.errstate(invalid="ignore"):  # an infinite weight times 0 is NaN, as in the reference
+        nrmsd = _seqsum(psi * psi * wdlok)
+        betrms = _seqsum(np.asarray(wmatdr, np.float64) * wdlok * dre * dre)
+        pharms = _seqsum(np.asarray(wmatdp, np.float64) * wdlok * dim * dim)
     if idum == 0:
         raise formats.CRError(99, "no datum left for the misfit")
     return Misfit(math.sqrt(nrmsd / idum), math.sqrt(betrms / idum), math.sqrt(pharms / idum), len(dat) - idum)
@@ -602,22 +628,20 @@ class Inversion:
     def _chkpol(self, lsetup: bool):
         """src/chkpol.f90 with lpol off: change the polarity of the model
         datum (the potential electrodes swap) and exclude the datum."""
+        imdat, imsig = self.dat.imag.copy(), self.sigmaa.imag.copy()
+        idat, isig = _phase_classes(imdat), _phase_classes(imsig)
+        c1 = (idat == 0) & (isig != 0)
+        c2 = (idat != 0) & (isig == 0)
+        c3 = (idat != 0) & (isig != 0)
+        flip = c1 | c3
+        self.swapped[flip] = ~self.swapped[flip]
+        imsig[flip] = imsig[flip] + isig[flip] * _PI
+        imdat[c1] = imdat[c1] - np.copysign(_PI, imdat[c1])
+        imdat[c3] = imdat[c3] + idat[c3] * _PI
+        self.sigmaa = self.sigmaa.real + 1j * imsig
+        self.dat = self.dat.real + 1j * imdat
         wdfak = np.ones(self.nanz, np.int32)
-        for i in range(self.nanz):
-            redat, imdat = self.dat[i].real, self.dat[i].imag
-            resig, imsig = self.sigmaa[i].real, self.sigmaa[i].imag
-            idat, isig = _phase_class(imdat), _phase_class(imsig)
-            if idat == 0 and isig != 0:
-                self.swapped[i] = ~self.swapped[i]
-                self.sigmaa[i] = complex(resig, imsig + isig * _PI)
-                self.dat[i] = complex(redat, imdat - math.copysign(_PI, imdat))
-                wdfak[i] = 0
-            elif idat != 0 and isig == 0:
-                wdfak[i] = 0
-            elif idat != 0 and isig != 0:
-                self.swapped[i] = ~self.swapped[i]
-                self.sigmaa[i] = complex(resig, imsig + isig * _PI)
-                self.dat[i] = complex(redat, imdat + idat * _PI)
+        wdfak[c1 | c2] = 0
         self.wdfak = wdfak
 
     def _misfit(self):
