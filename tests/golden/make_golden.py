@@ -44,6 +44,10 @@ INVERSION = {
 # crtomo_dc.cfg, inv_dc.ctr, a run that the DC factor ended with errnr 28)
 DC_PROBLEM = "tests/DC_Problem"
 
+# a robust DC inversion (examples/DifferenceInversion/02/time0): its
+# crtomo.cfg, grid, data and the inv.ctr of its run
+ROBUST_DC = "examples/DifferenceInversion/02/time0"
+
 CUTMCK = {
     "minimal": "tests/minimal/Reference/grid",
     "mixed_surf": "tests/2.5D_mixed_surf/Reference/grid",
@@ -84,6 +88,13 @@ def main(ref: str):
         shutil.copyfile(os.path.join(src, f), os.path.join(out, dst))
     with open(os.path.join(out, "SOURCE"), "w") as fh:
         fh.write(DC_PROBLEM + "/{Complex,DC}\n")
+    out = os.path.join(here, "robust_dc")
+    os.makedirs(out, exist_ok=True)
+    src = os.path.join(ref, ROBUST_DC)
+    for f in ("grid/elem.dat", "grid/elec.dat", "mod/volt.dat", "exe/crtomo.cfg", "inv/inv.ctr"):
+        shutil.copyfile(os.path.join(src, f), os.path.join(out, os.path.basename(f)))
+    with open(os.path.join(out, "SOURCE"), "w") as fh:
+        fh.write(ROBUST_DC + "\n")
     for name, d in CUTMCK.items():
         out = os.path.join(here, "cutmck_" + name)
         os.makedirs(out, exist_ok=True)

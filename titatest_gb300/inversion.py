@@ -17,9 +17,10 @@ with the error model of src/rdati.f90 (or individual errors), homogeneous or
 file start models (src/bsigm0.f90), structured (ltri 0) and triangular
 (ltri 1, 2) smoothness, a fixed lambda (llamf), the polarity checks
 (src/chkpol.f90, chkpo2 of src/dmisft.f90), the stopping rules of
-src/inv.f90:560-640, and DC inversion (ldc: the backends in DC mode,
-crgpu_set_dc, and the real update crgpu_update_dc).  Robust inversion,
-difference inversion, prior models and data noise raise NotImplementedError.
+src/inv.f90:560-640, DC inversion (ldc: the backends in DC mode,
+crgpu_set_dc, and the real update crgpu_update_dc) and robust inversion
+(lrobust: the reweighting of src/dmisft.f90:128-176).  Difference inversion,
+prior models and data noise raise NotImplementedError.
 """
 from __future__ import annotations
 
@@ -372,7 +373,29 @@ def dmisft(dat, sigmaa, wmatd, wmatdr, wmatdp, lfpi: bool = False, lpol: bool = 
         pharms = _seqsum(np.asarray(wmatdp, np.float64) * wdlok * dim * dim)
     if idum == 0:
         raise formats.CRError(99, "no datum left for the misfit")
-    return Misfit(math.sqrt(nrmsd / idum), math.sqrt(betrms / idum), math.sqrt(pharms / idum), len(dat) - idum)
+    m = Misfit(math.sqrt(nrmsd / idum), math.sqrt(betrms / idum), math.sqrt(pharms / idum), len(dat) - idum)
+    m.psi, m.wdlok = psi, wdlok
+    return m
+
+
+def robust_weights(wmatd, psi, wdlok, l1min: float = 1.0):
+    """The robust reweighting of src/dmisft.f90:128-176 (after LaBrecque):
+    estimated errors eps2_i = sqrt(psi_i) / sqrt(wmatd_i), scaled to the
+    1-norm and kept at least the prior errors; (l1rat, new wmatd or None when
+    l1rat <= l1min).  Sums in index order."""
+    wmatd = np.asarray(wmatd, np.float64)
+    dum = 1.0 / np.sqrt(wmatd)
+    eps2 = dum * np.sqrt(psi)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        norm = _seqsum(psi * wdlok)
+        norm2 = _seqsum(psi * wdlok * dum / eps2)
+        eps2 = eps2 * norm2 / norm
+        eps2 = np.maximum(dum, eps2)
+        norm2 = _seqsum(psi * wdlok * dum / eps2)
+    l1rat = norm / norm2
+    if l1rat > l1min:
+        return l1rat, 1.0 / (eps2 * eps2)
+    return l1rat, None
 
 
 def parfit(fa: float, fb: float, fc: float, fmin: float, smin: float, step: float) -> float:
@@ -494,6 +517,9 @@ class DeviceBackend:
     def jtj(self, wmatd, wdfak, phase_only: bool) -> np.ndarray:
         return self.m.blam0_jtj(wmatd, wdfak, phase_only)
 
+    def kfak(self) -> np.ndarray:
+        return self.m.bkfak()
+
     def mcm(self, wmatd, wdfak, ltri, smatm, nx, nachbar, lam, res, cov2) -> dict:
         return self.m.mcm(wmatd, wdfak, ltri, smatm, nx=nx, nachbar=nachbar, lam=lam, res=res, cov2=cov2)
 
@@ -539,6 +565,7 @@ class Row:
     npol: int = 0
     step: float = 0.0
     first: bool = False
+    l1rat: Optional[float] = None  # robust inversion: the L1 ratio of src/dmisft.f90
 
 
 class Inversion:
@@ -564,8 +591,8 @@ class Inversion:
 
     def __init__(self, grid, data: Data, cfg: CRTomoConfig, backend, sigma_start=None,
                  lamnull: Optional[tuple] = None, phase_stage: bool = True, ncgmax: Optional[int] = None):
-        if cfg.lrobust or cfg.ldiff:
-            raise NotImplementedError("robust and difference inversion are not built")
+        if cfg.ldiff:
+            raise NotImplementedError("difference inversion is not built")
         if cfg.ltri not in (0, 1, 2):
             raise NotImplementedError(f"regularisation ltri = {cfg.ltri} is not built")
         self.grid, self.data, self.cfg, self.b = grid, data, cfg, backend
@@ -604,8 +631,10 @@ class Inversion:
             self.sigma = np.full(grid.elanz, s, np.complex128)
         elif sigma_start is not None:
             self.sigma = np.array(sigma_start, np.complex128)
+        elif 11 in set(np.asarray(grid.typ).tolist()):  # lbeta: src/bsigm0.f90:87-125
+            self.sigma = np.full(grid.elanz, self._start_from_data(backend.kfak()), np.complex128)
         else:
-            raise NotImplementedError("start model from kfak-weighted data (lrho0 off, no start model)")
+            raise formats.CRError(100, "no start model (src/bsigm0.f90)")
         self.dat = data.dat.copy()
         self.swapped = np.zeros(self.nanz, bool)
         self.rows: List[Row] = []
@@ -615,6 +644,25 @@ class Inversion:
         self.models: List[dict] = []    # every accepted model (an IT / PIT line), for write_models
         self.lam_cri = None             # lambda when the final phase improvement started
         self.lamalt = None              # the last good lambda after run()
+
+    def _start_from_data(self, kfak) -> complex:
+        """src/bsigm0.f90:87-125: exp of the weighted mean of the data's
+        log apparent conductivities (phases brought into (-pi/2, pi/2]),
+        weights sqrt(wmatd) wdfak (all 1 here)."""
+        s0 = 0j
+        dum = 0.0
+        for i in range(self.nanz):
+            imdat = self.data.dat[i].imag
+            idat = _phase_class(imdat)
+            if idat != 0:
+                imdat = imdat + idat * _PI
+            redat = self.data.dat[i].real - math.log(abs(kfak[i]))
+            dum2 = math.sqrt(self.wmatd[i]) * 1.0
+            s0 = s0 + complex(redat, imdat) * complex(dum2)
+            dum = dum + dum2
+        if abs(dum) == 0.0:
+            raise formats.CRError(99, "unable to find starting value sigma0")
+        return np.exp(s0 / complex(dum))
 
     # -- pieces -----------------------------------------------------------------
     def _forward(self, sigma):
@@ -647,21 +695,26 @@ class Inversion:
     def _misfit(self):
         m = dmisft(self.dat, self.sigmaa, self.wmatd, self.data.wmatdr, self.data.wmatdp, self.lfpi, self.lpol)
         self.nrmsd, self.betrms, self.pharms, self.npol = m.nrmsd, m.betrms, m.pharms, m.npol
+        if self.lrobust:  # src/dmisft.f90:128-176: the weights of the next update
+            self.l1rat, w = robust_weights(self.wmatd, m.psi, m.wdlok, self.l1min)
+            if w is not None:
+                self.wmatd = w
 
     def _kont2(self, lsetup: bool):
         p = "P" if self.lfpi else ""
         if lsetup or (self.llam and not self.lstep):
             self.models.append(dict(it=self.it, sigma=self.sigma.copy(), sigmaa=self.sigmaa.copy(),
                                     wdfak=self.wdfak.copy(), betrms=self.betrms, pharms=self.pharms))
+        l1 = self.l1rat if self.lrobust else None
         if lsetup:
             self.rows.append(Row(p + "IT", self.it, self.nrmsd, betrms=self.betrms, pharms=self.pharms,
-                                 npol=self.npol, first=True))
+                                 npol=self.npol, first=True, l1rat=l1))
         elif self.llam and not self.lstep:
             self.rows.append(Row(p + "IT", self.it, self.nrmsd, self.bdpar, self.lam, self.rough, self.ncg,
-                                 self.betrms, self.pharms, self.npol, self.step))
+                                 self.betrms, self.pharms, self.npol, self.step, l1rat=l1))
         else:
             self.rows.append(Row(p + "UP", self.itr, self.nrmsd, self.bdpar, self.lam, self.rough, self.ncg,
-                                 step=self.step))
+                                 step=self.step, l1rat=l1))
 
     # -- the loop ---------------------------------------------------------------
     def run(self, max_iterations: Optional[int] = None) -> List[Row]:
@@ -689,6 +742,8 @@ class Inversion:
         sgmaa2 = None
         self.wdfak = np.ones(self.nanz, np.int32)
         lfphai = cfg.lfphai
+        self.lrobust, self.l1min, self.l1rat = cfg.lrobust, 1.0, 0.0  # src/rall.f90:194
+        wmatd2 = self.wmatd.copy()
         while True:
             self.it, self.itr = it, itr
             # modelling (src/inv.f90:342-503)
@@ -761,9 +816,13 @@ class Inversion:
                 if it > 1:
                     lamalt = self.lam
                 sigma2, sgmaa2 = self.sigma.copy(), self.sigmaa.copy()
+                if self.lrobust:  # src/inv.f90:727
+                    wmatd2 = self.wmatd.copy()
                 b.sensitivities()
             else:
                 self.sigma, self.sigmaa = sigma2.copy(), sgmaa2.copy()
+                if self.lrobust:  # src/inv.f90:760
+                    self.wmatd = wmatd2.copy()
             self.it, self.itr = it, itr
             if cfg.itmax == 0:
                 self.status = "109"
@@ -810,6 +869,8 @@ class Inversion:
                             self.lam *= dlam
                             if dlalt > 1.0 and dlam < 1.0:
                                 ldlamf = True
+                            if dlam > 1.0:  # src/inv.f90:868
+                                self.lrobust = False
                     else:
                         self.llam = True
                         self.lam /= dlam
