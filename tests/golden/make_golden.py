@@ -48,6 +48,12 @@ DC_PROBLEM = "tests/DC_Problem"
 # crtomo.cfg, grid, data and the inv.ctr of its run
 ROBUST_DC = "examples/DifferenceInversion/02/time0"
 
+# a robust DC difference inversion (examples/DifferenceInversion/02/time1)
+# against the reference state of time0: its data (d0.dat), final model
+# (m0.mag = time0's rho05.mag) and that model's response (fm0.dat =
+# time0's volt05.dat); the grid is time0's
+DIFF_DC = "examples/DifferenceInversion/02"
+
 CUTMCK = {
     "minimal": "tests/minimal/Reference/grid",
     "mixed_surf": "tests/2.5D_mixed_surf/Reference/grid",
@@ -95,6 +101,15 @@ def main(ref: str):
         shutil.copyfile(os.path.join(src, f), os.path.join(out, os.path.basename(f)))
     with open(os.path.join(out, "SOURCE"), "w") as fh:
         fh.write(ROBUST_DC + "\n")
+    out = os.path.join(here, "diff_dc")
+    os.makedirs(out, exist_ok=True)
+    src = os.path.join(ref, DIFF_DC)
+    for f, dst in (("time1/exe/crtomo.cfg", "crtomo.cfg"), ("time1/mod/volt1.dat", "volt.dat"),
+                   ("time1/inv/inv.ctr", "inv.ctr"), ("time0/mod/volt.dat", "d0.dat"),
+                   ("time0/inv/rho05.mag", "m0.mag"), ("time0/inv/volt05.dat", "fm0.dat")):
+        shutil.copyfile(os.path.join(src, f), os.path.join(out, dst))
+    with open(os.path.join(out, "SOURCE"), "w") as fh:
+        fh.write(DIFF_DC + "/{time0,time1}; grid: tests/golden/robust_dc (the same elem.dat, elec.dat)\n")
     for name, d in CUTMCK.items():
         out = os.path.join(here, "cutmck_" + name)
         os.makedirs(out, exist_ok=True)

@@ -239,3 +239,23 @@ def check_uncertainty(inv, backend, tmpdir, rel=5e-3):
         else:
             err = np.max(np.abs(a - r))
         assert err < tol, (name, err)
+
+
+def diff_case():
+    """The difference inversion of tests/golden/diff_dc: (grid, survey of the
+    kept data, data with d0 / fm0, m0, cfg, kwn, kwnwi).  The wavenumbers
+    come from all data (src/rall.f90 calls rwaven before it drops the data
+    without a reference-state match)."""
+    from titatest_gb300 import formats as F
+    from titatest_gb300 import inversion as I
+    d = os.path.join(GOLDEN, "diff_dc")
+    cfg = I.read_crtomo_cfg(os.path.join(d, "crtomo.cfg"))
+    g = F.read_elem(os.path.join(GOLDEN, "robust_dc", "elem.dat"))
+    enr = F.read_elec(os.path.join(GOLDEN, "robust_dc", "elec.dat"), g.sanz)
+    data = I.read_data(os.path.join(d, "volt.dat"), cfg, len(enr))
+    sv_all = F.Survey(enr=enr, strnr=data.strnr, vnr=data.vnr, strom=np.ones(len(data.strnr)))
+    kwn, kwnwi = O.Problem(g, sv_all).rwaven()
+    data, m0 = I.read_difference(data, os.path.join(d, "d0.dat"), os.path.join(d, "fm0.dat"),
+                                 os.path.join(d, "m0.mag"), g.elanz, cfg)
+    sv = F.Survey(enr=enr, strnr=data.strnr, vnr=data.vnr, strom=np.ones(len(data.strnr)))
+    return g, sv, data, m0, cfg, kwn, kwnwi

@@ -135,3 +135,21 @@ def test_gpu_robust_dc_inversion_first_iteration(gpu_lib, prec):
         b.close()
     assert len(rows) == 11 and rows[-1].npol == 5
     compare_rows(golden_rows_robust("robust_dc")[:11], rows, inv.ncgmax, skip=(8,))
+
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_gpu_difference_inversion_first_iteration(gpu_lib, prec):
+    """The difference inversion of tests/test_inversion.py on the GPU."""
+    from titatest_gb300 import inversion as I
+    from inversion_backend import diff_case, golden_rows_robust
+    g, sv, data, m0, cfg, kwn, kwnwi = diff_case()
+    b = I.DeviceBackend(g, sv, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink, prec, refinement=(8, 1e-10), ldc=True)
+    try:
+        inv = I.Inversion(g, data, cfg, b, m0=m0)
+        rows = inv.run(max_iterations=1)
+    finally:
+        b.close()
+    assert len(rows) == 10
+    compare_rows(golden_rows_robust("diff_dc")[:10], rows, inv.ncgmax)
+    assert abs(rows[0].betrms / 20.29 - 1) < 2e-3

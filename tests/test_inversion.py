@@ -22,7 +22,7 @@ import pytest
 import math
 
 from inversion_backend import (OracleBackend, check_models, check_uncertainty, compare_rows, dc_problem,
-                               golden_rows, golden_rows_file, golden_rows_robust, inversion_case)
+                               diff_case, golden_rows, golden_rows_file, golden_rows_robust, inversion_case)
 
 
 def _run(case, max_iterations=None, with_backend=False):
@@ -138,3 +138,21 @@ def test_robust_dc_inversion_first_iteration():
     gold = golden_rows_robust("robust_dc")[:11]
     assert len(rows) == 11 and rows[-1].npol == 5
     compare_rows(gold, rows, inv.ncgmax, skip=(8,))
+
+
+def test_difference_inversion_first_iteration():
+    """examples/DifferenceInversion/02/time1 of the reference: a robust DC
+    difference inversion (src/rall.f90:853-943, src/dmisft.f90:97-101,
+    src/update.f90:241-279) from time0's model, data and response; 361 of
+    its 528 data have a reference-state match.  The first iteration's 10
+    lines.  The magnitude RMS of IT 0 (20.29 against a misfit of 19.08)
+    pins the reference's data drop, which leaves wmatdr unshifted."""
+    from titatest_gb300 import inversion as I
+    g, sv, data, m0, cfg, kwn, kwnwi = diff_case()
+    assert cfg.ldiff and cfg.ldc and cfg.lrobust and len(data.strnr) == 361
+    inv = I.Inversion(g, data, cfg, OracleBackend(g, sv, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink, ldc=True),
+                      m0=m0)
+    rows = inv.run(max_iterations=1)
+    assert len(rows) == 10
+    compare_rows(golden_rows_robust("diff_dc")[:10], rows, inv.ncgmax)
+    assert abs(rows[0].betrms / 20.29 - 1) < 2e-3 and abs(rows[9].betrms / 5.087 - 1) < 1e-2

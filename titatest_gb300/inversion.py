@@ -19,8 +19,10 @@ file start models (src/bsigm0.f90), structured (ltri 0) and triangular
 (src/chkpol.f90, chkpo2 of src/dmisft.f90), the stopping rules of
 src/inv.f90:560-640, DC inversion (ldc: the backends in DC mode,
 crgpu_set_dc, and the real update crgpu_update_dc) and robust inversion
-(lrobust: the reweighting of src/dmisft.f90:128-176).  Difference inversion,
-prior models and data noise raise NotImplementedError.
+(lrobust: the reweighting of src/dmisft.f90:128-176), and difference
+inversion (ldiff: read_difference, the misfit and update against d0 - fm0).
+Prior models without reference-state data and data noise raise
+NotImplementedError.
 """
 from __future__ import annotations
 
@@ -186,6 +188,9 @@ def read_crtomo_cfg(path: str) -> CRTomoConfig:
         raise formats.CRError(105, "phase error model")
     if cfg.lrho0 and (cfg.bet0 <= 0.0 or (not cfg.ldc and abs(cfg.pha0) > 1e3 * _PI)):
         raise formats.CRError(91, "homogeneous start model")
+    if cfg.ldiff:  # src/rall.f90:624-629 (with reference-state data and response given)
+        cfg.lrho0 = False
+        cfg.ldc = True
     if cfg.ldc:
         cfg.lfphai = False
     return cfg
@@ -202,6 +207,9 @@ class Data:
     wmatdr: np.ndarray     # 1/eps_r^2
     wmatdp: np.ndarray     # 1/eps_p^2
     wmatd_cri: np.ndarray  # 1/(eps_r^2 + eps_p^2)
+    wmatd: Optional[np.ndarray] = None  # the working weights when set apart (difference inversion)
+    d0: Optional[np.ndarray] = None   # difference inversion: -ln|R| of the reference-state data
+    fm0: Optional[np.ndarray] = None  # and of the reference-state model's response
 
 
 def make_data(strnr, vnr, bet, pha, cfg: CRTomoConfig) -> Data:
@@ -220,6 +228,66 @@ def make_data(strnr, vnr, bet, pha, cfg: CRTomoConfig) -> Data:
         wc = np.zeros_like(bet) if cfg.ldc else 1.0 / (stabw ** 2 + stabwp ** 2)
     return Data(strnr=np.asarray(strnr, np.int32), vnr=np.asarray(vnr, np.int32), dat=dat, wmatdr=wr,
                 wmatdp=wp, wmatd_cri=wc)
+
+
+def read_difference(data: Data, d0_path: str, fm0_path: str, m0_path: str, elanz: int,
+                    cfg: Optional[CRTomoConfig] = None):
+    """The reference state of a difference inversion (src/rall.f90:853-943):
+    d0 from the reference-state data file, fm0 from the reference-state
+    model's response (a voltNN.dat: strnr vnr |R| wdfak), both matched to
+    the data by (strnr, vnr) where wdfak is 1; data without a match are
+    discarded.  m0 = ln sigma of the reference-state model (a rhoNN.mag:
+    x y log10 rho).  Returns (data kept, with d0 / fm0 set; m0).
+
+    As the reference's loop drops a datum it moves strnr, vnr, dat and the
+    working weights wmatd (set before, src/rall.f90:805-817) down by one, but
+    not wmatdr, wmatd_cri or (without lfphai) wmatdp: those keep the entries
+    of the original positions.  The magnitude RMS of src/dmisft.f90 reads
+    wmatdr, so it is reproduced with those weights."""
+    rec = formats._Records(d0_path)
+    nanz0 = int(rec._tokens(rec.read_line())[0])
+    ic, ip, dum = [], [], []
+    for _ in range(nanz0):
+        t = rec._tokens(rec.read_line())
+        if int(t[0]) - 10000 > 0:
+            ic.append(int(t[0]))
+            ip.append(int(t[1]))
+            dum.append(formats._f(t[2]))
+        else:
+            e = [int(x) for x in t[:4]]
+            ic.append(e[0] * 10000 + e[1])
+            ip.append(e[2] * 10000 + e[3])
+            dum.append(formats._f(t[4]))
+    rec = formats._Records(fm0_path)
+    rec.read_line()
+    dum2, idum = [], []
+    for _ in range(nanz0):
+        t = rec._tokens(rec.read_line())
+        dum2.append(formats._f(t[2]))
+        idum.append(int(t[3]))
+    keep, d0, fm0 = [], [], []
+    for i in range(len(data.strnr)):
+        for j in range(nanz0):  # the first match, as the reference's search finds it
+            if data.strnr[i] == ic[j] and data.vnr[i] == ip[j] and idum[j] == 1:
+                keep.append(i)
+                d0.append(complex(-math.log(dum[j]), 0.0))
+                fm0.append(complex(-math.log(dum2[j]), 0.0))
+                break
+    k = np.asarray(keep, np.int64)
+    nk = len(k)
+    lelerr = cfg is not None and ((not cfg.lfphai and not cfg.ldc) or bool(cfg.mswitch & 32))
+    wmatd = (data.wmatd_cri if lelerr else data.wmatdr)[k]
+    lfphai = cfg is not None and cfg.lfphai
+    kept = Data(strnr=data.strnr[k], vnr=data.vnr[k], dat=data.dat[k], wmatdr=data.wmatdr[:nk].copy(),
+                wmatdp=(data.wmatdp[k] if lfphai else data.wmatdp[:nk].copy()),
+                wmatd_cri=data.wmatd_cri[:nk].copy(), wmatd=wmatd, d0=np.asarray(d0, np.complex128),
+                fm0=np.asarray(fm0, np.complex128))
+    rec = formats._Records(m0_path)
+    rec.read_line()
+    m0 = np.zeros(elanz, np.complex128)
+    for j in range(elanz):
+        m0[j] = complex(-math.log(10.0) * formats._f(rec._tokens(rec.read_line())[2]), 0.0)
+    return kept, m0
 
 
 def read_data(path: str, cfg: CRTomoConfig, eanz: int) -> Data:
@@ -342,10 +410,10 @@ def _seqsum(v: np.ndarray) -> float:
     return float(np.cumsum(v)[-1]) if len(v) else 0.0
 
 
-def dmisft(dat, sigmaa, wmatd, wmatdr, wmatdp, lfpi: bool = False, lpol: bool = False) -> Misfit:
-    """src/dmisft.f90:60-125 (without robust reweighting or difference data),
-    the polarity cases of chkpo2 applied element-wise and the sums taken in
-    index order."""
+def dmisft(dat, sigmaa, wmatd, wmatdr, wmatdp, lfpi: bool = False, lpol: bool = False, off=None) -> Misfit:
+    """src/dmisft.f90:60-125 (robust reweighting: robust_weights), the
+    polarity cases of chkpo2 applied element-wise and the sums taken in index
+    order.  off: d0 - fm0 of a difference inversion (src/dmisft.f90:97-101)."""
     dat = np.asarray(dat, np.complex128)
     sigmaa = np.asarray(sigmaa, np.complex128)
     redat, imdat = dat.real.copy(), dat.imag.copy()
@@ -365,6 +433,8 @@ def dmisft(dat, sigmaa, wmatd, wmatdr, wmatdp, lfpi: bool = False, lpol: bool = 
     imsig[c3] = imsig[c3] + isig[c3] * _PI
     imdat[c3] = imdat[c3] + idat[c3] * _PI
     dre, dim = redat - resig, imdat - imsig
+    if off is not None:
+        dre, dim = dre - off.real, dim - off.imag
     psi = np.sqrt(np.asarray(wmatd, np.float64)) * (np.abs(dim) if lfpi else np.hypot(dre, dim))
     idum = int(wdlok.sum())
     with np.errstate(invalid="ignore"):  # an infinite weight times 0 is NaN, as in the reference
@@ -590,9 +660,11 @@ class Inversion:
     lpol = False
 
     def __init__(self, grid, data: Data, cfg: CRTomoConfig, backend, sigma_start=None,
-                 lamnull: Optional[tuple] = None, phase_stage: bool = True, ncgmax: Optional[int] = None):
-        if cfg.ldiff:
-            raise NotImplementedError("difference inversion is not built")
+                 lamnull: Optional[tuple] = None, phase_stage: bool = True, ncgmax: Optional[int] = None,
+                 m0=None):
+        if cfg.ldiff and (data.d0 is None or m0 is None):
+            raise NotImplementedError("difference inversion needs the reference state (read_difference)")
+        self.doff = (data.d0 - data.fm0) if cfg.ldiff else None
         if cfg.ltri not in (0, 1, 2):
             raise NotImplementedError(f"regularisation ltri = {cfg.ltri} is not built")
         self.grid, self.data, self.cfg, self.b = grid, data, cfg, backend
@@ -617,7 +689,7 @@ class Inversion:
         # weights (src/rall.f90:805-817): the complex stage with a final phase
         # improvement fits the magnitude error only
         lelerr = (not cfg.lfphai and not cfg.ldc) or bool(cfg.mswitch & 32)
-        self.wmatd = (data.wmatd_cri if lelerr else data.wmatdr).copy()
+        self.wmatd = (data.wmatd_cri if lelerr else data.wmatdr).copy() if data.wmatd is None else data.wmatd.copy()
         # smoothness (src/bsmatm_mod.f90)
         if cfg.ltri == 0:
             self.nachbar = None
@@ -626,7 +698,9 @@ class Inversion:
             self.nachbar = R.bnachbar(grid)
             self.smatm = R.bsmatmtri(grid, self.nachbar, cfg.alfx, cfg.alfz)
         # start model (src/bsigm0.f90)
-        if cfg.lrho0:
+        if cfg.ldiff:  # src/bsigm0.f90:66-69: the reference-state model
+            self.sigma = np.exp(np.asarray(m0, np.complex128))
+        elif cfg.lrho0:
             s = complex(math.cos(cfg.pha0 / 1e3) / cfg.bet0, -math.sin(cfg.pha0 / 1e3) / cfg.bet0)
             self.sigma = np.full(grid.elanz, s, np.complex128)
         elif sigma_start is not None:
@@ -693,7 +767,8 @@ class Inversion:
         self.wdfak = wdfak
 
     def _misfit(self):
-        m = dmisft(self.dat, self.sigmaa, self.wmatd, self.data.wmatdr, self.data.wmatdp, self.lfpi, self.lpol)
+        m = dmisft(self.dat, self.sigmaa, self.wmatd, self.data.wmatdr, self.data.wmatdp, self.lfpi, self.lpol,
+                   self.doff)
         self.nrmsd, self.betrms, self.pharms, self.npol = m.nrmsd, m.betrms, m.pharms, m.npol
         if self.lrobust:  # src/dmisft.f90:128-176: the weights of the next update
             self.l1rat, w = robust_weights(self.wmatd, m.psi, m.wdlok, self.l1min)
@@ -895,7 +970,9 @@ class Inversion:
             bdalt = self.bdpar
             if not self.llam:
                 dpar2, ncg2 = dpar, self.ncg
-                dpar, self.ncg = b.update(self.wmatd, self.wdfak, self.dat, self.sigmaa, cfg.ltri, self.smatm,
+                # difference inversion: dat - sigmaa - (d0 - fm0) (src/update.f90:241-279)
+                dat_eff = self.dat if self.doff is None else self.dat - self.doff
+                dpar, self.ncg = b.update(self.wmatd, self.wdfak, dat_eff, self.sigmaa, cfg.ltri, self.smatm,
                                           cfg.nx, self.nachbar, self.lam, self.eps, self.ncgmax, 1.0, par,
                                           phase_only=self.lfpi, dc=cfg.ldc)
                 dpar = np.array(dpar, np.complex128)
@@ -975,7 +1052,7 @@ def read_model_mag(path: str):
 
 
 def run_crtomo(exe_dir: str, precision: int = 1, refinement=(8, 1e-10), write: bool = True):
-    """CRTomo's complex stage on a tomodir: reads exe_dir/crtomo.cfg and its
+    """CRTomo on a tomodir: reads exe_dir/crtomo.cfg and its
     inputs, inverts on the GPU and (write) puts the IT/UP lines into
     <ramd>/inv.ctr, the final model into <ramd>/rho.dat (magnitude in ohm m
     and phase in mrad, as src/rsigma.f90 reads a model) and every accepted
@@ -998,14 +1075,17 @@ def run_crtomo(exe_dir: str, precision: int = 1, refinement=(8, 1e-10), write: b
             raise formats.CRError(110, "2D with mixed boundaries")
         kwn = np.array([0.0 if cfg.lrandb2 else 1e-6])
         kwnwi = np.zeros(1)
-    sigma_start = None
-    if not cfg.lrho0 and cfg.dm0:
+    sigma_start = m0 = None
+    if cfg.ldiff:  # the reference state; the wavenumbers above came from all data
+        data, m0 = read_difference(data, p(cfg.dd0), p(cfg.dfm0), p(cfg.dm0), grid.elanz, cfg)
+        survey = formats.Survey(enr=enr, strnr=data.strnr, vnr=data.vnr, strom=np.ones(len(data.strnr)))
+    elif not cfg.lrho0 and cfg.dm0:
         sigma_start = formats.read_rho(p(cfg.dm0), grid.elanz)
     b = DeviceBackend(grid, survey, kwn, kwnwi, cfg.swrtr, cfg.lsink, cfg.nsink, precision, refinement, cfg.ldc)
     try:
         if cfg.lrandb2:
             b.m.set_boundary_values(*formats.read_boundary_values(p(cfg.drandb), grid.sanz))
-        inv = Inversion(grid, data, cfg, b, sigma_start=sigma_start)
+        inv = Inversion(grid, data, cfg, b, sigma_start=sigma_start, m0=m0)
         inv.run()
         if write:  # coverage and, by mswitch, uncertainty (src/inv.f90:1050-1065)
             from . import uncertainty
