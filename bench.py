@@ -11,7 +11,9 @@ seeded; titatest_gb300.synth.config2).
 value : mixed mode (complex64 factor + FP64 refinement), inputs resident on
         the device, timed with CUDA events on the library's stream;
 e2e   : the same unit through the host C ABI (crgpu_forward + crgpu_sens with
-        pinned host buffers: sigma in, voltages and the Jacobian out);
+        pinned host buffers: sigma in, voltages and the Jacobian out), with
+        d2h_link_gbs, the rate of a plain pinned copy of the Jacobian's bytes
+        in the same run (the host link is shared and its rate varies);
 plain : the complex128 mode on the same inputs (the reference arithmetic),
         with the mixed/plain speed-up and the error of mixed against plain.
 --impl reference times the oracle (the plain-C restatement of the reference
@@ -293,6 +295,15 @@ def run_gpu(args):
     e2e_ms = e0.elapsed_time(e1) / e_steps
     h2d = 16 * manz
     d2h = 16 * nanz + 16 * nanz * manz
+    # the host link's own rate for the Jacobian's bytes (a plain pinned copy),
+    # so that the e2e figure can be read against what the link gave this run
+    h_sens.copy_(sens_dev, non_blocking=True)
+    e0.record(stream)
+    for _ in range(e_steps):
+        h_sens.copy_(sens_dev, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    link_gbs = 16 * nanz * manz * e_steps / (e0.elapsed_time(e1) * 1e6)
 
     # ---- plain complex128 on the same inputs
     mixed_stats = mixed.stats()
@@ -340,7 +351,8 @@ def run_gpu(args):
                    "autotuned_kernels": tune},
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
-        "e2e": {"value": 1e3 / e2e_ms, "unit": "units/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": 1e3 / e2e_ms, "unit": "units/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "d2h_link_gbs": link_gbs},
         "plain": {"value": 1e3 / plain_ms, "unit": "units/s", "ms_per_step": plain_ms,
                   "ms_factor": plain_stats["ms_factor"], "ms_solve": plain_stats["ms_solve"],
                   "ms_sens": plain_stats["ms_sens"]},
