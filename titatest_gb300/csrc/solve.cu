@@ -6,7 +6,9 @@
 // bulk copy per block brings them into shared memory S blocks ahead;
 // the working vector lives in a shared window.  Per block the dependent
 // chain is one warp reduction (forward) and an 8-step triangle of shuffles;
-// the rest is independent multiply-adds over the lanes' columns.
+// the rest is independent multiply-adds over the lanes' columns.  Launches
+// of few sweeps (up to kFewItems) give each right-hand side kSweepWarps
+// warps instead (k_fwd_mw, k_bwd_mw), since each sweep is then latency bound.
 #include <mutex>
 
 #include "async.cuh"
@@ -58,13 +60,16 @@ constexpr int kRB = 8;  // rows per block of a sweep
 // (together they saturate HBM), 8 when few do and each is latency bound
 constexpr int kStagesMany = 2, kStagesFew = 8;
 constexpr int kFewItems = 256;  // sweeps per launch up to which kStagesFew is used
+// warps per right-hand side of the few-sweeps kernels (k_fwd_mw, k_bwd_mw)
+constexpr int kSweepWarps = 4;
 
 // Per-warp shared memory (byte offsets): stage barriers, the right-hand side
 // of each staged block (forward sweep), the staged band rows, the window of
 // the working vector (entry j in slot j & wmask) and the vector entries that
-// enter the window with each block (backward sweep).
+// enter the window with each block (backward sweep); the multi-warp kernels
+// add the per-warp row sums (forward) or the block's solution (backward).
 struct SolveLayout {
-    int bars, rhs, rows, win, ent, total;
+    int bars, rhs, rows, win, ent, part, total;
 };
 template <typename T, int S>
 __host__ __device__ inline SolveLayout solve_layout(int W, int WW) {
@@ -74,7 +79,8 @@ __host__ __device__ inline SolveLayout solve_layout(int W, int WW) {
     s.rows = s.rhs + S * kRB * (int)sizeof(double2);
     s.win = s.rows + S * kRB * W * (int)sizeof(T);
     s.ent = s.win + WW * (int)sizeof(T);
-    s.total = (s.ent + S * kRB * (int)sizeof(T) + 127) & ~127;
+    s.part = s.ent + S * kRB * (int)sizeof(T);
+    s.total = (s.part + kSweepWarps * kRB * (int)sizeof(T) + 127) & ~127;
     return s;
 }
 
@@ -298,6 +304,201 @@ __global__ __launch_bounds__(32) void k_bwd(DevProblem P, DevBatch B, int nrhs, 
     cp_wait<0>();
 }
 
+// Few sweeps per launch (the last, partial round of a batch; small problems):
+// a sweep is a chain of n / 8 dependent blocks, and one warp alone spends
+// most of each block on its own issue and shuffle latency.  Here
+// kSweepWarps warps share one right-hand side: the columns are split over
+// all threads, warp 0 adds the per-warp row sums in warp order and solves
+// the 8x8 triangle, and two block barriers separate the phases of a block.
+// The staging (thread 0's bulk copies, warp 0's entering elements) is that
+// of k_fwd / k_bwd.
+template <typename T, int S>
+__global__ __launch_bounds__(32 * kSweepWarps) void k_fwd_mw(DevProblem P, DevBatch B, int nrhs,
+                                                             const double2 *__restrict__ rin, int wmask) {
+    extern __shared__ __align__(128) unsigned char sm_raw[];
+    constexpr int NT = 32 * kSweepWarps;
+    const int n = P.n, mb = P.mb, W = mb + 1, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int item = blockIdx.x;
+    if (item >= B.nsys * nrhs) return;
+    if (B.nprev && *B.nprev == 0) return;
+    if (B.active && !B.active[item]) return;
+    const SolveLayout lay = solve_layout<T, S>(W, wmask + 1);
+    uint64_t *bar = (uint64_t *)(sm_raw + lay.bars);
+    double2 *rv = (double2 *)(sm_raw + lay.rhs);
+    T *rows = (T *)(sm_raw + lay.rows);
+    T *win = (T *)(sm_raw + lay.win);
+    T *part = (T *)(sm_raw + lay.part);  // [kSweepWarps][kRB]
+    const T *L = (const T *)B.L + (size_t)(item / nrhs) * B.lpitch;
+    const double2 *r = rin + (size_t)item * n;
+    T *y = (T *)B.y + (size_t)item * n;
+    const int nblk = (n + kRB - 1) / kRB;
+    auto issue = [&](int t) {  // thread 0
+        if (t >= nblk) return;
+        const int st = t % S, i0 = t * kRB, nr = min(kRB, n - i0);
+        const uint32_t bl = ((uint32_t)(nr * W * (int)sizeof(T)) + 15u) & ~15u;
+        const uint32_t br = (uint32_t)nr * (uint32_t)sizeof(double2);
+        mbar_expect_tx(&bar[st], bl + br);
+        bulk_g2s(rows + (size_t)st * kRB * W, L + (size_t)i0 * W, bl, &bar[st]);
+        bulk_g2s(rv + st * kRB, r + i0, br, &bar[st]);
+    };
+    if (tid == 0) {
+        for (int q = 0; q < S; q++) mbar_init(&bar[q], 1);
+        mbar_init_fence();
+        for (int t = 0; t < S; t++) issue(t);
+    }
+    __syncthreads();
+    const int myr = lane >> 2;
+    for (int t = 0; t < nblk; t++) {
+        const int st = t % S, i0 = t * kRB, nr = min(kRB, n - i0);
+        const bool ok = mbar_wait(&bar[st], (t / S) & 1);
+        if (!__syncthreads_and(ok)) {
+            if (wid == 0) solve_timeout<S>(P, bar, t, min(nblk - 1, t + S - 1));
+            return;
+        }
+        const T *Lb = rows + (size_t)st * kRB * W;
+        T acc[kRB];
+#pragma unroll
+        for (int q = 0; q < kRB; q++) acc[q] = T{};
+        for (int c = tid; c < mb; c += NT) {
+            const int j = i0 - mb + c;
+            if (j < 0) continue;
+            const T yv = win[j & wmask];
+#pragma unroll
+            for (int q = 0; q < kRB; q++)
+                if (c >= q) acc[q] = Ops<T>::fms(acc[q], Lb[q * W + c - q], yv);
+        }
+        const T red = reduce_rows8<T>(acc, lane);
+        if ((lane & 3) == 0) part[wid * kRB + myr] = red;
+        __syncthreads();
+        if (wid == 0) {
+            T tv = Ops<T>::from(rv[st * kRB + myr]);
+#pragma unroll
+            for (int w = 0; w < kSweepWarps; w++) tv = Ops<T>::add(tv, part[w * kRB + myr]);
+            const T rinv = Ops<T>::rcp(Lb[myr * W + mb]);
+            T lt[kRB];
+#pragma unroll
+            for (int q = 0; q < kRB; q++) {
+                const int off = mb - myr + q;  // column i0 + q of row i0 + myr
+                lt[q] = (q < myr && off >= 0) ? Lb[myr * W + off] : T{};
+            }
+#pragma unroll
+            for (int q = 0; q < kRB - 1; q++) {
+                const T yq = Ops<T>::shfl(Ops<T>::mul(tv, rinv), 4 * q);
+                if (q < myr) tv = Ops<T>::fms(tv, lt[q], yq);
+            }
+            const T ymine = Ops<T>::mul(tv, rinv);
+            if ((lane & 3) == 0 && myr < nr) {
+                win[(i0 + myr) & wmask] = ymine;
+                y[i0 + myr] = ymine;
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            fence_proxy_async();
+            issue(t + S);
+        }
+    }
+}
+
+template <typename T, int S>
+__global__ __launch_bounds__(32 * kSweepWarps) void k_bwd_mw(DevProblem P, DevBatch B, int nrhs, int wmask) {
+    extern __shared__ __align__(128) unsigned char sm_raw[];
+    constexpr int NT = 32 * kSweepWarps;
+    const int n = P.n, mb = P.mb, W = mb + 1, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int item = blockIdx.x;
+    if (item >= B.nsys * nrhs) return;
+    if (B.nprev && *B.nprev == 0) return;
+    if (B.active && !B.active[item]) return;
+    const SolveLayout lay = solve_layout<T, S>(W, wmask + 1);
+    uint64_t *bar = (uint64_t *)(sm_raw + lay.bars);
+    T *rows = (T *)(sm_raw + lay.rows);
+    T *win = (T *)(sm_raw + lay.win);
+    T *ent = (T *)(sm_raw + lay.ent);
+    T *xs = (T *)(sm_raw + lay.part);  // the block's kRB solution entries
+    const T *L = (const T *)B.L + (size_t)(item / nrhs) * B.lpitch;
+    T *y = (T *)B.y + (size_t)item * n;
+    const int nblk = (n + kRB - 1) / kRB;
+    // warp 0: use u = 0, 1, ... processes block t = nblk - 1 - u
+    auto issue = [&](int u) {
+        const int t = nblk - 1 - u;
+        if (t >= 0) {
+            const int st = u % S, i0 = t * kRB;
+            if (lane == 0) {
+                const int nr = min(kRB, n - i0);
+                const uint32_t bl = ((uint32_t)(nr * W * (int)sizeof(T)) + 15u) & ~15u;
+                mbar_expect_tx(&bar[st], bl);
+                bulk_g2s(rows + (size_t)st * kRB * W, L + (size_t)i0 * W, bl, &bar[st]);
+            }
+            const int j = i0 - mb + lane;  // entering column (not for the last block)
+            if (u > 0 && lane < kRB && j >= 0) cp_async_elem<T>(ent + st * kRB + lane, y + j);
+        }
+        cp_commit();
+    };
+    const int i0l = (nblk - 1) * kRB;
+    for (int j = max(0, i0l - mb) + tid; j < n; j += NT) win[j & wmask] = y[j];
+    if (tid == 0) {
+        for (int q = 0; q < S; q++) mbar_init(&bar[q], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    if (wid == 0)
+        for (int u = 0; u < S; u++) issue(u);
+    const int myr = lane >> 2;
+    for (int u = 0; u < nblk; u++) {
+        const int t = nblk - 1 - u, st = u % S, i0 = t * kRB, nr = min(kRB, n - i0);
+        const bool ok = mbar_wait(&bar[st], (u / S) & 1);
+        if (wid == 0) cp_wait<S - 1>();
+        if (!__syncthreads_and(ok)) {
+            if (wid == 0) solve_timeout<S>(P, bar, u, min(nblk - 1, u + S - 1));
+            return;
+        }
+        const T *Lb = rows + (size_t)st * kRB * W;
+        if (wid == 0) {
+            {
+                const int j = i0 - mb + lane;
+                if (u > 0 && lane < kRB && j >= 0) win[j & wmask] = ent[st * kRB + lane];
+            }
+            __syncwarp();
+            T wv = win[(i0 + myr) & wmask];
+            const T rinv = Ops<T>::rcp(Lb[myr * W + mb]);
+            T lt[kRB];
+#pragma unroll
+            for (int q = 0; q < kRB; q++) {
+                const int off = mb - q + myr;  // column i0 + myr of row i0 + q
+                lt[q] = (myr < q && q < nr && off >= 0) ? Lb[q * W + off] : T{};
+            }
+            T xq[kRB];
+#pragma unroll
+            for (int q = kRB - 1; q >= 0; q--) {
+                xq[q] = Ops<T>::shfl(Ops<T>::mul(wv, rinv), 4 * q);
+                if (myr < q && q < nr) wv = Ops<T>::fms(wv, lt[q], xq[q]);
+            }
+            if ((lane & 3) == 0 && myr < nr) y[i0 + myr] = Ops<T>::mul(wv, rinv);
+            if (lane == 0) {
+#pragma unroll
+                for (int q = 0; q < kRB; q++) xs[q] = xq[q];
+            }
+        }
+        __syncthreads();
+        T xb[kRB];
+#pragma unroll
+        for (int q = 0; q < kRB; q++) xb[q] = xs[q];
+        for (int c = tid; c < mb; c += NT) {
+            const int j = i0 - mb + c;
+            if (j < 0) continue;
+            T w2 = win[j & wmask];
+#pragma unroll
+            for (int q = 0; q < kRB; q++)
+                if (q < nr && c >= q) w2 = Ops<T>::fms(w2, Lb[q * W + c - q], xb[q]);
+            win[j & wmask] = w2;
+        }
+        __syncthreads();
+        if (tid == 0) fence_proxy_async();
+        if (wid == 0) issue(u + S);
+    }
+    if (wid == 0) cp_wait<0>();
+}
+
 // The kernels' dynamic shared memory depends on the band width; contexts of
 // different widths may launch concurrently from several host threads, so the
 // limit is raised once to the device's opt-in maximum instead of per width.
@@ -308,8 +509,13 @@ static int set_solve_smem(int W, int WW) {
         int dev = 0, optin = 48 * 1024;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        cudaFuncSetAttribute(k_fwd<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-        cudaFuncSetAttribute(k_bwd<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        if constexpr (S == kStagesFew) {
+            cudaFuncSetAttribute(k_fwd_mw<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(k_bwd_mw<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        } else {
+            cudaFuncSetAttribute(k_fwd<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(k_bwd<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        }
     });
     return solve_layout<T, S>(W, WW).total;
 }
@@ -318,17 +524,24 @@ template <typename T, int S>
 static void fwd_launch(const DevProblem &P, const DevBatch &B, int nrhs, const double2 *rin, cudaStream_t st) {
     const int nitems = B.nsys * nrhs, W = P.mb + 1, WW = solve_window(P.mb);
     const int bytes = set_solve_smem<T, S>(W, WW);
-    k_fwd<T, S><<<nitems, 32, bytes, st>>>(P, B, nrhs, rin, WW - 1);
+    if constexpr (S == kStagesFew)
+        k_fwd_mw<T, S><<<nitems, 32 * kSweepWarps, bytes, st>>>(P, B, nrhs, rin, WW - 1);
+    else
+        k_fwd<T, S><<<nitems, 32, bytes, st>>>(P, B, nrhs, rin, WW - 1);
 }
 
 template <typename T, int S>
 static void bwd_launch(const DevProblem &P, const DevBatch &B, int nrhs, cudaStream_t st) {
     const int nitems = B.nsys * nrhs, W = P.mb + 1, WW = solve_window(P.mb);
     const int bytes = set_solve_smem<T, S>(W, WW);
-    k_bwd<T, S><<<nitems, 32, bytes, st>>>(P, B, nrhs, WW - 1);
+    if constexpr (S == kStagesFew)
+        k_bwd_mw<T, S><<<nitems, 32 * kSweepWarps, bytes, st>>>(P, B, nrhs, WW - 1);
+    else
+        k_bwd<T, S><<<nitems, 32, bytes, st>>>(P, B, nrhs, WW - 1);
 }
 
-// the deep pipeline for few sweeps, when its staging fits the block's shared memory
+// the deep pipeline with several warps per sweep for few sweeps, when its
+// staging fits the block's shared memory
 template <typename T>
 static bool use_few(const DevProblem &P, int nitems) {
     return nitems <= kFewItems && solve_layout<T, kStagesFew>(P.mb + 1, solve_window(P.mb)).total <= 200 * 1024;
