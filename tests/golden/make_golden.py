@@ -54,6 +54,10 @@ ROBUST_DC = "examples/DifferenceInversion/02/time0"
 # time0's volt05.dat); the grid is time0's
 DIFF_DC = "examples/DifferenceInversion/02"
 
+# data noise (src/make_noise.f90, src/rdati.f90:110-140, 257-290): the clean
+# data, the noise model (crt.noisemod, seed 1) and the noise the reference drew
+NOISE = "examples/MGS/01_simple/03_mgs"
+
 CUTMCK = {
     "minimal": "tests/minimal/Reference/grid",
     "mixed_surf": "tests/2.5D_mixed_surf/Reference/grid",
@@ -110,6 +114,14 @@ def main(ref: str):
         shutil.copyfile(os.path.join(src, f), os.path.join(out, dst))
     with open(os.path.join(out, "SOURCE"), "w") as fh:
         fh.write(DIFF_DC + "/{time0,time1}; grid: tests/golden/robust_dc (the same elem.dat, elec.dat)\n")
+    out = os.path.join(here, "noise_mgs")
+    os.makedirs(out, exist_ok=True)
+    src = os.path.join(ref, NOISE)
+    for f in ("mod/volt.dat", "exe/crt.noisemod", "exe/inv.mynoise_rho", "exe/inv.mynoise_pha",
+              "exe/inv.mynoise_voltages"):
+        shutil.copyfile(os.path.join(src, f), os.path.join(out, os.path.basename(f)))
+    with open(os.path.join(out, "SOURCE"), "w") as fh:
+        fh.write(NOISE + "/{mod,exe}\n")
     for name, d in CUTMCK.items():
         out = os.path.join(here, "cutmck_" + name)
         os.makedirs(out, exist_ok=True)

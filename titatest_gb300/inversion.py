@@ -21,8 +21,8 @@ src/inv.f90:560-640, DC inversion (ldc: the backends in DC mode,
 crgpu_set_dc, and the real update crgpu_update_dc) and robust inversion
 (lrobust: the reweighting of src/dmisft.f90:128-176), and difference
 inversion (ldiff: read_difference, the misfit and update against d0 - fm0).
-Prior models without reference-state data and data noise raise
-NotImplementedError.
+Data noise (lnse, noise.py) is added to the data as they are read.  Prior
+models without reference-state data raise NotImplementedError.
 """
 from __future__ import annotations
 
@@ -34,6 +34,7 @@ from typing import List, Optional
 import numpy as np
 
 from . import formats
+from . import noise as N
 from . import regularization as R
 
 _PI = math.acos(-1.0)
@@ -87,6 +88,7 @@ class CRTomoConfig:
     llamf: int = 0
     lamfix: float = 0.0
     lffhom: bool = False
+    noise: Optional[tuple] = None  # (iseed, A, B, A1, B1, A2, p0) when data noise is added
 
 
 def _cfg_lines(path: str):
@@ -175,6 +177,18 @@ def read_crtomo_cfg(path: str) -> CRTomoConfig:
     cfg.lffhom = cfg.stabp0 < 0  # src/rall.f90:470-471
     if cfg.lffhom:
         cfg.stabp0 = -cfg.stabp0
+    noisemod = os.path.join(os.path.dirname(os.path.abspath(path)), "crt.noisemod")
+    if cfg.stabw0 < 0:  # src/rall.f90:484-505: noise coupled to the error model, seed on the next line
+        cfg.stabw0 = -cfg.stabw0
+        iseed = 1
+        if not at_end():
+            try:
+                iseed = int(_tok(nxt())[0])
+            except (ValueError, IndexError):
+                iseed = 1
+        cfg.noise = (iseed, cfg.stabw0, cfg.stabm0, cfg.stabpA1, cfg.stabpB, cfg.stabpA2, cfg.stabp0)
+    elif os.path.exists(noisemod):  # src/rall.f90:480-516 (lnse2)
+        cfg.noise = N.read_noisemodel(noisemod)
     if (cfg.nx <= 0 or cfg.nz <= 0) and cfg.ltri == 0:
         cfg.ltri = 1
     if cfg.ltri == 0 and (cfg.nx < 2 or cfg.nz < 2):
@@ -290,10 +304,13 @@ def read_difference(data: Data, d0_path: str, fm0_path: str, m0_path: str, elanz
     return kept, m0
 
 
-def read_data(path: str, cfg: CRTomoConfig, eanz: int) -> Data:
+def read_data(path: str, cfg: CRTomoConfig, eanz: int, noise_records: Optional[list] = None) -> Data:
     """Measurements and their weights.  Without individual errors the error
     model err(R) = A1 |R| + A2 (as an error of ln R: 1e-2 A1 + A2/|R|) and
-    err(phase) = (A1p |R|^B + 1e-2 A2p |phase| + A3p) mrad."""
+    err(phase) = (A1p |R|^B + 1e-2 A2p |phase| + A3p) mrad, and with
+    cfg.noise the synthetic noise of the noise model on R and the phase
+    (noise.py; the weights keep the clean values' errors).  noise_records
+    receives per datum (g_r, g_p, eps_r, eps_p, R, phase, R_new, phase_new)."""
     rec = formats._Records(path)
     first = rec._tokens(rec.read_line())
     nanz = int(first[0])
@@ -310,6 +327,9 @@ def read_data(path: str, cfg: CRTomoConfig, eanz: int) -> Data:
     wp = np.zeros(nanz)
     wc = np.zeros(nanz)
     crtf = None
+    g_r = g_p = None
+    if cfg.noise is not None:  # src/rdati.f90:127-138, drawn before any datum
+        g_r, g_p = N.draw(cfg.noise, nanz, cfg.ldc)
     for i in range(nanz):
         t = rec._tokens(rec.read_line())
         if crtf is None:
@@ -332,6 +352,12 @@ def read_data(path: str, cfg: CRTomoConfig, eanz: int) -> Data:
             if bet <= 0.0:
                 raise formats.CRError(94, f"datum {i + 1}: resistance not positive")
             stabw = 1e-2 * cfg.stabw0 + cfg.stabm0 / bet
+            if g_r is not None:  # src/rdati.f90:257-290
+                gp = None if g_p is None else float(g_p[i])
+                nb, npha, er, ep = N.apply(bet, pha, float(g_r[i]), gp, cfg.noise, cfg.ldc)
+                if noise_records is not None:
+                    noise_records.append((float(g_r[i]), gp, er, ep, bet, pha, nb, npha))
+                bet, pha = nb, npha
         if bet <= 0.0:
             raise formats.CRError(94, f"datum {i + 1}: resistance not positive")
         if not cfg.ldc and abs(pha) > 1e3 * _PI:
@@ -1065,7 +1091,10 @@ def run_crtomo(exe_dir: str, precision: int = 1, refinement=(8, 1e-10), write: b
 
     grid = formats.read_elem(p(cfg.delem))
     enr = formats.read_elec(p(cfg.delectr), grid.sanz)
-    data = read_data(p(cfg.dstrom), cfg, len(enr))
+    recs: list = []
+    data = read_data(p(cfg.dstrom), cfg, len(enr), recs)
+    if write and cfg.noise is not None and recs:
+        N.write_records(exe_dir, data.strnr, data.vnr, recs, cfg.ldc)
     survey = formats.Survey(enr=enr, strnr=data.strnr, vnr=data.vnr, strom=np.ones(len(data.strnr)))
     if cfg.swrtr:
         from .crmod import rwaven
