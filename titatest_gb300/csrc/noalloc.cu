@@ -1,9 +1,11 @@
 // crgpu_factor_system_noalloc: the band factor of one (wavenumber, electrode)
-// system for callers that cannot allocate device memory at call time -- code
-// that runs while a CUDA graph is being captured, or inside a host framework
-// that owns all device memory through its own pool.  The caller passes the
-// conductivities and the two output buffers (device memory); everything the
-// kernels need in between lives in one file-scope device array.
+// system for callers that cannot allocate device memory when they call: a
+// host framework that hands out all device memory from its own pool (its
+// budget leaves nothing for allocations outside it), or a host that must not
+// make the implicit device-wide synchronisation of cudaMalloc/cudaFree in the
+// middle of its work.  The caller passes the conductivities and the two
+// output buffers (device memory); everything the kernels need in between,
+// including their error word, lives in one file-scope device array.
 //
 // The array (kScratchBytes) exists once on every GPU that loads the library
 // and stays allocated until the process exits.  Its device address is looked
@@ -27,11 +29,13 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 std::mutex g_mu;
 void *g_scratch_addr[kMaxDevices] = {};
 
-// status word, system wavenumber (relative) and electrode of the batch of one
+// status word, system wavenumber (relative), electrode of the batch of one,
+// and the problem-wide error word (kept here, not in the context)
 __global__ void k_noalloc_init(int *ints, int l) {
     ints[0] = 0;  // status: the kernels record errors with atomicCAS from 0
     ints[1] = 0;  // k relative to the shifted element arrays
     ints[2] = l;
+    ints[3] = 0;  // error word of the assembly and factor kernels
 }
 
 int fail(crgpu_ctx *c, int code, const std::string &msg) {
@@ -46,6 +50,7 @@ extern "C" int crgpu_factor_system_noalloc(crgpu_ctx *c, const void *sigma_devic
     if (!c || !sigma_device || !a_device || !fak_device) return ERR_ARG;
     if (k < 1 || k > c->K || l < 1 || l > c->eanz) return fail(c, ERR_ARG, "system (k, l) out of range");
     if (c->precision != CRGPU_PLAIN) return fail(c, ERR_UNSUPPORTED, "no-alloc factor: plain precision only");
+    if (c->P.ldc) return fail(c, ERR_UNSUPPORTED, "no-alloc factor: not available in DC mode");
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev != c->device || dev >= kMaxDevices)
         return fail(c, ERR_ARG, "no-alloc factor: the context's device must be current");
@@ -78,6 +83,7 @@ extern "C" int crgpu_factor_system_noalloc(crgpu_ctx *c, const void *sigma_devic
     // element arrays shifted to wavenumber k, so that the batch sees k = 0
     DevProblem Pk = P;
     Pk.K = 1;
+    Pk.err = ints + 3;  // the context's own error word is left alone
     Pk.elbg = P.elbg + (size_t)(k - 1) * P.elanz * 10;
     Pk.kg = P.kg + (size_t)(k - 1) * P.eanz * P.relanz;
     const int32_t ll = c->hg.lbeta ? l - 1 : 0;
@@ -92,7 +98,6 @@ extern "C" int crgpu_factor_system_noalloc(crgpu_ctx *c, const void *sigma_devic
     B.L = a_device;
     B.lpitch = (size_t)c->hg.n * (c->hg.mb + 1);  // one system
     B.status = ints;
-    if (cudaMemsetAsync(P.err, 0, sizeof(int), st) != cudaSuccess) return fail(c, ERR_CUDA, "memset");
     k_noalloc_init<<<1, 1, 0, st>>>(ints, ll);
     launch_adom(Pk, (const double2 *)sigma_device, adom, st);
     launch_assemble(Pk, B, (const double2 *)sigma_device, adom, st);
@@ -100,12 +105,12 @@ extern "C" int crgpu_factor_system_noalloc(crgpu_ctx *c, const void *sigma_devic
     launch_factor_plain(Pk, B, 1, c->nsm, st);
     cudaError_t ce = cudaGetLastError();
     if (ce != cudaSuccess) return fail(c, ERR_CUDA, cudaGetErrorString(ce));
-    int h[2] = {0, 0};
-    if (cudaMemcpyAsync(&h[0], ints, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaMemcpyAsync(&h[1], P.err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+    // the call waits for its kernels and reads the two status words back
+    int h[4] = {0, 0, 0, 0};
+    if (cudaMemcpyAsync(h, ints, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return fail(c, ERR_CUDA, "no-alloc factor: status read-back failed");
-    if (h[1]) return fail(c, h[1], "device reported error " + std::to_string(h[1]));
+    if (h[3]) return fail(c, h[3], "device reported error " + std::to_string(h[3]));
     if (h[0]) return fail(c, h[0], "system failed with error " + std::to_string(h[0]));
     return 0;
 }
