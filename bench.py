@@ -7,6 +7,7 @@ is the 200x60-quad, 96-electrode, 4000-quadrupole configuration (synthetic,
 seeded; titatest_gb300.synth.config2).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+  python bench.py --case --config C [--batch B] [--sens] ...   (one forward, for ncu)
 
 value : mixed mode (complex64 factor + FP64 refinement), inputs resident on
         the device, timed with CUDA events on the library's stream;
@@ -17,7 +18,7 @@ e2e   : the same unit through the host C ABI (crgpu_forward + crgpu_sens with
 plain : the complex128 mode on the same inputs (the reference arithmetic),
         with the mixed/plain speed-up and the error of mixed against plain.
 --impl reference times the oracle (the plain-C restatement of the reference
-routines, OpenMP over all host cores) on a bounded sample of the same unit.
+routines, OpenMP over all host cores) on whole units of the same workload.
 """
 from __future__ import annotations
 
@@ -118,48 +119,42 @@ def read_profile_traffic(name: str):
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline: the oracle (plain-C restatement, OpenMP) on a bounded sample
+# CPU baseline: the oracle (plain-C restatement, OpenMP) on whole units
 # ---------------------------------------------------------------------------
-def cpu_baseline(s, kwn, kwnwi, kpot, target_s=12.0, threads=None):
+def oracle_unit(P, sigma, kwn, kwnwi, threads):
+    """One whole unit on the oracle's timing build: the forward of every
+    (k, l) system with OpenMP over the wavenumbers (src/fem.f90:257-277,
+    327-397: at most kwnanz threads), rtrafo, bvolt, and bsens over every
+    measurement with OpenMP over the measurements (src/bsens.f90:94-100).
+    Returns (volt, sens (nanz, elanz) view, forward seconds, sens seconds)."""
+    t0 = time.perf_counter()
+    kp = P.forward(sigma, kwn, kwnwi, nthreads=threads)
+    hp = P.rtrafo(kp, kwnwi)
+    volt, _ = P.bvolt(hp, 0, None)
+    t1 = time.perf_counter()
+    sens = P.bsens(kp, kwn, kwnwi, sigma, volt, mode=0, nthreads=threads, contiguous=False)
+    t2 = time.perf_counter()
+    return volt, sens, t1 - t0, t2 - t1
+
+
+def cpu_baseline(s, kwn, kwnwi, threads=None, units=1):
+    """The oracle timed on `units` whole units of the workload (no sampling,
+    no scaling): forward on its own potentials, then the full Jacobian."""
     from oracle import oracle as O
     threads = threads or os.cpu_count() or 1
-    P = O.Problem(s.grid, s.survey)
-    K, E = len(kwn), s.survey.eanz
-    nsys = K * E
-    rng = np.random.default_rng(7)
-    # set-up (precal for all wavenumbers and electrodes) is timed once; then
-    # systems are solved in parallel (one per thread), as many rounds as fit
-    t0 = time.perf_counter()
-    P.forward_pairs(s.sigma, kwn, kwnwi, np.zeros((0, 2), np.int32), nthreads=threads)
-    t_setup = time.perf_counter() - t0
-    pairs_all = np.array([(k, l) for k in range(K) for l in range(E)], np.int32)
-    nsample = 2 * threads
-    t_fwd = 0.0
-    solved = 0
-    while t_fwd < target_s * 0.6 and solved < nsys:
-        pick = pairs_all[rng.choice(nsys, size=min(nsample, nsys), replace=False)]
-        t0 = time.perf_counter()
-        P.forward_pairs(s.sigma, kwn, kwnwi, pick, nthreads=threads)
-        t_fwd += time.perf_counter() - t0 - t_setup
-        solved += len(pick)
-    fwd_per_unit = t_setup + t_fwd / solved * nsys
-    # Jacobian: a sample of measurements (timing only; the numbers are those
-    # of the GPU kpot)
-    from titatest_gb300 import formats as F
-    q = max(threads * 4, 64)
-    idx = rng.choice(s.survey.nanz, size=min(q, s.survey.nanz), replace=False)
-    sub = F.Survey(enr=s.survey.enr, strnr=s.survey.strnr[idx], vnr=s.survey.vnr[idx],
-                   strom=s.survey.strom[idx])
-    Ps = O.Problem(s.grid, sub)
-    t0 = time.perf_counter()
-    Ps.bsens(kpot, kwn, kwnwi, s.sigma, None, mode=0, nthreads=threads)
-    t_j = time.perf_counter() - t0
-    sens_per_unit = t_j / len(idx) * s.survey.nanz
-    unit_s = fwd_per_unit + sens_per_unit
+    P = O.Problem(s.grid, s.survey, timing=True)
+    fw, sj = [], []
+    for _ in range(units):
+        _, _, tf, ts = oracle_unit(P, s.sigma, kwn, kwnwi, threads)
+        fw.append(tf)
+        sj.append(ts)
+    unit_s = (sum(fw) + sum(sj)) / units
+    nsys = len(kwn) * s.survey.eanz
     return {"value": 1.0 / unit_s, "unit": "units/s", "cores": threads, "kind": "port",
-            "sample": (f"{solved} of {nsys} (k,l) systems and {len(idx)} of {s.survey.nanz} Jacobian rows, "
-                       f"scaled to one unit ({t_fwd + t_j:.1f} s of CPU work)"),
-            "seconds_per_unit": unit_s, "forward_s": fwd_per_unit, "sens_s": sens_per_unit}
+            "sample": (f"{units} whole unit(s): all {nsys} (k,l) systems (OpenMP over the {len(kwn)} wavenumbers, "
+                       f"as src/fem.f90) and all {s.survey.nanz} Jacobian rows (OpenMP over measurements, as "
+                       f"src/bsens.f90); oracle built with the reference's -O3 -ffast-math flags"),
+            "seconds_per_unit": unit_s, "forward_s": statistics.mean(fw), "sens_s": statistics.mean(sj)}
 
 
 def workload_string(cfg: int, s, K: int) -> str:
@@ -170,31 +165,66 @@ def workload_string(cfg: int, s, K: int) -> str:
             f"{sv.nanz} quadrupoles, {K} wavenumbers ({nsys} band systems)")
 
 
+def _product_library_mapped() -> bool:
+    """True when libcrtomo_gb300.so is mapped into this process."""
+    try:
+        with open("/proc/self/maps") as f:
+            return any("libcrtomo_gb300" in line for line in f)
+    except OSError:
+        return False
+
+
+def workload_config(cfg: int, s, K: int) -> dict:
+    """The `config` object of both arms (identical for the same workload)."""
+    g, sv = s.grid, s.survey
+    nsys = K * sv.eanz
+    return {"workload": workload_string(cfg, s, K),
+            "l2": "inputs larger than L2: the band factors of all %d systems are %.1f GB in complex64"
+                  % (nsys, nsys * g.sanz * (g.mb + 1) * 8 / 1e9)}
+
+
 def run_reference(args):
+    """The reference arm: the oracle port of the reference routines (the
+    Fortran reference cannot be built without a Fortran compiler) on whole
+    units of the same workload, on the host cores.  The inputs come from the
+    same seeded generator as the GPU arm, renumbered by the oracle's own
+    CutMcK; no part of the GB300 library is loaded (checked below)."""
     rank, world, _ = _dist_env()
     if rank != 0:
         return 0
-    from titatest_gb300 import synth
     from oracle import oracle as O
-    s = synth.make(args.config)
-    P = O.Problem(s.grid, s.survey)
+    from titatest_gb300 import synth  # numpy input generator; cutmck from the oracle
+    threads = os.cpu_count() or 1
+    s = synth.make(args.config, cutmck=O.cutmck)
+    P = O.Problem(s.grid, s.survey, timing=True)
     kwn, kwnwi = P.rwaven()
-    # potentials for the Jacobian timing: zeros have the same cost
-    kpot = np.zeros((len(kwn), s.survey.eanz, s.grid.sanz), np.complex128)
-    vals = []
-    for it in range(args.warmup + args.steps):
-        cb = cpu_baseline(s, kwn, kwnwi, kpot, target_s=args.ref_seconds)
-        if it >= args.warmup:
-            vals.append(cb["value"])
-    v = statistics.median(vals)
-    cb["value"] = v
+    for _ in range(args.warmup):
+        oracle_unit(P, s.sigma, kwn, kwnwi, threads)
+    fw, sj = [], []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _, _, tf, ts = oracle_unit(P, s.sigma, kwn, kwnwi, threads)
+        fw.append(tf)
+        sj.append(ts)
+    wall = time.perf_counter() - t0
+    v = args.steps / wall
+    mapped = _product_library_mapped()
+    if mapped:
+        raise RuntimeError("the GB300 library was loaded into the reference arm")
+    nsys = len(kwn) * s.survey.eanz
+    cb = {"value": v, "unit": "units/s", "cores": threads, "kind": "port",
+          "sample": (f"{args.steps} whole units: all {nsys} (k,l) systems (OpenMP over the {len(kwn)} wavenumbers, "
+                     f"as src/fem.f90) and all {s.survey.nanz} Jacobian rows (OpenMP over measurements, as "
+                     f"src/bsens.f90) per unit"),
+          "seconds_per_unit": wall / args.steps, "forward_s": statistics.mean(fw), "sens_s": statistics.mean(sj)}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "units/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-            "data": "synthetic (seeded)",
-            "config": {"workload": workload_string(args.config, s, len(kwn)),
-                       "parallelism": f"OpenMP {cb['cores']} threads"},
-            "cpu_baseline": cb,
+            "data": "synthetic (seeded model and survey with the configuration's shapes)",
+            "config": workload_config(args.config, s, len(kwn)),
+            "parallelism": f"OpenMP {threads} threads (host cores)",
+            "cpu_baseline": cb, "product_library_mapped": mapped,
+            "build": "oracle/crt_oracle.c with -O3 -ftree-vectorize -ffast-math -finline-functions -fopenmp",
             "e2e": {"value": v, "unit": "units/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -340,15 +370,12 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64 factor + f64 refinement (c128 assembly, residuals, quadrature, J)",
         "data": "synthetic (seeded model and survey with the configuration's shapes)",
-        "config": {"workload": workload_string(args.config, s, K),
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "launch": "forward + Jacobian calls" if args.no_graph else
-                             "forward + Jacobian as one CUDA graph (crgpu_forward_sens_graph)",
-                   "l2": "inputs larger than L2 (band factors of all systems, ~%d GB)" % int(
-                       nsys * n * (mb + 1) * 8 / 1e9),
-                   "refinement": {"maxit": args.refine_maxit, "tol": args.refine_tol,
-                                  "iterations": statistics.mean(iters)},
-                   "autotuned_kernels": tune},
+        "config": workload_config(args.config, s, K),
+        "parallelism": "replicas" if world > 1 else "single GPU",
+        "launch": "forward + Jacobian calls" if args.no_graph else
+                  "forward + Jacobian as one CUDA graph (crgpu_forward_sens_graph)",
+        "refinement": {"maxit": args.refine_maxit, "tol": args.refine_tol, "iterations": statistics.mean(iters)},
+        "autotuned_kernels": tune,
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
         "e2e": {"value": 1e3 / e2e_ms, "unit": "units/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -368,10 +395,10 @@ def run_gpu(args):
                      "note": "latency-bound band factor: each 4-column step is a serial panel plus 4 tf32 MMAs "
                              "(3 hi/lo products + row injection) on a 128x128 complex window"},
     }
-    if rank == 0 and args.cpu_baseline:
-        kpot = mixed.forward(s.sigma, kpot=True)["kpot"]
-        line["cpu_baseline"] = cpu_baseline(s, mixed.kwn, mixed.kwnwi, kpot, target_s=args.ref_seconds)
+    kwn, kwnwi = mixed.kwn, mixed.kwnwi
     mixed.close()
+    if rank == 0 and args.cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(s, kwn, kwnwi)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
@@ -479,15 +506,14 @@ def run_inversion(args):
             rows = inv.run()
             torch.cuda.synchronize()
             wall = time.perf_counter() - t0
-        kpot = b.m.forward(s.sigma, kpot=True)["kpot"] if args.cpu_baseline else None
     finally:
         b.close()
     cpu = None
-    if kpot is not None:
-        # the oracle on a bounded sample of the forward's systems and of the
-        # Jacobian's rows, scaled to the forwards and Jacobians of one GN
-        # iteration as this run made them (the CPU CG is not included)
-        cb = cpu_baseline(s, kwn, kwnwi, kpot, target_s=args.ref_seconds)
+    if args.cpu_baseline:
+        # the oracle on one whole forward + Jacobian unit, multiplied by the
+        # forwards and Jacobians of one GN iteration as this run made them
+        # (the CPU CG is not included)
+        cb = cpu_baseline(s, kwn, kwnwi)
         n_it_ = max(1, sum(1 for r in rows if r.kind == "IT") - 1)
         est = (calls["forward"] * cb["forward_s"] + calls["sens"] * cb["sens_s"]) / n_it_
         cpu = {"value": est, "unit": "s/iteration (forwards + Jacobians only)", "cores": cb["cores"],
@@ -513,6 +539,53 @@ def run_inversion(args):
     return 0
 
 
+def run_case(args):
+    """--case: one forward (and optionally the Jacobian, an update, the model
+    uncertainty) of a configuration, printed as plain timings: the command
+    that the ncu captures in profiles/ run.  --batch limits the systems per
+    factor batch, so that a capture holds one launch of known size."""
+    from titatest_gb300 import MIXED, PLAIN, CRMod, synth
+
+    s = synth.make(args.config)
+    prec = MIXED if args.precision == "mixed" else PLAIN
+    with CRMod(s.grid, s.survey, precision=prec) as m:
+        m.set_refinement(args.refine_maxit, args.refine_tol)
+        if args.batch:
+            g = s.grid
+            esz = 8 if prec == MIXED else 16
+            per = g.sanz * (g.mb + 1) * esz + (g.sanz * 12 * 16) + g.sanz * 8 + g.sanz * (3 * 16 + esz) + 64
+            m.set_memory_budget(int(per * args.batch + per // 2))
+        for _ in range(args.repeat):
+            t = time.time()
+            out = m.forward(s.sigma)
+            st = m.stats()
+            msg = (f"forward {1e3 * (time.time() - t):.1f} ms, batches {st['nbatches']}, factor "
+                   f"{st['ms_factor']:.1f} ms, solve {st['ms_solve']:.1f} ms, refinement {st['refine_iterations']}")
+            if args.sens:
+                J = m.sens(0)
+                msg += f", sens {m.stats()['ms_sens']:.1f} ms, |J|max {np.abs(J).max():.3e}"
+            print(msg, flush=True)
+        assert np.all(np.isfinite(out["volt"]))
+        if args.update_steps:
+            from titatest_gb300 import regularization as R
+            sa = m.forward(s.sigma, volt_mode=1)["sigmaa"]
+            m.sens_on_device(1)
+            dat = sa - np.log(1.03)
+            w = np.full(len(sa), 1.0 / 0.03 ** 2)
+            sm = R.bsmatmreg(s.grid, s.nx, s.nz)
+            t = time.time()
+            _, dpar, _, _, ncg = m.update(w, np.ones(len(sa), np.int32), dat, sa, 0, sm, nx=s.nx, lam=300.0,
+                                          eps=1e-4, ncgmax=args.update_steps, par=np.log(s.sigma))
+            print(f"update {1e3 * (time.time() - t):.1f} ms, {ncg} CG steps, |dpar|max {np.abs(dpar).max():.3e}",
+                  flush=True)
+            if args.mcm:
+                t = time.time()
+                d = m.mcm(w, np.ones(len(sa), np.int32), 0, sm, nx=s.nx, lam=300.0)
+                print(f"mcm {1e3 * (time.time() - t):.1f} ms for manz {len(d['cov1'])} (ata, ata_reg, Cholesky "
+                      f"inverse, resolution, cov2), min cov1 {d['cov1'].min():.3e}", flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -530,13 +603,23 @@ def main():
                     help="mixed refinement stop: max|dx| <= tol max|x|.  Default 0.1 on config 2 (one "
                          "correction: volt within 1.4e-7 and J within 9e-7 of complex128, against the targets "
                          "1e-6 / 1e-5; both errors are measured and checked in every line), 1e-2 elsewhere")
-    ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--workers", type=int, default=8, help="config 5: concurrent worker streams")
     ap.add_argument("--ensemble-count", type=int, default=256, help="config 5: number of problems")
+    ap.add_argument("--case", action="store_true",
+                    help="plain timings of one forward of --config (the command the ncu captures run)")
+    ap.add_argument("--precision", choices=["mixed", "plain"], default="mixed", help="--case: precision")
+    ap.add_argument("--batch", type=int, default=0, help="--case: systems per factor batch (0: as many as fit)")
+    ap.add_argument("--repeat", type=int, default=1, help="--case: forwards to run")
+    ap.add_argument("--sens", action="store_true", help="--case: also the Jacobian")
+    ap.add_argument("--update-steps", type=int, default=0,
+                    help="--case: also the CRTomo Jacobian and one update with at most this many CG steps")
+    ap.add_argument("--mcm", action="store_true", help="--case with --update-steps: also crgpu_mcm")
     args = ap.parse_args()
     if args.refine_tol is None:
-        args.refine_tol = 0.1 if args.config == 2 else 1e-2
+        args.refine_tol = 1e-8 if args.case else 0.1 if args.config == 2 else 1e-2
+    if args.case:
+        return run_case(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.config == 5:

@@ -4,8 +4,8 @@
  *
  * Every entry point replaces one reference routine (or one block of a
  * reference driver); the comment above each names it (paths relative to the
- * reference project root).  A Fortran host binds these with ISO_C_BINDING;
- * the binding is shown in INTEGRATION.md.
+ * reference project root).  A Fortran host binds these with ISO_C_BINDING
+ * (a module of BIND(C) interfaces, one per function below).
  *
  * Conventions
  *  - All array arguments are HOST pointers unless the name ends in _device.
@@ -123,6 +123,10 @@ int crgpu_set_dc(crgpu_ctx *ctx, int32_t ldc);
  * processed in batches that fit.  Default: 60% of free device memory. */
 int crgpu_set_memory_budget(crgpu_ctx *ctx, int64_t bytes);
 
+/* No counterpart in the reference.  Free and total memory of the current
+ * device (cudaMemGetInfo), for hosts that size memory budgets. */
+int crgpu_device_memory(int64_t *free_bytes, int64_t *total_bytes);
+
 /* ------------------------------------------------------------------ */
 /* forward modelling                                                    */
 /* ------------------------------------------------------------------ */
@@ -166,17 +170,20 @@ int crgpu_factor_system(crgpu_ctx *ctx, const double *sigma, int32_t k, int32_t 
                         double *a, double *fak);
 
 /* No counterpart in the reference.  The same band factor and fak as
- * crgpu_factor_system (plain precision contexts only), for callers that
- * cannot allocate device memory when they call: code running while a CUDA
- * graph is captured, or inside a framework that owns all device memory.
- * sigma_device (elanz complex), a_device (sanz*(mb+1) complex) and
- * fak_device (sanz) are caller-owned device buffers; stream may be NULL (the
- * context's stream).  The call allocates nothing: its scratch is one fixed
- * 8 MiB device array in the library (held on every GPU that loads it until
- * exit); systems needing more (16 + 32*(nnz + sanz) bytes) are rejected with
- * an error.  The first call on a device looks the array up and should come
- * before any stream capture.  Calls share the array: calls that overlap on
- * the GPU race. */
+ * crgpu_factor_system (plain precision, non-DC contexts only), for callers
+ * that cannot allocate device memory when they call: a host framework that
+ * hands out all device memory from its own pool, or a host that must not
+ * make the implicit device-wide synchronisation of cudaMalloc/cudaFree in the
+ * middle of its work.  sigma_device (elanz complex), a_device
+ * (sanz*(mb+1) complex) and fak_device (sanz) are caller-owned device
+ * buffers; stream may be NULL (the context's stream).  The call allocates
+ * nothing: its scratch, error word included, is one fixed 8 MiB device array
+ * in the library (held on every GPU that loads it until exit); systems
+ * needing more (16 + 32*(nnz + sanz) bytes) are rejected with 1001.  The
+ * first call on a device looks the array up (cudaGetSymbolAddress) and
+ * should come before any stream capture.  Every call shares the array, which
+ * keeps the last call's contents: calls that overlap on the GPU race.  The
+ * call waits for its kernels on `stream` and returns their status. */
 int crgpu_factor_system_noalloc(crgpu_ctx *ctx, const void *sigma_device, int32_t k, int32_t l,
                                 void *a_device, void *fak_device, void *stream);
 

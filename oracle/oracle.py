@@ -15,8 +15,13 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libcrt_oracle.so")
+# the same source built with the reference's optimisation flags
+# (configure.ac:19-26: -O3 -ffast-math ..., less -march=native), for timing
+# only: the parity checks use the strict build above
+_LIB_TIMING_PATH = os.path.join(_HERE, "_build", "libcrt_oracle_timing.so")
 _lock = threading.Lock()
 _lib = None
+_lib_timing = None
 
 i32p = C.POINTER(C.c_int)
 f64p = C.POINTER(C.c_double)
@@ -24,7 +29,9 @@ f64p = C.POINTER(C.c_double)
 
 def build(force: bool = False) -> str:
     src = os.path.join(_HERE, "crt_oracle.c")
-    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+    stale = [p for p in (_LIB_PATH, _LIB_TIMING_PATH)
+             if not os.path.exists(p) or os.path.getmtime(p) < os.path.getmtime(src)]
+    if force or stale:
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
@@ -46,28 +53,41 @@ class OrOpts(C.Structure):
                 ("rwdanz", C.c_int), ("rwdnr", i32p), ("rwd", f64p), ("ldc", C.c_int)]
 
 
+def _declare(L):
+    L.or_rwaven.restype = C.c_int
+    L.or_forward.restype = C.c_int
+    L.or_forward_pairs.restype = C.c_int
+    L.or_bvolt.restype = C.c_int
+    L.or_bkfak.restype = C.c_int
+    L.or_cutmck.restype = C.c_int
+    L.or_elbg.restype = C.c_int
+    L.or_precal_all.restype = C.c_int
+    L.or_update.restype = C.c_int
+    L.or_factor.restype = C.c_int
+    L.or_bsytop.restype = C.c_double
+    L.or_bessk0.restype = C.c_double
+    L.or_bessk0.argtypes = [C.c_double]
+    L.or_bessk1.restype = C.c_double
+    L.or_bessk1.argtypes = [C.c_double]
+    return L
+
+
+def lib_timing():
+    """The timing build (reference optimisation flags); not for parity."""
+    global _lib_timing
+    with _lock:
+        if _lib_timing is None:
+            build()
+            _lib_timing = _declare(C.CDLL(_LIB_TIMING_PATH))
+    return _lib_timing
+
+
 def lib():
     global _lib
     with _lock:
         if _lib is None:
             build()
-            L = C.CDLL(_LIB_PATH)
-            L.or_rwaven.restype = C.c_int
-            L.or_forward.restype = C.c_int
-            L.or_forward_pairs.restype = C.c_int
-            L.or_bvolt.restype = C.c_int
-            L.or_bkfak.restype = C.c_int
-            L.or_cutmck.restype = C.c_int
-            L.or_elbg.restype = C.c_int
-            L.or_precal_all.restype = C.c_int
-            L.or_update.restype = C.c_int
-            L.or_factor.restype = C.c_int
-            L.or_bsytop.restype = C.c_double
-            L.or_bessk0.restype = C.c_double
-            L.or_bessk0.argtypes = [C.c_double]
-            L.or_bessk1.restype = C.c_double
-            L.or_bessk1.argtypes = [C.c_double]
-            _lib = L
+            _lib = _declare(C.CDLL(_LIB_PATH))
     return _lib
 
 
@@ -76,9 +96,11 @@ def _p(a, t):
 
 
 class Problem:
-    """Holds the arrays of one grid + survey and the or_mesh view of them."""
+    """Holds the arrays of one grid + survey and the or_mesh view of them.
+    timing=True runs the timing build (reference optimisation flags)."""
 
-    def __init__(self, grid, survey):
+    def __init__(self, grid, survey, timing: bool = False):
+        self._L = lib_timing() if timing else lib()
         self.grid = grid
         self.survey = survey
         self._keep = dict(
@@ -109,7 +131,7 @@ class Problem:
     def rwaven(self):
         kwn = np.zeros(32)
         kwnwi = np.zeros(32)
-        n = lib().or_rwaven(C.byref(self.m), _p(kwn, f64p), _p(kwnwi, f64p))
+        n = self._L.or_rwaven(C.byref(self.m), _p(kwn, f64p), _p(kwnwi, f64p))
         if n < 0:
             raise RuntimeError(f"rwaven errnr {-n}")
         return kwn[:n].copy(), kwnwi[:n].copy()
@@ -117,7 +139,7 @@ class Problem:
     def refsig(self, sigma):
         sigma = np.ascontiguousarray(sigma, np.complex128)
         out = np.zeros(2)
-        lib().or_refsig(C.byref(self.m), _p(sigma, f64p), _p(out, f64p))
+        self._L.or_refsig(C.byref(self.m), _p(sigma, f64p), _p(out, f64p))
         return complex(out[0], out[1])
 
     def precal(self, kwn, sytop=0.0):
@@ -128,7 +150,7 @@ class Problem:
         relbg = np.zeros(max(g.relanz, 1) * 10)
         kg = np.zeros(max(g.relanz, 1) * self.survey.eanz * K)
         flags = np.zeros(2, np.int32)
-        e = lib().or_precal_all(C.byref(self.m), K, _p(kwn, f64p), C.c_double(sytop),
+        e = self._L.or_precal_all(C.byref(self.m), K, _p(kwn, f64p), C.c_double(sytop),
                                 _p(elbg, f64p), _p(relbg, f64p), _p(kg, f64p), _p(flags, i32p))
         if e:
             raise RuntimeError(f"precal errnr {e}")
@@ -174,7 +196,7 @@ class Problem:
         K = len(kwn)
         kpot = np.zeros((K, self.survey.eanz, g.sanz), np.complex128)
         o = self._opts(swrtr, int(lsr), int(lana), int(lsink), int(nsink), int(lsytop), int(nthreads))
-        e = lib().or_forward(C.byref(self.m), C.byref(o), K, _p(kwn, f64p), _p(kwnwi, f64p),
+        e = self._L.or_forward(C.byref(self.m), C.byref(o), K, _p(kwn, f64p), _p(kwnwi, f64p),
                              _p(sigma, f64p), _p(kpot, f64p))
         if e:
             raise RuntimeError(f"forward errnr {e}")
@@ -192,7 +214,7 @@ class Problem:
         o = self._opts(kw.get("swrtr", 1), int(kw.get("lsr", 0)), int(kw.get("lana", 0)),
                    int(kw.get("lsink", 0)), int(kw.get("nsink", 0)), int(kw.get("lsytop", 0)),
                    int(nthreads))
-        e = lib().or_forward_pairs(C.byref(self.m), C.byref(o), K, _p(kwn, f64p), _p(kwnwi, f64p),
+        e = self._L.or_forward_pairs(C.byref(self.m), C.byref(o), K, _p(kwn, f64p), _p(kwnwi, f64p),
                                    _p(sigma, f64p), len(pr), _p(pr, i32p), _p(kpot, f64p))
         if e:
             raise RuntimeError(f"forward errnr {e}")
@@ -207,7 +229,7 @@ class Problem:
         fak = np.zeros(g.sanz)
         o = self._opts(kw.get("swrtr", 1), 0, 0, int(kw.get("lsink", 0)), int(kw.get("nsink", 0)),
                    int(kw.get("lsytop", 0)), 0)
-        e = lib().or_factor(C.byref(self.m), C.byref(o), len(kwn), _p(kwn, f64p), _p(sigma, f64p),
+        e = self._L.or_factor(C.byref(self.m), C.byref(o), len(kwn), _p(kwn, f64p), _p(sigma, f64p),
                             int(k), int(l), _p(a, f64p), _p(fak, f64p))
         if e:
             raise RuntimeError(f"factor errnr {e}")
@@ -218,13 +240,13 @@ class Problem:
         kpot = np.ascontiguousarray(kpot, np.complex128)
         kwnwi = np.ascontiguousarray(kwnwi, np.float64)
         hpot = np.zeros((self.survey.eanz, g.sanz), np.complex128)
-        lib().or_rtrafo(C.byref(self.m), swrtr, len(kwnwi), _p(kwnwi, f64p), _p(kpot, f64p),
+        self._L.or_rtrafo(C.byref(self.m), swrtr, len(kwnwi), _p(kwnwi, f64p), _p(kpot, f64p),
                         _p(hpot, f64p))
         return hpot
 
     def bkfak(self):
         kfak = np.zeros(self.survey.nanz)
-        e = lib().or_bkfak(C.byref(self.m), _p(kfak, f64p))
+        e = self._L.or_bkfak(C.byref(self.m), _p(kfak, f64p))
         if e:
             raise RuntimeError(f"bkfak errnr {e}")
         return kfak
@@ -234,20 +256,23 @@ class Problem:
         volt = np.zeros(self.survey.nanz, np.complex128)
         sigmaa = np.zeros(self.survey.nanz, np.complex128)
         kf = None if kfak is None else np.ascontiguousarray(kfak, np.float64)
-        e = lib().or_bvolt(C.byref(self.m), mode, _p(hpot, f64p),
+        e = self._L.or_bvolt(C.byref(self.m), mode, _p(hpot, f64p),
                            None if kf is None else _p(kf, f64p), _p(volt, f64p), _p(sigmaa, f64p))
         if e:
             raise RuntimeError(f"bvolt errnr {e}")
         return volt, sigmaa
 
-    def bsens(self, kpot, kwn, kwnwi, sigma, volt=None, mode=0, swrtr=1, nthreads=0, sytop=0.0):
-        """sens as array (nanz, elanz) complex128 (C order; Fortran sens(i, m))."""
+    def bsens(self, kpot, kwn, kwnwi, sigma, volt=None, mode=0, swrtr=1, nthreads=0, sytop=0.0,
+              contiguous=True):
+        """sens as array (nanz, elanz) complex128 (C order; Fortran sens(i, m));
+        contiguous=False returns the transposed view of the column-major
+        result instead of a C-ordered copy."""
         g = self.grid
         kwn = np.ascontiguousarray(kwn, np.float64)
         kwnwi = np.ascontiguousarray(kwnwi, np.float64)
         K = len(kwn)
         elbg = np.zeros(g.elanz * 10 * K)
-        e = lib().or_elbg(C.byref(self.m), K, _p(kwn, f64p), C.c_double(sytop), _p(elbg, f64p))
+        e = self._L.or_elbg(C.byref(self.m), K, _p(kwn, f64p), C.c_double(sytop), _p(elbg, f64p))
         if e:
             raise RuntimeError(f"precal errnr {e}")
         kpot = np.ascontiguousarray(kpot, np.complex128)
@@ -256,26 +281,26 @@ class Problem:
                                     np.complex128)
         sens = np.zeros((g.elanz, self.survey.nanz), np.complex128)  # column-major (nanz, manz)
         o = self._opts(swrtr, 0, 0, 0, 0, 0, int(nthreads))
-        lib().or_bsens_elbg(C.byref(self.m), C.byref(o), mode, swrtr, K, _p(kwnwi, f64p),
+        self._L.or_bsens_elbg(C.byref(self.m), C.byref(o), mode, swrtr, K, _p(kwnwi, f64p),
                             _p(elbg, f64p), _p(kpot, f64p), _p(sigma, f64p), _p(volt, f64p),
                             _p(sens, f64p))
-        return np.ascontiguousarray(sens.T)
+        return np.ascontiguousarray(sens.T) if contiguous else sens.T
 
     def potana(self, l, kw, sigma0):
         pota = np.zeros(self.grid.sanz, np.complex128)
         s0 = np.array([sigma0.real, sigma0.imag])
-        lib().or_potana(C.byref(self.m), int(l), C.c_double(kw), _p(s0, f64p), _p(pota, f64p))
+        self._L.or_potana(C.byref(self.m), int(l), C.c_double(kw), _p(s0, f64p), _p(pota, f64p))
         return pota
 
     def bnachbar(self):
         g = self.grid
         nb = np.zeros((g.maxnk + 1, g.elanz), np.int32)
-        lib().or_bnachbar(C.byref(self.m), _p(nb, i32p))
+        self._L.or_bnachbar(C.byref(self.m), _p(nb, i32p))
         return nb  # [col][elem] == Fortran nachbar(elem, col)
 
     def bsmatmreg(self, nx, nz, alfx=1.0, alfz=1.0):
         sm = np.zeros((3, nx * nz))
-        lib().or_bsmatmreg(C.byref(self.m), nx, nz, C.c_double(alfx), C.c_double(alfz),
+        self._L.or_bsmatmreg(C.byref(self.m), nx, nz, C.c_double(alfx), C.c_double(alfz),
                            _p(sm, f64p))
         return sm
 
@@ -283,7 +308,7 @@ class Problem:
         g = self.grid
         sm = np.zeros((g.maxnk + 1, g.elanz))
         nb = np.ascontiguousarray(nachbar, np.int32)
-        lib().or_bsmatmtri(C.byref(self.m), _p(nb, i32p), C.c_double(alfx), C.c_double(alfz),
+        self._L.or_bsmatmtri(C.byref(self.m), _p(nb, i32p), C.c_double(alfx), C.c_double(alfz),
                            _p(sm, f64p))
         return sm
 

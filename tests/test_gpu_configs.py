@@ -1,0 +1,211 @@
+"""GPU parity on the benchmark configurations themselves, against the oracle.
+
+The workloads the bench measures are compared with the oracle's restatement of
+the reference routines on the same seeded inputs:
+
+  config 2  (200x60 quads, 12261 nodes, mb 121, 96 electrodes, 4000
+            quadrupoles, 1248 systems; the bench workload): the whole forward
+            (kpot, hpot, voltages) and 256 seeded Jacobian rows of
+            src/bsens.f90 (mode 0) and src/bsensi.f90 (mode 1), plain and
+            mixed at the bench's refinement setting;
+  config 4  (400x100 quads, 40501 nodes, mb 201, 192 electrodes, 2880
+            systems): 24 seeded (k, l) systems of src/fem.f90:327-397 against
+            the oracle's, in both precisions, and 64 Jacobian rows;
+  config 5  (the uneven ensemble): its smallest and median problems whole
+            (forward and every Jacobian row), its widest (mb 161) on 24
+            seeded systems and 64 Jacobian rows.
+
+Tolerances (relative, max-norm over the compared array), as in
+test_gpu_forward.py: plain complex128 1e-10; mixed complex64 + FP64
+refinement 1e-6 for potentials and voltages, 1e-5 for the Jacobian.
+
+Where the oracle cannot run the whole forward in seconds (configs 4 and the
+widest ensemble problem), its Jacobian rows are formed from the plain GPU
+potentials, which the sampled systems tie to the oracle at 1e-10.
+"""
+import numpy as np
+import pytest
+
+from conftest import relerr
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+PLAIN_TOL = 1e-10
+MIXED_POT_TOL = 1e-6
+MIXED_SENS_TOL = 1e-5
+
+
+def _sub_survey(sv, idx):
+    from titatest_gb300 import formats as F
+    return F.Survey(enr=sv.enr, strnr=sv.strnr[idx], vnr=sv.vnr[idx], strom=sv.strom[idx])
+
+
+def _oracle_rows(s, kp, kwn, kwnwi, volt, idx, mode):
+    """Rows idx of the oracle's sensitivities (each row depends only on its own
+    measurement, so a sub-survey gives the same numbers)."""
+    P = O.Problem(s.grid, _sub_survey(s.survey, idx))
+    return P.bsens(kp, kwn, kwnwi, s.sigma, volt[idx], mode=mode)
+
+
+# ---------------------------------------------------------------------------
+# config 2: the bench workload
+# ---------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def cfg2():
+    from titatest_gb300 import synth
+    s = synth.config2()
+    P = O.Problem(s.grid, s.survey)
+    kwn, kwnwi = P.rwaven()
+    kp = P.forward(s.sigma, kwn, kwnwi)
+    hp = P.rtrafo(kp, kwnwi)
+    volt, _ = P.bvolt(hp, 0, None)
+    idx = np.sort(np.random.default_rng(2002).choice(s.survey.nanz, size=256, replace=False))
+    rows = {mode: _oracle_rows(s, kp, kwn, kwnwi, volt, idx, mode) for mode in (0, 1)}
+    return s, kwn, kwnwi, kp, hp, volt, idx, rows
+
+
+def test_cfg2_wavenumbers_match_oracle(gpu_lib, cfg2):
+    from titatest_gb300.crmod import rwaven
+    s, kwn, kwnwi = cfg2[:3]
+    k2, w2 = rwaven(s.grid, s.survey)
+    np.testing.assert_allclose(k2, kwn, rtol=1e-14)
+    np.testing.assert_allclose(w2, kwnwi, rtol=1e-14)
+
+
+def test_cfg2_plain_whole_forward_and_jacobian_rows(gpu_lib, cfg2):
+    from titatest_gb300 import PLAIN, CRMod
+    s, kwn, kwnwi, kp, hp, volt, idx, rows = cfg2
+    assert s.grid.mb == 121 and len(kwn) * s.survey.eanz == 1248
+    with CRMod(s.grid, s.survey, kwn, kwnwi, precision=PLAIN) as m:
+        out = m.forward(s.sigma, kpot=True, hpot=True)
+        assert relerr(out["kpot"], kp) < PLAIN_TOL
+        assert relerr(out["hpot"], hp) < PLAIN_TOL
+        assert relerr(out["volt"], volt) < PLAIN_TOL
+        assert relerr(m.bsens()[idx], rows[0]) < PLAIN_TOL
+        assert relerr(m.bsensi()[idx], rows[1]) < PLAIN_TOL
+
+
+def test_cfg2_mixed_at_bench_setting_against_oracle(gpu_lib, cfg2):
+    """The bench's own setting: refinement maxit 8, tol 0.1 (one correction)."""
+    from titatest_gb300 import MIXED, CRMod
+    s, kwn, kwnwi, kp, hp, volt, idx, rows = cfg2
+    with CRMod(s.grid, s.survey, kwn, kwnwi, precision=MIXED) as m:
+        m.set_refinement(8, 0.1)
+        out = m.forward(s.sigma, kpot=True)
+        assert m.stats()["refine_iterations"] >= 1
+        assert relerr(out["volt"], volt) < MIXED_POT_TOL
+        assert relerr(out["kpot"], kp) < MIXED_POT_TOL
+        assert relerr(m.bsens()[idx], rows[0]) < MIXED_SENS_TOL
+        assert relerr(m.bsensi()[idx], rows[1]) < MIXED_SENS_TOL
+
+
+def test_cfg2_graph_replay_matches_oracle(gpu_lib, cfg2):
+    """The bench times the unit as a replayed CUDA graph: its voltages and
+    Jacobian rows, read back from the device buffers, against the oracle."""
+    import torch
+
+    from titatest_gb300 import MIXED, CRMod
+    s, kwn, kwnwi, kp, hp, volt, idx, rows = cfg2
+    nanz, manz = s.survey.nanz, s.grid.elanz
+    sig = torch.from_numpy(s.sigma.view(np.float64).copy()).cuda()
+    vd = torch.zeros(2 * nanz, dtype=torch.float64, device="cuda")
+    jd = torch.zeros(2 * nanz * manz, dtype=torch.float64, device="cuda")
+    with CRMod(s.grid, s.survey, kwn, kwnwi, precision=MIXED) as m:
+        m.set_stream(torch.cuda.current_stream().cuda_stream)
+        m.set_refinement(8, 0.1)
+        for _ in range(2):  # record, then replay
+            m.forward_sens_graph(sig.data_ptr(), vd.data_ptr(), 0, jd.data_ptr())
+        torch.cuda.synchronize()
+    v = vd.cpu().numpy().view(np.complex128)
+    J = jd.cpu().numpy().view(np.complex128).reshape(manz, nanz).T
+    assert relerr(v, volt) < MIXED_POT_TOL
+    assert relerr(J[idx], rows[0]) < MIXED_SENS_TOL
+
+
+# ---------------------------------------------------------------------------
+# config 4: mb 201 (the widest band of the configurations)
+# ---------------------------------------------------------------------------
+def _sampled_systems_and_rows(s, seed, npairs, nrows):
+    from titatest_gb300 import MIXED, PLAIN, CRMod
+    P = O.Problem(s.grid, s.survey)
+    kwn, kwnwi = P.rwaven()
+    K, E = len(kwn), s.survey.eanz
+    rng = np.random.default_rng(seed)
+    flat = np.sort(rng.choice(K * E, size=npairs, replace=False))
+    pairs = np.stack([flat // E, flat % E], 1).astype(np.int32)  # 0-based (k, l)
+    kp_or = P.forward_pairs(s.sigma, kwn, kwnwi, pairs)
+    idx = np.sort(rng.choice(s.survey.nanz, size=nrows, replace=False))
+    out = {}
+    for prec in (PLAIN, MIXED):
+        with CRMod(s.grid, s.survey, kwn, kwnwi, precision=prec) as m:
+            if prec == MIXED:
+                m.set_refinement(8, 1e-2)  # the setting of the config-4 bench
+            f = m.forward(s.sigma, kpot=True)
+            out[prec] = (f["kpot"], f["volt"], m.bsens()[idx], m.bsensi()[idx])
+    return kwn, kwnwi, pairs, kp_or, idx, out
+
+
+def _check_sampled(s, kwn, kwnwi, pairs, kp_or, idx, out):
+    from titatest_gb300 import MIXED, PLAIN
+    sel = (pairs[:, 0], pairs[:, 1])
+    kp_plain, volt_plain, J0p, J1p = out[PLAIN]
+    kp_mixed, volt_mixed, J0m, J1m = out[MIXED]
+    assert relerr(kp_plain[sel], kp_or[sel]) < PLAIN_TOL
+    assert relerr(kp_mixed[sel], kp_or[sel]) < MIXED_POT_TOL
+    assert relerr(volt_mixed, volt_plain) < MIXED_POT_TOL
+    # Jacobian rows of the oracle on the plain potentials (tied to the oracle above)
+    r0 = _oracle_rows(s, kp_plain, kwn, kwnwi, volt_plain, idx, 0)
+    r1 = _oracle_rows(s, kp_plain, kwn, kwnwi, volt_plain, idx, 1)
+    assert relerr(J0p, r0) < PLAIN_TOL
+    assert relerr(J1p, r1) < PLAIN_TOL
+    assert relerr(J0m, r0) < MIXED_SENS_TOL
+    assert relerr(J1m, r1) < MIXED_SENS_TOL
+
+
+def test_cfg4_sampled_systems_both_precisions(gpu_lib):
+    from titatest_gb300 import synth
+    s = synth.config4()
+    assert s.grid.mb == 201
+    _check_sampled(s, *_sampled_systems_and_rows(s, 4004, 24, 64))
+
+
+# ---------------------------------------------------------------------------
+# config 5: smallest, median and widest problem of the ensemble
+# ---------------------------------------------------------------------------
+def _config5_picks():
+    from titatest_gb300 import synth
+    shapes = synth.config5_shapes()
+    order = sorted(range(len(shapes)), key=lambda q: shapes[q][0] * shapes[q][1])
+    return order[0], order[len(order) // 2], order[-1]
+
+
+@pytest.mark.parametrize("which", [0, 1])
+def test_cfg5_small_and_median_problem_whole(gpu_lib, which):
+    from titatest_gb300 import MIXED, PLAIN, CRMod, synth
+    q = _config5_picks()[which]
+    s = synth.config5(indices=[q])[0]
+    P = O.Problem(s.grid, s.survey)
+    kwn, kwnwi = P.rwaven()
+    kp = P.forward(s.sigma, kwn, kwnwi)
+    volt, _ = P.bvolt(P.rtrafo(kp, kwnwi), 0, None)
+    J0 = P.bsens(kp, kwn, kwnwi, s.sigma, volt, mode=0)
+    J1 = P.bsens(kp, kwn, kwnwi, s.sigma, volt, mode=1)
+    for prec, pt, jt in ((PLAIN, PLAIN_TOL, PLAIN_TOL), (MIXED, MIXED_POT_TOL, MIXED_SENS_TOL)):
+        with CRMod(s.grid, s.survey, kwn, kwnwi, precision=prec) as m:
+            if prec == MIXED:
+                m.set_refinement(8, 1e-2)  # the setting of the config-5 bench
+            f = m.forward(s.sigma, kpot=True)
+            assert relerr(f["kpot"], kp) < pt
+            assert relerr(f["volt"], volt) < pt
+            assert relerr(m.bsens(), J0) < jt
+            assert relerr(m.bsensi(), J1) < jt
+
+
+def test_cfg5_widest_problem_sampled(gpu_lib):
+    from titatest_gb300 import synth
+    q = _config5_picks()[2]
+    s = synth.config5(indices=[q])[0]
+    assert s.grid.mb > 124  # beyond one 128-row tensor-memory window
+    _check_sampled(s, *_sampled_systems_and_rows(s, 5005, 24, 64))

@@ -31,7 +31,7 @@ EXPORTS = (
     "crgpu_rwaven", "crgpu_cutmck", "crgpu_bkfak", "crgpu_get_stats", "crgpu_factor_system_noalloc",
     "crgpu_adjoint", "crgpu_adjoint_device", "crgpu_autotune", "crgpu_get_tune", "crgpu_forward_sens_graph",
     "crgpu_set_boundary_values", "crgpu_update_fpi", "crgpu_blam0_jtj", "crgpu_set_dc", "crgpu_update_dc",
-    "crgpu_mcm", "crgpu_column_sums",
+    "crgpu_mcm", "crgpu_column_sums", "crgpu_device_memory",
 )
 
 
@@ -74,6 +74,15 @@ def lib() -> C.CDLL:
                     getattr(L, name).restype = C.c_int
             _lib = L
     return _lib
+
+
+def device_memory():
+    """(free, total) bytes of the current device (crgpu_device_memory)."""
+    fr, tot = C.c_int64(0), C.c_int64(0)
+    code = lib().crgpu_device_memory(C.byref(fr), C.byref(tot))
+    if code:
+        raise CRGPUError(code, "crgpu_device_memory")
+    return fr.value, tot.value
 
 
 def ptr(a: np.ndarray, t):

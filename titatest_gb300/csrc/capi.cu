@@ -824,6 +824,15 @@ int crgpu_set_memory_budget(crgpu_ctx *c, int64_t bytes) {
     return 0;
 }
 
+int crgpu_device_memory(int64_t *free_bytes, int64_t *total_bytes) {
+    if (!free_bytes || !total_bytes) return ERR_ARG;
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return ERR_CUDA;
+    *free_bytes = (int64_t)fr;
+    *total_bytes = (int64_t)tot;
+    return 0;
+}
+
 int crgpu_forward_device(crgpu_ctx *c, const void *sigma_device, int32_t volt_mode, const void *kfak_device,
                          void *volt_device, void *sigmaa_device) {
     if (!c || !sigma_device) return ERR_ARG;

@@ -20,6 +20,7 @@ from typing import List, Optional, Sequence
 import numpy as np
 
 from . import MIXED, CRMod
+from ._lib import device_memory
 
 
 def problem_work(p) -> float:
@@ -35,15 +36,13 @@ class Ensemble:
     def __init__(self, problems: Sequence, precision: int = MIXED, workers: int = 8,
                  refine_maxit: int = 8, refine_tol: float = 1e-6, budget_bytes: Optional[int] = None,
                  autotune: bool = False):
-        import torch
-
         self.problems = list(problems)
         self.precision = precision
         self.workers = max(1, int(workers))
         self.refine = (refine_maxit, refine_tol)
         self.autotune = autotune  # per problem shape, cached by the library after the first run
         if budget_bytes is None:
-            free, _ = torch.cuda.mem_get_info()
+            free, _ = device_memory()
             budget_bytes = int(0.5 * free / self.workers)
         self.budget = budget_bytes
         self.order = sorted(range(len(self.problems)), key=lambda i: -problem_work(self.problems[i]))

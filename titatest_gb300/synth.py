@@ -22,17 +22,20 @@ Configurations (seed = 1000*cfg + i):
      (a 1..6, n 1..10) sub-sampled, model of 2 plus two elliptic anomalies.
   5  ensemble of 256 problems, 40x15 ... 300x80 quads (log-uniform), 24-128
      electrodes at 1 m, 200-6000 dipole-dipole each.
+
+The generator itself is numpy only.  The Cuthill-McKee renumbering is the
+library's (crgpu_cutmck) unless a `cutmck(grid, enr) -> (grid, enr)` callable
+is passed: any implementation of cutmckee/cutmck.f gives the same integers.
 """
 from __future__ import annotations
 
 import dataclasses
 import math
-from typing import List, Optional, Tuple
+from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 
 from . import formats
-from .crmod import cutmck
 
 
 @dataclasses.dataclass
@@ -219,7 +222,9 @@ def _subsample(quads, k, rng):
     return [quads[i] for i in idx]
 
 
-def _finish(name, grid, surface, enodes, quads, mag, pha, nx, nz, triangles=False):
+def _finish(name, grid, surface, enodes, quads, mag, pha, nx, nz, triangles=False, cutmck=None):
+    if cutmck is None:
+        from .crmod import cutmck
     enr = surface[enodes]
     g2, enr2 = cutmck(grid, enr)
     s, v = _encode(quads)
@@ -232,7 +237,7 @@ def _finish(name, grid, surface, enodes, quads, mag, pha, nx, nz, triangles=Fals
 # ---------------------------------------------------------------------------
 # configurations
 # ---------------------------------------------------------------------------
-def config1(seed: int = 1000) -> Synthetic:
+def config1(seed: int = 1000, cutmck=None) -> Synthetic:
     rng = np.random.default_rng(seed)
     nx, nz = 60, 20
     grid, surface, X, Y = _quad_grid(np.arange(nx + 1, dtype=float), np.arange(nz + 1, dtype=float))
@@ -245,7 +250,7 @@ def config1(seed: int = 1000) -> Synthetic:
     pha = np.zeros(nx * nz)
     enodes = np.arange(1, 60, 2)               # 30 electrodes at 2 m
     quads = dipole_dipole(30, [1], range(1, 9))
-    return _finish("cfg1", grid, surface, enodes, quads, mag, pha, nx, nz)
+    return _finish("cfg1", grid, surface, enodes, quads, mag, pha, nx, nz, cutmck=cutmck)
 
 
 def _cfg2_depths():
@@ -270,7 +275,7 @@ def _topography(xs, rng, amp=2.0):
     return amp * t / (np.abs(t).max() + 1e-300)
 
 
-def config2(seed: int = 2000) -> Synthetic:
+def config2(seed: int = 2000, cutmck=None) -> Synthetic:
     rng = np.random.default_rng(seed)
     nx = 200
     xs = np.arange(nx + 1, dtype=float) - 52.0   # electrodes at x = 0..95
@@ -282,10 +287,10 @@ def config2(seed: int = 2000) -> Synthetic:
     enodes = np.arange(52, 52 + 96)
     dd = _subsample(dipole_dipole(96, range(1, 5), range(1, 9)), 2000, rng)
     ws = _subsample(wenner_schlumberger(96, range(1, 5), range(1, 9)), 2000, rng)
-    return _finish("cfg2", grid, surface, enodes, dd + ws, mag, pha, nx, nz)
+    return _finish("cfg2", grid, surface, enodes, dd + ws, mag, pha, nx, nz, cutmck=cutmck)
 
 
-def config3(seed: int = 3000) -> Synthetic:
+def config3(seed: int = 3000, cutmck=None) -> Synthetic:
     rng = np.random.default_rng(seed)
     nx, nz = 250, 100
     xs = np.arange(nx + 1, dtype=float) * 0.5 - 30.0
@@ -294,10 +299,10 @@ def config3(seed: int = 3000) -> Synthetic:
     mag, pha = random_model(grid, rng)
     enodes = np.arange(60, 60 + 2 * 64, 2)   # 64 electrodes at 1 m
     dd = _subsample(dipole_dipole(64, range(1, 5), range(1, 9)), 2000, rng)
-    return _finish("cfg3", grid, surface, enodes, dd, mag, pha, nx, nz, triangles=True)
+    return _finish("cfg3", grid, surface, enodes, dd, mag, pha, nx, nz, triangles=True, cutmck=cutmck)
 
 
-def config4(seed: int = 4000) -> Synthetic:
+def config4(seed: int = 4000, cutmck=None) -> Synthetic:
     rng = np.random.default_rng(seed)
     nx, nz = 400, 100
     xs = np.arange(nx + 1, dtype=float) * 0.5 - 52.0
@@ -313,16 +318,28 @@ def config4(seed: int = 4000) -> Synthetic:
         pha[inside] = -50.0
     enodes = np.arange(104, 104 + 192)
     dd = _subsample(dipole_dipole(192, range(1, 7), range(1, 11)), 20000, rng)
-    return _finish("cfg4", grid, surface, enodes, dd, mag, pha, nx, nz)
+    return _finish("cfg4", grid, surface, enodes, dd, mag, pha, nx, nz, cutmck=cutmck)
 
 
-def config5(seed: int = 5000, count: int = 256) -> List[Synthetic]:
+def _config5_shape(rng):
+    f = rng.uniform(0, 1)
+    nx = int(round(40 * (300 / 40) ** f))
+    nz = int(round(15 * (80 / 15) ** f))
+    return nx, nz
+
+
+def config5_shapes(seed: int = 5000, count: int = 256) -> List[Tuple[int, int]]:
+    """(nx, nz) quads of every ensemble problem, without building them."""
+    return [_config5_shape(np.random.default_rng(seed + q)) for q in range(count)]
+
+
+def config5(seed: int = 5000, count: int = 256, cutmck=None,
+            indices: Optional[Sequence[int]] = None) -> List[Synthetic]:
+    """The ensemble; `indices` builds only those problems (same seeds)."""
     out = []
-    for q in range(count):
+    for q in (range(count) if indices is None else indices):
         rng = np.random.default_rng(seed + q)
-        f = rng.uniform(0, 1)
-        nx = int(round(40 * (300 / 40) ** f))
-        nz = int(round(15 * (80 / 15) ** f))
+        nx, nz = _config5_shape(rng)
         ne = int(rng.integers(24, min(128, nx - 4) + 1))
         first = (nx - ne) // 2
         xs = np.arange(nx + 1, dtype=float) - first
@@ -332,10 +349,11 @@ def config5(seed: int = 5000, count: int = 256) -> List[Synthetic]:
         enodes = np.arange(first, first + ne)
         allq = dipole_dipole(ne, range(1, 7), range(1, 11))
         k = int(rng.integers(200, 6001))
-        out.append(_finish(f"cfg5_{q}", grid, surface, enodes, _subsample(allq, k, rng), mag, pha, nx, nz))
+        out.append(_finish(f"cfg5_{q}", grid, surface, enodes, _subsample(allq, k, rng), mag, pha, nx, nz,
+                           cutmck=cutmck))
     return out
 
 
-def make(cfg: int, seed: Optional[int] = None):
+def make(cfg: int, seed: Optional[int] = None, cutmck=None):
     f = {1: config1, 2: config2, 3: config3, 4: config4, 5: config5}[cfg]
-    return f() if seed is None else f(seed)
+    return f(cutmck=cutmck) if seed is None else f(seed, cutmck=cutmck)
