@@ -1,0 +1,126 @@
+"""Byte-level output (titatest_gb300.fortran_io) against the reference's own files.
+
+The reference's result files hold gfortran's list-directed records.  Every
+record of the files below is parsed and written again by the emulator; the
+bytes must be identical (each REAL*4 value is recovered exactly from its 9
+significant digits, each REAL*8 from its 17).  The inv.ctr lines go through
+the T/G/I/F edit descriptors of src/kont2.f90:33-50.
+
+tests/golden/mixed_surf/volt.dat is left out: it was written by another
+compiler's list-directed output (7-digit 0.dddE-xx fields in 10-column
+integers), not gfortran's.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+from titatest_gb300 import fortran_io as F
+
+LIST_FILES = [
+    ("minimal", "volt.dat"), ("testmodinv", "volt.dat"), ("decoupling_2d_sink", "volt.dat"),
+    ("minimal", "volt01.dat"), ("mixed_surf", "volt01.dat"),
+    ("minimal", "rho01.mag"), ("minimal", "rho01.pha"), ("minimal", "rho02.mag"),
+    ("mixed_surf", "rho01.mag"), ("mixed_surf", "rho01.pha"),
+    ("minimal", "coverage.mag"), ("minimal", "coverage.mag_fpi"),
+]
+
+
+def _kinds(name, ln, toks):
+    if toks[0] == "Max:":
+        return ["s", "r8"]
+    if ln == 0:
+        return ["i", "tab", "r8"] if name.startswith("rho") else ["i"]
+    if name.startswith("volt"):
+        return ["i", "i", "r4", "r4"] + ["i"] * (len(toks) - 4)
+    if name.startswith("rho"):
+        return ["r4"] * 3
+    return ["r8"] * 3
+
+
+@pytest.mark.parametrize("case,name", LIST_FILES)
+def test_list_directed_records_are_byte_identical(case, name):
+    text = open(os.path.join(GOLDEN, case, name)).read()
+    lines = text.split("\n")[:-1]
+    out = []
+    for ln, line in enumerate(lines):
+        toks = line.split()
+        if ln == 0 and name.startswith("rho"):
+            toks = [toks[0], "\t", toks[1]]  # elanz, ACHAR(9), rms
+        items = []
+        for k, t in zip(_kinds(name, ln, toks), toks):
+            items.append({"i": lambda t: F.int4(int(t)), "tab": lambda t: F.char("\t"), "s": F.char,
+                          "r4": lambda t: F.real4(float(t)), "r8": lambda t: F.real8(float(t))}[k](t))
+        out.append(F.record(items))
+    assert "".join(out) == text
+
+
+def test_list_directed_edge_values():
+    assert F.real4(0.0) == "   0.00000000    "
+    assert F.real4(-0.0) == "  -0.00000000    "
+    assert F.real4(0.1) == "  0.100000001    "
+    assert F.real4(0.09999999) == "   9.99999866E-02"  # the REAL*4 nearest 0.09999999
+    assert F.real4(123456789.0) == "   123456792.    "
+    assert F.real4(1e9) == "   1.00000000E+09"
+    assert F.real4(-3.5e-20) == "  -3.49999989E-20"
+    assert F.real4(999999999.0) == "   1.00000000E+09"  # rounds to 10^9: E editing
+    assert F.real8(1e-3) == "   1.0000000000000000E-003"
+    assert F.real8(-2.25) == "  -2.2500000000000000     "
+    assert F.int4(-7) == "          -7"
+
+
+def test_edit_descriptors():
+    assert F.fmt_G(111.9, 10, 4) == " 111.9    "
+    assert F.fmt_G(1360.0, 9, 3) == "0.136E+04"
+    assert F.fmt_G(0.0, 10, 4) == " 0.000    "
+    assert F.fmt_G(36.68, 10, 4) == " 36.68    "
+    assert F.fmt_G(0.05, 10, 4) == "0.5000E-01"
+    assert F.fmt_F(1.0, 5, 3) == "1.000"
+    assert F.fmt_G(784.0, 9, 3) == " 784.    "
+    assert F.fmt_F(-0.25, 10, 4) == "   -0.2500"
+    assert F.fmt_I(30, 6) == "    30"
+    assert F.fmt_A("IT", 3) == " IT"
+
+
+def test_inv_ctr_iteration_lines_are_byte_identical():
+    """The IT/UP lines of the reference's minimal run, rebuilt from their
+    values through format_rows.  The golden files hold the CG count two
+    columns left of where src/kont2.f90:39-50 (t58, i6) puts it (they were
+    written by an earlier build of kont2); the check moves it back and
+    compares every other byte as it stands."""
+    from titatest_gb300.inversion import Row, format_rows
+    text = open(os.path.join(GOLDEN, "minimal", "inv.ctr")).read().split("\n")
+    picked = [ln for ln in text if ln[:3].strip() in ("IT", "UP", "PIT", "PUP") and ln[4:7].strip().isdigit()]
+    assert len(picked) > 10
+    for ln in picked:
+        kind = ln[:3].strip()
+        idx = int(ln[4:7])
+        f = lambda a, b: float(ln[a - 1:b]) if ln[a - 1:b].strip() else 0.0
+        if len(ln) > 96:  # the count: columns 56-61 in the golden, 58-63 in the format
+            ln = ln[:55] + "  " + ln[55:61] + ln[63:]
+        if len(ln) <= 96:  # format 101: the first line of a stage
+            r = Row(kind, idx, f(11, 20), betrms=f(69, 78), pharms=f(81, 90), npol=int(ln[92:96]), first=True)
+        elif kind.endswith("IT"):
+            r = Row(kind, idx, f(11, 20), bdpar=f(23, 32), lam=f(34, 43), rough=f(46, 55), ncg=int(ln[57:63]),
+                    betrms=f(69, 78), pharms=f(81, 90), npol=int(ln[92:96]), step=f(105, 109))
+        else:
+            r = Row(kind, idx, f(11, 20), bdpar=f(23, 31), lam=f(34, 43), rough=f(46, 55), ncg=int(ln[57:63]),
+                    step=f(105, 109))
+        assert format_rows([r]) == ln + "\n", ln
+
+
+def test_written_volt_file_layout(tmp_path):
+    """formats.write_volt: gfortran's records for computed values."""
+    from titatest_gb300 import formats
+    s = np.array([10002, 10002], np.int32)
+    v = np.array([40003, 50004], np.int32)
+    sa = np.array([0.0491579510, -0.0137898624 + 1e-9j])
+    p = tmp_path / "volt.dat"
+    formats.write_volt(str(p), s, v, sa)
+    lines = p.read_text().split("\n")
+    assert lines[0] == "           2"
+    assert lines[1] == "       10002       40003   4.91579510E-02   0.00000000    "
+    # a wrapped phase swaps the voltage electrodes (src/wdatm.f90:66-71)
+    assert lines[2].startswith("       10002       40005   1.37898624E-02")

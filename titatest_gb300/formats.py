@@ -26,6 +26,8 @@ from typing import List, Optional, Sequence
 
 import numpy as np
 
+from . import fortran_io as FIO
+
 
 class CRError(RuntimeError):
     """Error carrying one of the reference's error numbers (src/error.txt)."""
@@ -440,14 +442,14 @@ def volt_record(sigmaa: np.ndarray, strnr: np.ndarray, vnr: np.ndarray):
 
 
 def write_volt(path: str, strnr, vnr, sigmaa):
-    """src/wdatm.f90: magnitude and phase in real*4, polarity swapped where
-    the phase wraps."""
+    """src/wdatm.f90:55-76, byte for byte as gfortran writes it: nanz, then
+    strnr, vnr, real(|sigmaa|), real(1e3 phase) list-directed, with the
+    voltage electrodes swapped where the phase wraps."""
     bet, pha, vout = volt_record(np.asarray(sigmaa), np.asarray(strnr), np.asarray(vnr))
     with open(path, "w") as fh:
-        fh.write(f"{len(strnr):12d}\n")
+        fh.write(FIO.record([FIO.int4(len(strnr))]))
         for s, v, b, p in zip(strnr, vout, bet, pha):
-            fh.write(f"{int(s):12d}{int(v):12d} {float(np.float32(b)):16.8E}"
-                     f" {float(np.float32(p)):16.8E}\n")
+            fh.write(FIO.record([FIO.int4(s), FIO.int4(v), FIO.real4(b), FIO.real4(p)]))
 
 
 def read_volt(path: str):
@@ -530,11 +532,9 @@ def write_boundary_values(path: str, nodes, values):
 
 
 def f4(x) -> str:
-    """A REAL*4 value as list-directed output prints it: 9 significant digits."""
-    x = float(np.float32(x))
-    if x == 0.0 or 1e-1 <= abs(x) < 1e8:
-        return f"{x:.9g}"
-    return f"{x:.8E}"
+    """A REAL*4 value as gfortran's list-directed output prints it (9
+    significant digits), without the field's padding."""
+    return FIO.real4(x).strip()
 
 
 def numbered_path(datei: str, i: int, count: int) -> str:
@@ -562,9 +562,9 @@ def write_potentials(datei: str, hpot: np.ndarray, strnr, strom, grid: "Grid"):
             pot = -hpot[e1 - 1] * strom[i]
         else:
             pot = (hpot[e2 - 1] - hpot[e1 - 1]) * strom[i]
-        with open(numbered_path(datei, i + 1, nanz), "w") as fh:
-            for j in range(len(pot)):
-                fh.write(f"  {f4(x[j])}  {f4(y[j])}  {f4(pot[j].real)}  {f4(pot[j].imag)}\n")
+        with open(numbered_path(datei, i + 1, nanz), "w") as fh:  # src/wpot.f90:82-85
+            fh.write("".join(FIO.record([FIO.real4(x[j]), FIO.real4(y[j]), FIO.real4(pot[j].real),
+                                         FIO.real4(pot[j].imag)]) for j in range(len(pot))))
 
 
 def write_sensitivities(datei: str, sens: np.ndarray, cx: np.ndarray, cy: np.ndarray):
@@ -575,13 +575,13 @@ def write_sensitivities(datei: str, sens: np.ndarray, cx: np.ndarray, cy: np.nda
     os.makedirs(os.path.dirname(datei) or ".", exist_ok=True)
     for i in range(nanz):
         summe = complex(np.sum(sens[i]))
-        with open(numbered_path(datei, i + 1, nanz), "w") as fh:
+        with open(numbered_path(datei, i + 1, nanz), "w") as fh:  # src/wsens.f90:82-93
             if abs(summe) > 0.0:
-                fh.write(f"  {f4(abs(summe))}  {f4(1e3 * math.atan2(summe.imag, summe.real))}\n")
+                fh.write(FIO.record([FIO.real4(abs(summe)), FIO.real4(1e3 * math.atan2(summe.imag, summe.real))]))
             else:
-                fh.write("   0.00000000       0.00000000\n")
-            for j in range(sens.shape[1]):
-                fh.write(f"  {f4(cx[j])}  {f4(cy[j])}  {f4(sens[i, j].real)}  {f4(sens[i, j].imag)}\n")
+                fh.write(FIO.record([FIO.real4(0.0), FIO.real4(0.0)]))
+            fh.write("".join(FIO.record([FIO.real4(cx[j]), FIO.real4(cy[j]), FIO.real4(sens[i, j].real),
+                                         FIO.real4(sens[i, j].imag)]) for j in range(sens.shape[1])))
 
 
 @dataclasses.dataclass

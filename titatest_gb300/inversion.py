@@ -34,6 +34,7 @@ from typing import List, Optional
 import numpy as np
 
 from . import formats
+from . import fortran_io as FIO
 from . import noise as N
 from . import regularization as R
 
@@ -1016,57 +1017,66 @@ class Inversion:
 
 
 def format_rows(rows: List[Row]) -> str:
-    """The IT/UP lines in the columns of src/kont2.f90 (formats 101, 105,
-    111); the numbers in Python's g notation, not Fortran's G edit."""
+    """The IT/UP lines of inv.ctr, byte for byte as the formats 100-111 of
+    src/kont2.f90:33-50 lay them out (T positions, A3, I3, G10.4, G9.3, I6,
+    I4, F5.3)."""
+    A, I, G, Fx = FIO.fmt_A, FIO.fmt_I, FIO.fmt_G, FIO.fmt_F
     out = []
     for r in rows:
-        if r.first:
-            out.append(f"{r.kind:>3s}{r.index:4d}   {r.nrmsd:10.4g}{'':48s}{r.betrms:10.4g}  {r.pharms:10.4g}  {r.npol:4d}")
-        elif r.kind.endswith("IT"):
-            out.append(f"{r.kind:>3s}{r.index:4d}   {r.nrmsd:10.4g}  {r.bdpar:10.4g} {r.lam:10.4g}  {r.rough:10.4g}  "
-                       f"{r.ncg:6d}     {r.betrms:10.4g}  {r.pharms:10.4g}  {r.npol:4d}        {r.step:5.3f}")
-        else:
-            out.append(f"{r.kind:>3s}{r.index:4d}   {r.nrmsd:10.4g}  {r.bdpar:9.3g}  {r.lam:10.4g}  {r.rough:10.4g}  "
-                       f"{r.ncg:6d}{'':46s}{r.step:5.3f}")
-    return "\n".join(out) + "\n"
+        robust = r.l1rat is not None
+        head = [(1, A(r.kind, 3)), (5, I(r.index, 3)), (11, G(r.nrmsd, 10, 4))]
+        if r.first:  # formats 100 / 101
+            f = head + [(69, G(r.betrms, 10, 4)), (81, G(r.pharms, 10, 4)), (93, I(r.npol, 4))]
+            if robust:
+                f.append((105, G(r.l1rat, 9, 3)))
+        elif r.kind.endswith("IT"):  # formats 110 / 111
+            f = head + [(23, G(r.bdpar, 10, 4)), (34, G(r.lam, 10, 4)), (46, G(r.rough, 10, 4)),
+                        (58, I(r.ncg, 6)), (69, G(r.betrms, 10, 4)), (81, G(r.pharms, 10, 4)),
+                        (93, I(r.npol, 4))]
+            f += [(105, G(r.l1rat, 9, 3)), (117, Fx(r.step, 5, 3))] if robust else [(105, Fx(r.step, 5, 3))]
+        else:  # formats 105 / 106
+            f = head + [(23, G(r.bdpar, 9, 3)), (34, G(r.lam, 10, 4)), (46, G(r.rough, 10, 4)),
+                        (58, I(r.ncg, 6))]
+            f += [(105, G(r.l1rat, 9, 3)), (117, Fx(r.step, 5, 3))] if robust else [(105, Fx(r.step, 5, 3))]
+        out.append(FIO.tab_record(f))
+    return "".join(out)
 
 
 def write_models(inv: "Inversion", ramd: str, ldc: bool = False):
-    """The files src/wout.f90 writes for every accepted model NN: rhoNN.mag
-    (centroid x, y, log10 |rho|; header elanz and the magnitude RMS),
-    rhoNN.pha (phase of rho in mrad; header the phase RMS), rhoNN.modl
-    (|rho|-like 1/Re(sigma) and the phase), rhoNN.sig (sigma) and voltNN.dat
-    (strnr, vnr, |R|, phase in mrad, wdfak).  Numbers in list-directed
-    REAL*4 style; the layout, not the bytes, of the reference's files."""
+    """The files src/wout.f90:61-200 writes for every accepted model NN, byte
+    for byte as gfortran writes them: rhoNN.mag (elanz, TAB, the magnitude
+    RMS; centroid x, y, log10 |rho|), rhoNN.pha (the phase RMS; x, y, phase
+    of rho in mrad), rhoNN.modl (I7; 1/Re(sigma) and the phase in
+    (2(1x,G12.4))), rhoNN.sig (Re, Im of sigma in REAL*8) and voltNN.dat
+    (strnr, vnr, |R|, phase in mrad, wdfak)."""
     os.makedirs(ramd, exist_ok=True)
     g = inv.grid
     cx, cy = R._centroids(g)
+    r4, r8, i4, rec = FIO.real4, FIO.real8, FIO.int4, FIO.record
     for m in inv.models:
         nn = f"{m['it']:02d}"
         rho = 1.0 / m["sigma"]
+        pha = [1e3 * math.atan2(z.imag, z.real) for z in rho]
         with open(os.path.join(ramd, f"rho{nn}.mag"), "w") as fh:
-            fh.write(f"{g.elanz:12d} \t {m['betrms']!r}\n")
-            for i in range(g.elanz):
-                fh.write(f"  {formats.f4(cx[i])}  {formats.f4(cy[i])}  {formats.f4(math.log10(abs(rho[i])))}\n")
+            fh.write(rec([i4(g.elanz), FIO.char("\t"), r8(m["betrms"])]))
+            fh.write("".join(rec([r4(cx[i]), r4(cy[i]), r4(math.log10(abs(rho[i])))]) for i in range(g.elanz)))
         with open(os.path.join(ramd, f"rho{nn}.modl"), "w") as fh:
-            fh.write(f"{g.elanz:7d}\n")
-            for i in range(g.elanz):
-                fh.write(f" {1.0 / m['sigma'][i].real:12.4G} {1e3 * math.atan2(rho[i].imag, rho[i].real):12.4G}\n")
+            fh.write(FIO.fmt_I(g.elanz, 7) + "\n")
+            # dum2 = real(1d3*datan2(...)): the phase passes through REAL*4
+            fh.write("".join(" " + FIO.fmt_G(1.0 / m["sigma"][i].real, 12, 4) + " "
+                             + FIO.fmt_G(float(np.float32(pha[i])), 12, 4) + "\n" for i in range(g.elanz)))
         if not ldc:
             with open(os.path.join(ramd, f"rho{nn}.pha"), "w") as fh:
-                fh.write(f"{g.elanz:12d} \t {m['pharms']!r}\n")
-                for i in range(g.elanz):
-                    fh.write(f"  {formats.f4(cx[i])}  {formats.f4(cy[i])}  {formats.f4(1e3 * math.atan2(rho[i].imag, rho[i].real))}\n")
+                fh.write(rec([i4(g.elanz), FIO.char("\t"), r8(m["pharms"])]))
+                fh.write("".join(rec([r4(cx[i]), r4(cy[i]), r4(pha[i])]) for i in range(g.elanz)))
             with open(os.path.join(ramd, f"rho{nn}.sig"), "w") as fh:
-                fh.write(f"{g.elanz:12d} {m['betrms']!r} {m['pharms']!r}\n")
-                for s in m["sigma"]:
-                    fh.write(f"  {formats.f4(s.real)}  {formats.f4(s.imag)}\n")
+                fh.write(rec([i4(g.elanz), r8(m["betrms"]), r8(m["pharms"])]))
+                fh.write("".join(rec([r8(z.real), r8(z.imag)]) for z in m["sigma"]))
         with open(os.path.join(ramd, f"volt{nn}.dat"), "w") as fh:
-            fh.write(f"{len(m['sigmaa']):12d}\n")
+            fh.write(rec([i4(len(m["sigmaa"]))]))
             for i, sa in enumerate(m["sigmaa"]):
-                cols = [formats.f4(1.0 / math.exp(sa.real))] + ([] if ldc else [formats.f4(-1e3 * sa.imag)])
-                fh.write(f"{int(inv.data.strnr[i]):12d}{int(inv.data.vnr[i]):12d}  " + "  ".join(cols)
-                         + f"{int(m['wdfak'][i]):12d}\n")
+                cols = [r4(1.0 / math.exp(sa.real))] + ([] if ldc else [r4(-1e3 * sa.imag)])
+                fh.write(rec([i4(inv.data.strnr[i]), i4(inv.data.vnr[i])] + cols + [i4(m["wdfak"][i])]))
 
 
 def read_model_mag(path: str):
