@@ -25,19 +25,23 @@ LIST_FILES = [
     ("minimal", "rho01.mag"), ("minimal", "rho01.pha"), ("minimal", "rho02.mag"),
     ("mixed_surf", "rho01.mag"), ("mixed_surf", "rho01.pha"),
     ("minimal", "coverage.mag"), ("minimal", "coverage.mag_fpi"),
+    ("minimal", "ata.diag"), ("minimal", "ata.diag_fpi"), ("minimal", "ata_reg.diag"),
+    ("minimal", "cov1_m.diag"), ("minimal", "cov2_m.diag"), ("minimal", "res_m.diag"),
 ]
 
 
 def _kinds(name, ln, toks):
     if toks[0] == "Max:":
         return ["s", "r8"]
+    if toks[0] == "Max/Min:":
+        return ["s", "r8", "s", "r8"]
     if ln == 0:
-        return ["i", "tab", "r8"] if name.startswith("rho") else ["i"]
+        return ["i", "tab", "r8"] if name.startswith("rho") else ["i"] + ["r8"] * (len(toks) - 1)
     if name.startswith("volt"):
         return ["i", "i", "r4", "r4"] + ["i"] * (len(toks) - 4)
     if name.startswith("rho"):
         return ["r4"] * 3
-    return ["r8"] * 3
+    return ["r8"] * len(toks)
 
 
 @pytest.mark.parametrize("case,name", LIST_FILES)

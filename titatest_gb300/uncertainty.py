@@ -16,13 +16,13 @@ import os
 import numpy as np
 
 from . import formats
+from . import fortran_io as FIO
 from . import regularization as R
 
 f4 = formats.f4
 
 
-def _f8(x) -> str:
-    return repr(float(x))
+r8, i4, ch, rec = FIO.real8, FIO.int4, FIO.char, FIO.record  # list-directed items, as gfortran writes them
 
 
 def weights(inv):
@@ -56,16 +56,14 @@ def coverage(inv, backend, ramd: str):
     os.makedirs(ramd, exist_ok=True)
     cmax = float(np.max(c1))
     with open(os.path.join(ramd, "coverage.mag"), "w") as fh:
-        fh.write(f"{len(c1):12d}  {_f8(cmax)}\n")
-        for j in range(len(c1)):
-            fh.write(f"  {_f8(cx[j])}  {_f8(cy[j])}  {_f8(math.log10(c1[j] / cmax))}\n")
+        fh.write(rec([i4(len(c1)), r8(cmax)]))
+        fh.write("".join(rec([r8(cx[j]), r8(cy[j]), r8(math.log10(c1[j] / cmax))]) for j in range(len(c1))))
     if inv.lfpi:
         fmax = float(np.max(c2))
         with open(os.path.join(ramd, "coverage.mag_fpi"), "w") as fh:
-            fh.write(f"{len(c2):12d}\n")
-            for j in range(len(c2)):
-                fh.write(f"  {_f8(cx[j])}  {_f8(cy[j])}  {_f8(math.log10(c2[j] / fmax))}\n")
-            fh.write(f" Max:  {_f8(fmax)}\n")
+            fh.write(rec([i4(len(c2))]))
+            fh.write("".join(rec([r8(cx[j]), r8(cy[j]), r8(math.log10(c2[j] / fmax))]) for j in range(len(c2))))
+            fh.write(rec([ch("Max:"), r8(fmax)]))
     return c1, c2
 
 
@@ -84,39 +82,36 @@ def buncert(inv, backend, ramd: str, res: bool = True, cov2: bool = True) -> dic
     n = len(out["ata"])
     d = out["ata"]
     with open(os.path.join(ramd, "ata.diag"), "w") as fh:  # bata
-        fh.write(f"{n:12d}  {_f8(d.min())}  {_f8(d.max())}\n")
-        for v in d:
-            fh.write(f"  {_f8(v)}  {_f8(math.log10(v) - math.log10(d.max()))}\n")
+        fh.write(rec([i4(n), r8(d.min()), r8(d.max())]))
+        fh.write("".join(rec([r8(v), r8(math.log10(v) - math.log10(d.max()))]) for v in d))
     if inv.lfpi:  # bata: the FPI diagonal sum_i Re(J_ij)^2 wmatdp_i wdfak_i
         _, _, dfpi = backend.column_sums(np.zeros(len(w_mcm)), np.zeros(len(w_mcm)),
                                          inv.data.wmatdp * np.asarray(inv.wdfak, np.float64))
         out["ata_fpi"] = dfpi
         with open(os.path.join(ramd, "ata.diag_fpi"), "w") as fh:
-            fh.write(f"{n:12d}\n")
-            for v in dfpi:
-                fh.write(f"  {_f8(v)}  {_f8(math.log10(v) - math.log10(dfpi.max()))}\n")
+            fh.write(rec([i4(n)]))
+            fh.write("".join(rec([r8(v), r8(math.log10(v) - math.log10(dfpi.max()))]) for v in dfpi))
+            fh.write(rec([ch("Max/Min:"), r8(dfpi.max()), ch("/"), r8(dfpi.min())]))
     d = out["reg"]
     with open(os.path.join(ramd, "ata_reg.diag"), "w") as fh:  # bata_reg
-        fh.write(f"{n:12d}  {_f8(lam)}\n")
-        for v in d:
-            fh.write(f"  {_f8(v)}  {_f8(math.log10(v))}\n")
-        fh.write(f" Max/Min:  {_f8(d.max())}  /  {_f8(d.min())}\n")
+        fh.write(rec([i4(n), r8(lam)]))
+        fh.write("".join(rec([r8(v), r8(math.log10(v))]) for v in d))
+        fh.write(rec([ch("Max/Min:"), r8(d.max()), ch("/"), r8(d.min())]))
 
     def mcm_file(name, dg):  # bmcm, bmcm2
         with open(os.path.join(ramd, name), "w") as fh:
-            fh.write(f"{n:12d}  {_f8(lam)}\n")
+            fh.write(rec([i4(n), r8(lam)]))
             for j in range(n):
                 r = math.sqrt(dg[j])
-                fh.write(f"  {_f8(r * 1e2)}  {_f8(sigma[j].real * r)}  {_f8(sigma[j].imag * r)}\n")
-            fh.write(f" Max/Min:  {_f8(dg.max())}  /  {_f8(dg.min())}\n")
+                fh.write(rec([r8(r * 1e2), r8(sigma[j].real * r), r8(sigma[j].imag * r)]))
+            fh.write(rec([ch("Max/Min:"), r8(dg.max()), ch("/"), r8(dg.min())]))
 
     mcm_file("cov1_m.diag", out["cov1"])
     if res:
         d = out["res"]
         with open(os.path.join(ramd, "res_m.diag"), "w") as fh:  # bres
-            fh.write(f"{n:12d}  {_f8(lam)}  {_f8(d.min())}  {_f8(d.max())}\n")
-            for v in d:
-                fh.write(f"  {_f8(abs(v))}  {_f8(math.log10(abs(v)) - math.log10(d.max()))}\n")
+            fh.write(rec([i4(n), r8(lam), r8(d.min()), r8(d.max())]))
+            fh.write("".join(rec([r8(abs(v)), r8(math.log10(abs(v)) - math.log10(d.max()))]) for v in d))
         if cov2:
             mcm_file("cov2_m.diag", out["cov2"])
     return out
