@@ -706,7 +706,7 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
     // area parts adom[K][nnz], then fak_area[K][n] (doubles) in the same allocation
     if (!e) e = dalloc(c, &c->d_adom, (size_t)c->K * c->pat.nnz + ((size_t)c->K * hg.n + 1) / 2);
     if (!e) e = dalloc(c, &c->d_kpot, (size_t)c->K * c->eanz * hg.n);
-    if (!e && precision == CRGPU_MIXED) e = dalloc(c, &c->d_kpot32, (size_t)c->K * c->eanz * hg.n);
+    if (!e && precision == CRGPU_MIXED) e = dalloc(c, &c->d_kpot32, 2 * (size_t)c->K * c->eanz * hg.n);  // hi, lo
     if (!e) e = dalloc(c, &c->d_hpot, (size_t)c->eanz * hg.n);
     if (!e) e = dalloc(c, &c->d_volt, (size_t)std::max(c->nanz, 1));
     if (!e) e = dalloc(c, &c->d_sigmaa, (size_t)std::max(c->nanz, 1));

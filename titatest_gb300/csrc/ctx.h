@@ -25,7 +25,7 @@ struct crgpu_ctx {
     // device state
     double2 *d_sigma = nullptr, *d_adom = nullptr, *d_kpot = nullptr, *d_hpot = nullptr;
     double2 *d_volt = nullptr, *d_sigmaa = nullptr, *d_sens = nullptr;
-    float2 *d_kpot32 = nullptr;  // complex64 copy of kpot (mixed precision: the Jacobian's input)
+    float2 *d_kpot32 = nullptr;  // kpot as complex64 hi and lo planes (mixed precision: the Jacobian's input)
     double *d_kfak = nullptr;
     double2 *d_rwd = nullptr;     // [2][n] valued Dirichlet nodes: b values, moved-column values
     double2 *d_sigma0 = nullptr;  // reference conductivity (singularity removal)

@@ -111,8 +111,11 @@ __global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P,
                                                          const double2 *__restrict__ volt,
                                                          double2 *__restrict__ sens, int e_first) {
     using C = typename SensT<R>::C;
+    constexpr bool kTwoPlanes = sizeof(R) == 4;  // complex64: hi and lo planes of kpot
     extern __shared__ __align__(16) unsigned char kp_raw[];
     C *kp_sh = (C *)kp_raw;  // [4][eanz]
+    C *kl_sh = kp_sh + 4 * P.eanz;  // [4][eanz] lo plane (complex64 only)
+    const size_t plane = (size_t)P.K * P.eanz * P.n;
     __shared__ R kel[10];
     const int e = e_first + blockIdx.x;
     const int nk = P.etype[e] == 3 ? 3 : 4;
@@ -129,7 +132,9 @@ __global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P,
             __syncthreads();
             for (int t = threadIdx.x; t < nk * eanz; t += kSensThreads) {
                 int q = t / eanz, l = t % eanz;
-                kp_sh[t] = kpot[((size_t)k * eanz + l) * P.n + nodes[q]];
+                const size_t at = ((size_t)k * eanz + l) * P.n + nodes[q];
+                kp_sh[t] = kpot[at];
+                if (kTwoPlanes) kl_sh[t] = kpot[at + plane];
             }
             if (threadIdx.x < 10) kel[threadIdx.x] = (R)P.elbg[((size_t)k * P.elanz + e) * 10 + threadIdx.x];
             __syncthreads();
@@ -148,6 +153,13 @@ __global__ __launch_bounds__(kSensThreads) void k_bsens(DevProblem P,
                     C s4 = ee.w >= 0 ? kp_sh[q * eanz + ee.w] : SensT<R>::mk(0, 0);
                     u[q] = SensT<R>::mk(s2.x - s1.x, s2.y - s1.y);
                     v[q] = SensT<R>::mk(s4.x - s3.x, s4.y - s3.y);
+                    if (kTwoPlanes) {  // the dipole differences to ~complex64 accuracy of the difference
+                        const C z = SensT<R>::mk(0, 0);
+                        C t1 = ee.x >= 0 ? kl_sh[q * eanz + ee.x] : z, t2 = ee.y >= 0 ? kl_sh[q * eanz + ee.y] : z;
+                        C t3 = ee.z >= 0 ? kl_sh[q * eanz + ee.z] : z, t4 = ee.w >= 0 ? kl_sh[q * eanz + ee.w] : z;
+                        u[q] = SensT<R>::mk(u[q].x + (t2.x - t1.x), u[q].y + (t2.y - t1.y));
+                        v[q] = SensT<R>::mk(v[q].x + (t4.x - t3.x), v[q].y + (t4.y - t3.y));
+                    }
                     if (q >= nk) { u[q] = SensT<R>::mk(0, 0); v[q] = SensT<R>::mk(0, 0); }
                 }
                 C hs = SensT<R>::mk(0, 0);
@@ -200,7 +212,7 @@ void launch_bsens(const DevProblem &P, const double2 *kpot, const float2 *kpot32
         return;
     }
     if (single) {
-        size_t smem = sizeof(float2) * 4 * P.eanz;
+        size_t smem = sizeof(float2) * 8 * P.eanz;  // hi and lo planes
         if (mode == 0) k_bsens<0, float><<<e_count, kSensThreads, smem, st>>>(P, kpot32, sigma, volt, sens, e_first);
         else k_bsens<1, float><<<e_count, kSensThreads, smem, st>>>(P, kpot32, sigma, volt, sens, e_first);
     } else {

@@ -661,7 +661,8 @@ void launch_copy_solution(const DevProblem &P, const DevBatch &B, int nrhs, cuda
     k_copy_solution<<<(unsigned)((tot + nt - 1) / nt), nt, 0, st>>>(P, B, nrhs);
 }
 
-// kpot(j, l, k) = pot(j) * fak(j) with pot = -x (src/fem.f90:388-389)
+// kpot(j, l, k) = pot(j) * fak(j) with pot = -x (src/fem.f90:388-389); for the
+// mixed Jacobian also kpot as two complex64 planes hi + lo
 __global__ void k_kpot(DevProblem P, DevBatch B, int nrhs, double2 *kpot, float2 *kpot32) {
     size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t tot = (size_t)B.nsys * nrhs * P.n;
@@ -673,8 +674,13 @@ __global__ void k_kpot(DevProblem P, DevBatch B, int nrhs, double2 *kpot, float2
     double2 x = B.x[gid];
     double2 v = cz(-x.x * f, -x.y * f);
     if (P.lsr) v = cadd(v, B.pota[(size_t)s * P.n + i]);  // src/fem.f90:390-391
-    kpot[((size_t)k * P.eanz + l) * P.n + i] = v;
-    if (kpot32) kpot32[((size_t)k * P.eanz + l) * P.n + i] = to_f(v);
+    const size_t at = ((size_t)k * P.eanz + l) * P.n + i;
+    kpot[at] = v;
+    if (kpot32) {  // complex64 hi plane, then the lo plane (v - hi)
+        const float2 hi = to_f(v);
+        kpot32[at] = hi;
+        kpot32[at + (size_t)P.K * P.eanz * P.n] = cf((float)(v.x - (double)hi.x), (float)(v.y - (double)hi.y));
+    }
 }
 
 void launch_kpot(const DevProblem &P, const DevBatch &B, int nrhs, double2 *kpot, float2 *kpot32,
