@@ -12,9 +12,10 @@
 // Each entry therefore sees its updates in increasing j, the same summation
 // order as the reference's left-looking dot products.
 //
-//  * k_factor_plain (complex128): the window is updated in place in the band
-//    buffer (global memory; the active ~(mb+1)^2 * 16 B stays in L2).  On
-//    GB300 the FP64 pipe, not memory, bounds this kernel.
+//  * complex128: k_factor_plain_reg (factor_plain.cu) keeps the window in
+//    registers for mb < 127; wider bands use k_factor_plain, which updates the
+//    window in place in the band buffer (global memory; the active
+//    ~(mb+1)^2 * 16 B stays in L2).
 //  * complex64, mb <= 124: k_factor_tc (tc_factor.cu) keeps the window in
 //    tensor memory and applies the trailing updates with tcgen05.mma.
 //  * complex64, mb > 175: k_factor_mixed_smem<WP> (factor_smem.cu), the same
@@ -108,6 +109,7 @@ __global__ __launch_bounds__(kPlainThreads) void k_factor_plain(DevProblem P, De
 }
 
 void launch_factor_plain(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st) {
+    if (launch_factor_plain_reg(P, B, fuse, nsm, st)) return;  // mb < 127: window in registers
     int grid = B.nsys < nsm * 2 ? B.nsys : nsm * 2;
     size_t smem = sizeof(double2) * (P.mb + 1);
     k_factor_plain<<<grid, kPlainThreads, smem, st>>>(P, B, fuse);

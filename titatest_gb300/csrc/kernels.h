@@ -28,6 +28,9 @@ void launch_pota_rhs(const DevProblem &P, const DevBatch &B, const double2 *sigm
 // factorisation (src/chol.f90) with fused forward substitution when fuse != 0
 void launch_factor_plain(const DevProblem &P, const DevBatch &B, int fuse, int nsm,
                          cudaStream_t st);
+// complex128 factor with the window in registers (factor_plain.cu); false
+// when the band is too wide for it
+bool launch_factor_plain_reg(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st);
 int launch_factor_mixed(const DevProblem &P, const DevBatch &B, int fuse, int nsm, bool exclusive,
                         cudaStream_t st);
 int mixed_window_supported(int W);
