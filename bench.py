@@ -106,6 +106,24 @@ def tensor_peak_tflops():
         return 1700.0, "fallback 1.7 PFLOP/s sustained bf16 (of fallback)"
 
 
+def fp64_dgemm_tflops(stream) -> float:
+    """The FP64 rate of this GPU as cuBLAS DGEMM reaches it (4096^3, best of
+    3, CUDA events): the denominator of the complex128 factor's roofline."""
+    import torch
+    a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = float("inf")
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        torch.matmul(a, b)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2.0 * 4096 ** 3 / (best * 1e-3) / 1e12
+
+
 def read_profile_traffic(name: str):
     """DRAM bytes per launch recorded from an ncu capture (profiles/<name>)."""
     p = os.path.join(ROOT, "profiles", name)
@@ -361,6 +379,7 @@ def run_gpu(args):
     n, mb = g.sanz, g.mb
     nsys = K * sv.eanz
     flops_factor = nsys * 4.0 * n * mb * mb  # 8 flops per complex multiply-add, n*mb^2/2 of them
+    fp64_peak = fp64_dgemm_tflops(stream)
     fac_avg_ms = statistics.mean(fac_ms)
     achieved = flops_factor / (fac_avg_ms * 1e-3) / 1e12
     peak, peak_source = tensor_peak_tflops()
@@ -382,7 +401,12 @@ def run_gpu(args):
                 "d2h_link_gbs": link_gbs},
         "plain": {"value": 1e3 / plain_ms, "unit": "units/s", "ms_per_step": plain_ms,
                   "ms_factor": plain_stats["ms_factor"], "ms_solve": plain_stats["ms_solve"],
-                  "ms_sens": plain_stats["ms_sens"]},
+                  "ms_sens": plain_stats["ms_sens"],
+                  "roofline": {"kernel": "k_factor_plain_reg", "bound": "fp64",
+                               "achieved": flops_factor / (plain_stats["ms_factor"] * 1e-3) / 1e12,
+                               "peak": fp64_peak, "unit": "TFLOP/s",
+                               "frac": flops_factor / (plain_stats["ms_factor"] * 1e-3) / 1e12 / fp64_peak,
+                               "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (best of 3, CUDA events)"}},
         "speedup_mixed_vs_plain": plain_ms / ms_per_step,
         "mixed_vs_plain_rel_err": {"volt": err_v, "jacobian": err_j},
         "accuracy_target": {"volt": 1e-6, "jacobian": 1e-5, "met": bool(err_v < 1e-6 and err_j < 1e-5)},

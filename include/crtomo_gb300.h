@@ -83,6 +83,24 @@ enum {
 int crgpu_create(const crgpu_grid *grid, const crgpu_survey *survey, int32_t precision,
                  crgpu_ctx **ctx);
 
+/* crgpu_create with the choice of the complex64 factor's node order (no
+ * counterpart in the reference, which factors in the cutmckee band):
+ * band_order 0 keeps the grid's band; 1 (crgpu_create's default) lets a
+ * CRGPU_MIXED context whose band is too wide for the tensor-core window
+ * (mb > 124) number its nodes by their coordinate along the mesh's longer
+ * extent when that band fits the window.  The refinement's FP64 residuals
+ * use the same matrix, so only the preconditioner changes; potentials,
+ * voltages and sensitivities come back in the grid's order and numbering.
+ * Such a context returns 1002 from crgpu_factor_system; its device buffers
+ * (crgpu_device_buffers) are in the order crgpu_node_order reports. */
+int crgpu_create2(const crgpu_grid *grid, const crgpu_survey *survey, int32_t precision, int32_t band_order,
+                  crgpu_ctx **ctx);
+
+/* No counterpart in the reference.  grid_node[j] (1-based, sanz entries):
+ * the grid node in position j of the context's device arrays (j + 1 unless
+ * the context factors in the geometric order of crgpu_create2). */
+int crgpu_node_order(const crgpu_ctx *ctx, int32_t *grid_node);
+
 /* Frees the context and its device memory. */
 int crgpu_destroy(crgpu_ctx *ctx);
 

@@ -220,7 +220,7 @@ def test_wide_band_mixed_factor_shared_memory_window(gpu_lib):
     P = O.Problem(g, sv)
     kwn, kwnwi = P.rwaven()
     a_ref, fak_ref = P.factor(sig, kwn, 1, 1)
-    with CRMod(g, sv, kwn, kwnwi, precision=MIXED) as m:
+    with CRMod(g, sv, kwn, kwnwi, precision=MIXED, band_order=0) as m:  # the grid's own band
         a, fak = m.factor_system(sig, 1, 1)
         m.set_refinement(10, 1e-10)
         vm = m.forward(sig)["volt"]
@@ -265,3 +265,29 @@ def test_run_tomodir_writes_crmod_outputs(gpu_lib, tmp_path):
     J = out["sens"]
     body = np.loadtxt(tmp_path / "mod" / "sens" / "sens12.dat", skiprows=1)
     assert np.allclose(body[:, 2] + 1j * body[:, 3], J[11], rtol=1e-6, atol=1e-7 * np.abs(J[11]).max())
+
+
+def test_wide_band_mixed_in_geometric_order(gpu_lib):
+    """The same mb = 192 strip with the default band order: the complex64
+    factor runs on the tensor cores in the nodes' geometric order (band 8);
+    potentials, voltages and sensitivities come back in the grid's order and
+    equal the complex128 path's."""
+    from titatest_gb300 import MIXED, PLAIN, CRMod
+    from titatest_gb300._lib import CRGPUError
+    g, sv, sig = _wide_band_case()
+    kwn, kwnwi = O.Problem(g, sv).rwaven()
+    with CRMod(g, sv, kwn, kwnwi, precision=PLAIN) as m:
+        op = m.forward(sig, kpot=True, hpot=True)
+        Jp = m.bsens()
+    with CRMod(g, sv, kwn, kwnwi, precision=MIXED) as m:
+        m.set_refinement(10, 1e-10)
+        order = m.node_order()
+        assert sorted(order.tolist()) == list(range(1, g.sanz + 1)) and np.any(order != np.arange(1, g.sanz + 1))
+        om = m.forward(sig, kpot=True, hpot=True)
+        Jm = m.bsens()
+        with pytest.raises(CRGPUError):
+            m.factor_system(sig, 1, 1)
+    assert relerr(om["kpot"], op["kpot"]) < MIXED_VOLT_TOL
+    assert relerr(om["hpot"], op["hpot"]) < MIXED_VOLT_TOL
+    assert relerr(om["volt"], op["volt"]) < MIXED_VOLT_TOL
+    assert relerr(Jm, Jp) < MIXED_SENS_TOL

@@ -68,11 +68,7 @@ def build(verbose: bool = False, ptxas_v: bool = False) -> str:
                 if verbose and msg:
                     print(f"== {os.path.basename(futs[f])}\n{msg}", file=sys.stderr)
     if jobs or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        # cuBLAS / cuSOLVER for the dense steps of the model uncertainty (mcm.cu),
-        # found at run time beside the toolkit's other libraries
-        libdir = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "lib64")
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lcublas", "-lcusolver",
-                                                                 "-Xlinker", "-rpath=" + libdir]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

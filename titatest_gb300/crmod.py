@@ -67,11 +67,14 @@ class CRMod:
 
     precision: PLAIN (complex128, the reference arithmetic) or MIXED (complex64
     factorisation with FP64 iterative refinement).
+    band_order: 1 (default) lets a MIXED context whose band is too wide for
+    the tensor-core window factor in the geometric node order when that band
+    fits (crgpu_create2); 0 keeps the grid's band.
     """
 
     def __init__(self, grid: formats.Grid, survey: formats.Survey, kwn=None, kwnwi=None,
                  swrtr: int = 1, lsink: bool = False, nsink: int = 0, lsytop: bool = False,
-                 precision: int = PLAIN, lsr: bool = False):
+                 precision: int = PLAIN, lsr: bool = False, band_order: int = 1):
         self.grid = grid
         self.survey = survey
         if kwn is None:
@@ -95,7 +98,8 @@ class CRMod:
                            ptr(self.kwn, f64p), ptr(self.kwnwi, f64p), int(swrtr), int(lsr),
                            int(lsink), int(nsink), int(lsytop))
         h = C.c_void_p()
-        code = lib().crgpu_create(C.byref(self._cg), C.byref(self._cs), int(precision), C.byref(h))
+        code = lib().crgpu_create2(C.byref(self._cg), C.byref(self._cs), int(precision), int(band_order),
+                                   C.byref(h))
         self._h = h
         if code:
             msg = lib().crgpu_last_error(h).decode() if h.value else ""
@@ -259,6 +263,13 @@ class CRMod:
 
     def sens_device(self, mode: int, sens_ptr: int):
         _check(self._h, lib().crgpu_sens_device(self._h, int(mode), C.c_void_p(sens_ptr)))
+
+    def node_order(self) -> np.ndarray:
+        """crgpu_node_order: the grid node (1-based) in each position of the
+        context's device arrays."""
+        out = np.zeros(self.grid.sanz, np.int32)
+        _check(self._h, lib().crgpu_node_order(self._h, ptr(out, i32p)))
+        return out
 
     def device_buffers(self):
         kp = C.c_void_p()

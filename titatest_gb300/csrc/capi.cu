@@ -26,6 +26,7 @@ struct RefineCount {
     double z;  // largest relative correction of the step
 };
 constexpr int kRefineCap = 64;  // refinement steps at most (crgpu_set_refinement)
+constexpr int kRefineSlots = 8;  // counter arrays: one per factor round of a pipelined forward
 
 int fail(crgpu_ctx *c, int code, const std::string &msg) {
     if (c) c->last_error = msg;
@@ -132,8 +133,8 @@ int ensure_batch(crgpu_ctx *c, int want) {
     e = e ? e : dalloc(c, &B.status, (size_t)want);
     e = e ? e : dalloc(c, &B.active, (size_t)want * nr);
     if (!e && !c->d_refine) {
-        char *cnt = nullptr;  // [2][kRefineCap] steps of {int count, pad, double zmax}
-        e = dalloc(c, &cnt, 2 * kRefineCap * sizeof(RefineCount));
+        char *cnt = nullptr;  // [kRefineSlots][kRefineCap] steps of {int count, pad, double zmax}
+        e = dalloc(c, &cnt, kRefineSlots * kRefineCap * sizeof(RefineCount));
         c->d_refine = cnt;
     }
     e = e ? e : dalloc(c, &c->d_ks, (size_t)want);
@@ -276,7 +277,7 @@ int solve_batch(crgpu_ctx *c, int ns, bool fused) { return solve_view(c, batch_v
 // streams must be idle): steps that ran, and the largest relative correction
 // of the last one
 int collect_refine_stats(crgpu_ctx *c) {
-    for (int slot = 0; slot < 2; slot++) {
+    for (int slot = 0; slot < kRefineSlots; slot++) {
         const int used = c->refine_used[slot];
         if (!used) continue;
         std::vector<RefineCount> h(used);
@@ -392,19 +393,32 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
             e = solve_view(c, B, fuse != 0, c->st, 0);
             if (e) return e;
         } else {
-            // full rounds on st; the last, partial round starts on st_hi once they are
-            // done, beside the full rounds' solves, and is solved there
-            const DevBatch Bf = sub_view(c, B, 0, ns - tail), Bt = sub_view(c, B, ns - tail, tail);
-            e = run_factor_view(c, Bf, fuse, c->st);
-            if (e) return e;
-            cudaEventRecord(f1, c->st);
-            CUCHECK(c, cudaStreamWaitEvent(c->st_hi, f1, 0));
+            // full rounds of 2 blocks per SM, one launch each on st; each round's solves
+            // run on st_solve beside the next round's factor (a sweep block fits beside
+            // the two factor blocks of an SM).  The last, partial round starts on st_hi
+            // once the full rounds are factored and is solved there.
+            const int round = 2 * c->nsm, nfull = (ns - tail) / round;
+            for (int r = 0; r < nfull; r++) {
+                const DevBatch Br = sub_view(c, B, r * round, round);
+                e = run_factor_view(c, Br, fuse, c->st);
+                if (e) return e;
+                cudaEvent_t er = c->ev_round[std::min(r, 7)];
+                CUCHECK(c, cudaEventRecord(er, c->st));
+                CUCHECK(c, cudaStreamWaitEvent(c->st_solve, er, 0));
+                e = solve_view(c, Br, fuse != 0, c->st_solve, std::min(r, kRefineSlots - 2));
+                if (e) return e;
+            }
+            if (!cap) cudaEventRecord(f1, c->st);
+            const DevBatch Bt = sub_view(c, B, ns - tail, tail);
+            CUCHECK(c, cudaEventRecord(c->ev_join2, c->st));
+            CUCHECK(c, cudaStreamWaitEvent(c->st_hi, c->ev_join2, 0));
             e = run_factor_view(c, Bt, fuse, c->st_hi, true);  // SMs of its own
-            if (!e) e = solve_view(c, Bt, fuse != 0, c->st_hi, 1);
-            if (!e) e = solve_view(c, Bf, fuse != 0, c->st, 0);
+            if (!e) e = solve_view(c, Bt, fuse != 0, c->st_hi, kRefineSlots - 1);
             if (e) return e;
             CUCHECK(c, cudaEventRecord(c->ev_join, c->st_hi));
             CUCHECK(c, cudaStreamWaitEvent(c->st, c->ev_join, 0));
+            CUCHECK(c, cudaEventRecord(c->ev_join2, c->st_solve));
+            CUCHECK(c, cudaStreamWaitEvent(c->st, c->ev_join2, 0));
         }
         launch_kpot(P, B, nr, c->d_kpot, c->d_kpot32, c->st);
         c->stats.kernel_launches += 1;
@@ -558,6 +572,11 @@ float time_on(crgpu_ctx *c, F &&fn) {
 extern "C" {
 
 int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precision, crgpu_ctx **out) {
+    return crgpu_create2(grid, sv, precision, 1, out);
+}
+
+int crgpu_create2(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precision, int32_t band_order,
+                  crgpu_ctx **out) {
     if (!out) return ERR_ARG;
     *out = nullptr;
     crgpu_ctx *c = new crgpu_ctx();
@@ -569,6 +588,22 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
     if (!e && precision != CRGPU_PLAIN && precision != CRGPU_MIXED) {
         e = ERR_ARG;
         c->last_error = "precision";
+    }
+    if (!e && (band_order < 0 || band_order > 1)) {
+        e = ERR_ARG;
+        c->last_error = "band_order";
+    }
+    // complex64 factor of a band too wide for the tensor-core window: factor
+    // in the geometric node order when its band fits (the results are mapped
+    // back to the grid's node order at the boundary)
+    if (!e && band_order == 1 && precision == CRGPU_MIXED && c->hg.mb + 4 > 128) {
+        const int mb2 = host_geometric_order(c->hg, c->old_of_new, c->new_of_old);
+        if (mb2 + 4 <= 128 && mb2 < c->hg.mb) {
+            host_permute_grid(c->hg, c->old_of_new, c->new_of_old, mb2);
+        } else {
+            c->old_of_new.clear();
+            c->new_of_old.clear();
+        }
     }
     if (!e) e = build_pattern(c->hg, c->pat, c->last_error);
     if (e) {
@@ -582,6 +617,7 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
     c->swrtr = sv->swrtr;
     c->lsink = sv->lsink;
     c->nsink = sv->lsink ? sv->nsink - 1 : -1;
+    if (c->nsink >= 0 && !c->new_of_old.empty()) c->nsink = c->new_of_old[c->nsink];
     c->lsytop = sv->lsytop;
     // src/fem.f90:311 (no mixed boundaries: no singularity removal) and 2D
     c->lsr = (sv->lsr && c->hg.lbeta && sv->swrtr != 0) ? 1 : 0;
@@ -592,7 +628,10 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
         cudaDeviceGetStreamPriorityRange(&lo, &hi);
         ce = cudaStreamCreateWithPriority(&c->st_hi, cudaStreamNonBlocking, hi);
     }
+    if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&c->st_solve, cudaStreamNonBlocking);
     if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&c->ev_join2, cudaEventDisableTiming);
+    for (int q = 0; q < 8 && ce == cudaSuccess; q++) ce = cudaEventCreateWithFlags(&c->ev_round[q], cudaEventDisableTiming);
     if (ce != cudaSuccess) {
         c->last_error = cudaGetErrorString(ce);
         *out = c;
@@ -627,7 +666,7 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precisi
             *out = c;
             return 29;
         }
-        enr0[i] = sv->enr[i] - 1;
+        enr0[i] = c->new_of_old.empty() ? sv->enr[i] - 1 : c->new_of_old[sv->enr[i] - 1];
     }
     for (int i = 0; i < c->nanz; i++) {
         int a1 = sv->strnr[i] % 10000, a2 = (sv->strnr[i] - a1) / 10000;
@@ -753,6 +792,10 @@ int crgpu_destroy(crgpu_ctx *c) {
     if (c->own_st) cudaStreamDestroy(c->own_st);
     if (c->copy_st) cudaStreamDestroy(c->copy_st);
     if (c->st_hi) cudaStreamDestroy(c->st_hi);
+    if (c->st_solve) cudaStreamDestroy(c->st_solve);
+    if (c->ev_join2) cudaEventDestroy(c->ev_join2);
+    for (auto &ev_ : c->ev_round)
+        if (ev_) cudaEventDestroy(ev_);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     delete c;
     return 0;
@@ -783,7 +826,7 @@ int crgpu_set_boundary_values(crgpu_ctx *c, int32_t rwdanz, const int32_t *rwdnr
     std::vector<uint8_t> dir(c->hg.dirichlet);
     std::vector<double2> vals((size_t)2 * n, make_double2(0.0, 0.0));
     for (int ir = 0; ir < rwdanz; ir++) {
-        const int k = rwdnr[ir] - 1;
+        const int k = c->new_of_old.empty() ? rwdnr[ir] - 1 : c->new_of_old[rwdnr[ir] - 1];
         const double2 v = make_double2(rwd[2 * ir], rwd[2 * ir + 1]);
         vals[k] = v;
         if (dir[k] == 0) vals[(size_t)n + k] = v;
@@ -857,6 +900,19 @@ int crgpu_forward(crgpu_ctx *c, const double *sigma, double *kpot, double *hpot,
                                    cudaMemcpyDeviceToHost, c->st));
     if (hpot)
         CUCHECK(c, cudaMemcpyAsync(hpot, c->d_hpot, (size_t)c->eanz * nn * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+    if (!c->old_of_new.empty() && (kpot || hpot)) {  // back to the grid's node order
+        CUCHECK(c, cudaStreamSynchronize(c->st));
+        std::vector<double2> tmp(nn);
+        auto unpermute = [&](double *arr, size_t blocks) {
+            double2 *a = (double2 *)arr;
+            for (size_t b = 0; b < blocks; b++) {
+                std::copy(a + b * nn, a + (b + 1) * nn, tmp.begin());
+                for (size_t j = 0; j < nn; j++) a[b * nn + c->old_of_new[j]] = tmp[j];
+            }
+        };
+        if (kpot) unpermute(kpot, (size_t)c->K * c->eanz);
+        if (hpot) unpermute(hpot, (size_t)c->eanz);
+    }
     if (volt)
         CUCHECK(c, cudaMemcpyAsync(volt, c->d_volt, (size_t)c->nanz * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
     if (sigmaa)
@@ -886,8 +942,7 @@ int crgpu_forward_sens_graph(crgpu_ctx *c, const void *sigma_device, void *volt_
         int e = check_device_errors(c, c->Bmax.status, (int)c->sys_k.size());
         c->stats.refine_iterations = 0;
         c->stats.refine_last_correction = 0.0;
-        c->refine_used[0] = c->graph_refine_used[0];
-        c->refine_used[1] = c->graph_refine_used[1];
+        for (int q = 0; q < kRefineSlots; q++) c->refine_used[q] = c->graph_refine_used[q];
         if (!e) e = collect_refine_stats(c);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, a, b);
@@ -918,9 +973,10 @@ int crgpu_forward_sens_graph(crgpu_ctx *c, const void *sigma_device, void *volt_
     }
     c->capturing = false;
     c->stats = keep;
-    c->graph_refine_used[0] = c->refine_used[0];
-    c->graph_refine_used[1] = c->refine_used[1];
-    c->refine_used[0] = c->refine_used[1] = 0;
+    for (int q = 0; q < kRefineSlots; q++) {
+        c->graph_refine_used[q] = c->refine_used[q];
+        c->refine_used[q] = 0;
+    }
     if (!e && ce == cudaSuccess && graph) ce = cudaGraphInstantiate(&c->graph, graph, 0);
     if (graph) cudaGraphDestroy(graph);
     if (e || ce != cudaSuccess) {  // no graph: later calls record again; this call's results stand
@@ -1065,6 +1121,12 @@ int crgpu_adjoint(crgpu_ctx *c, const double *g, double *grad) {
     return 0;
 }
 
+int crgpu_node_order(const crgpu_ctx *c, int32_t *grid_node) {
+    if (!c || !grid_node) return ERR_ARG;
+    for (int j = 0; j < c->hg.n; j++) grid_node[j] = c->old_of_new.empty() ? j + 1 : c->old_of_new[j] + 1;
+    return 0;
+}
+
 int crgpu_device_buffers(crgpu_ctx *c, void **kpot_device, void **hpot_device) {
     if (!c) return ERR_ARG;
     if (kpot_device) *kpot_device = c->d_kpot;
@@ -1074,6 +1136,9 @@ int crgpu_device_buffers(crgpu_ctx *c, void **kpot_device, void **hpot_device) {
 
 int crgpu_factor_system(crgpu_ctx *c, const double *sigma, int32_t k, int32_t l, double *a, double *fak) {
     if (!c || !sigma || k < 1 || k > c->K || l < 1 || l > c->eanz) return ERR_ARG;
+    if (!c->old_of_new.empty())
+        return fail(c, ERR_UNSUPPORTED, "this context factors in the geometric node order (create it with band order 0 "
+                                        "to read the grid's band)");
     c->factors_resident = false;  // system 0's factor is overwritten below
     const int n = c->hg.n, W = c->hg.mb + 1;
     CUCHECK(c, cudaMemcpyAsync(c->d_sigma, sigma, c->hg.elanz * sizeof(double2), cudaMemcpyHostToDevice, c->st));

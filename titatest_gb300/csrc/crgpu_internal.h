@@ -58,5 +58,8 @@ int host_cutmck(int32_t sanz, int32_t typanz, const int32_t *typ, const int32_t 
                 const int32_t *selanz, int32_t *nrel, int32_t ld_nrel, int32_t *snr, int32_t eanz,
                 int32_t *enr, int32_t *mb);
 double host_sytop(const crgpu_grid *g);
+int host_geometric_order(const HostGrid &hg, std::vector<int32_t> &old_of_new, std::vector<int32_t> &new_of_old);
+void host_permute_grid(HostGrid &hg, const std::vector<int32_t> &old_of_new, const std::vector<int32_t> &new_of_old,
+                       int mb);
 
 }  // namespace crgpu

@@ -537,4 +537,70 @@ int host_cutmck(int32_t sanz, int32_t typanz, const int32_t *typ, const int32_t 
     return 0;
 }
 
+// A second node order for the complex64 factor of wide bands: the nodes
+// sorted by the coordinate along the mesh's longer extent, then by the other
+// one.  On structured meshes this numbers the nodes line by line across the
+// short side, a band of about one line instead of the two lines of a
+// Cuthill-McKee level structure grown from a single node.  old_of_new[j] is
+// the grid's node in position j; returns the band width of that order.
+int host_geometric_order(const HostGrid &hg, std::vector<int32_t> &old_of_new, std::vector<int32_t> &new_of_old) {
+    const int n = hg.n;
+    double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
+    for (int i = 0; i < n; i++) {
+        x0 = std::min(x0, hg.x[i]);
+        x1 = std::max(x1, hg.x[i]);
+        y0 = std::min(y0, hg.y[i]);
+        y1 = std::max(y1, hg.y[i]);
+    }
+    const bool along_x = (x1 - x0) >= (y1 - y0);
+    old_of_new.resize(n);
+    for (int i = 0; i < n; i++) old_of_new[i] = i;
+    std::stable_sort(old_of_new.begin(), old_of_new.end(), [&](int a, int b) {
+        const double pa = along_x ? hg.x[a] : hg.y[a], pb = along_x ? hg.x[b] : hg.y[b];
+        if (pa != pb) return pa < pb;
+        const double qa = along_x ? hg.y[a] : hg.x[a], qb = along_x ? hg.y[b] : hg.x[b];
+        return qa < qb;
+    });
+    new_of_old.assign(n, 0);
+    for (int j = 0; j < n; j++) new_of_old[old_of_new[j]] = j;
+    int mb = 0;
+    for (int e = 0; e < hg.elanz; e++) {
+        int lo = n, hi = -1;
+        for (int q = 0; q < 4; q++) {
+            const int v = hg.enodes[(size_t)e * 4 + q];
+            if (v < 0) continue;
+            lo = std::min(lo, new_of_old[v]);
+            hi = std::max(hi, new_of_old[v]);
+        }
+        mb = std::max(mb, hi - lo);
+    }
+    for (int b = 0; b < hg.relanz; b++) {
+        const int u = hg.bnodes[(size_t)b * 2], v = hg.bnodes[(size_t)b * 2 + 1];
+        if (u >= 0 && v >= 0) mb = std::max(mb, std::abs(new_of_old[u] - new_of_old[v]));
+    }
+    return mb;
+}
+
+// hg renumbered by new_of_old (coordinates, element and boundary nodes,
+// Dirichlet flags), with band width mb
+void host_permute_grid(HostGrid &hg, const std::vector<int32_t> &old_of_new, const std::vector<int32_t> &new_of_old,
+                       int mb) {
+    const int n = hg.n;
+    std::vector<double> x(n), y(n);
+    std::vector<uint8_t> dir(n);
+    for (int j = 0; j < n; j++) {
+        x[j] = hg.x[old_of_new[j]];
+        y[j] = hg.y[old_of_new[j]];
+        dir[j] = hg.dirichlet[old_of_new[j]];
+    }
+    hg.x.swap(x);
+    hg.y.swap(y);
+    hg.dirichlet.swap(dir);
+    for (auto &v : hg.enodes)
+        if (v >= 0) v = new_of_old[v];
+    for (auto &v : hg.bnodes)
+        if (v >= 0) v = new_of_old[v];
+    hg.mb = mb;
+}
+
 }  // namespace crgpu

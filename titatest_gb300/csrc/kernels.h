@@ -100,6 +100,15 @@ struct McmArgs {
     int want_res, want_cov2;
     double *diag_ata, *diag_reg, *diag_cov1, *diag_res, *diag_cov2;
 };
+// dense FP64 kernels (dense.cu), column-major: C (lower) = S^T S for S k x n;
+// the Cholesky factor of A (n x n, lower, in place; info_dev: first
+// non-positive pivot, 1-based, 0 if none); C (lower) = (L L^T)^-1 with work Y
+// (n x n); d_j = sum_l (S C)_lj^2 for S m x n, with work (ceil(m/64) x n)
+void dense_syrk_t(int n, int k, const double *S, int lds, double *C, cudaStream_t st);
+void dense_potrf(int n, double *A, int *info_dev, cudaStream_t st);
+void dense_potri(int n, const double *L, double *Y, double *C, cudaStream_t st);
+void dense_col_sq_of_product(int m, int n, const double *S, int lds, const double *C, double *work, double *d,
+                             cudaStream_t st);
 int run_mcm(const McmArgs &a, cudaStream_t st, std::string &msg);
 void launch_column_sums(int nanz, int manz, const double2 *sens, const double *wa, const double *wb,
                         const double *wc, double *c1, double *c2, double *c3, cudaStream_t st);

@@ -2,18 +2,15 @@
 // bata_reg, bmcm, bres, bmcm2) and the coverage sums (src/bbsens.f90) on the
 // sensitivities held on the device.
 //
-//   ata     = Re(J^H W J)                       (bata: DSYRK on [sqrt(w) Re J; sqrt(w) Im J])
+//   ata     = Re(J^H W J) = S^T S               (bata; S = [sqrt(w) Re J; sqrt(w) Im J])
 //   ata_reg = ata + lam R                       (bata_reg)
-//   cov     = ata_reg^-1                        (bmcm: Cholesky factor and inverse, cuSOLVER)
+//   cov     = ata_reg^-1 = L^-T L^-1            (bmcm: blocked Cholesky, triangular inverse, Y^T Y)
 //   res     = cov ata          -> diag          (bres: row-column dots, O(manz^2))
-//   cov2    = cov ata cov      -> diag          (bmcm2: one DGEMM, then row-column dots)
+//   cov2    = cov ata cov      -> diag          (bmcm2: = (S cov)^T (S cov), column sums of squares)
 //
-// The dense steps are plain library calls (cuBLAS DSYRK / DGEMM, cuSOLVER
-// DPOTRF / DPOTRI) on real symmetric matrices; the kernels here form the
-// weighted operand, the regularisation entries and the diagonals.
-#include <cublas_v2.h>
-#include <cusolverDn.h>
-
+// The dense steps are this library's own FP64 kernels (dense.cu); the kernels
+// here form the weighted operand, the regularisation entries and the
+// diagonals.
 #include <algorithm>
 #include <string>
 
@@ -157,10 +154,8 @@ void launch_column_sums(int nanz, int manz, const double2 *sens, const double *w
 int run_mcm(const McmArgs &a, cudaStream_t st, std::string &msg) {
     const int n = a.manz, m = a.nanz;
     const size_t nn = (size_t)n * n;
-    double *A = nullptr, *ata = nullptr, *reg = nullptr, *tmp = nullptr, *d = nullptr, *work = nullptr;
-    int *info = nullptr, lwork = 1;
-    cublasHandle_t hb = nullptr;
-    cusolverDnHandle_t hs = nullptr;
+    double *A = nullptr, *ata = nullptr, *reg = nullptr, *Y = nullptr, *cov = nullptr, *d = nullptr, *work = nullptr;
+    int *info = nullptr;
     int rc = 0;
     auto fail = [&](int code, const std::string &what) {
         if (!rc) {
@@ -176,23 +171,11 @@ int run_mcm(const McmArgs &a, cudaStream_t st, std::string &msg) {
     dal((void **)&reg, sizeof(double) * nn);
     dal((void **)&d, sizeof(double) * n);
     dal((void **)&info, sizeof(int));
-    if (!rc && cublasCreate(&hb) != CUBLAS_STATUS_SUCCESS) fail(1000, "cublasCreate");
-    if (!rc && cusolverDnCreate(&hs) != CUSOLVER_STATUS_SUCCESS) fail(1000, "cusolverDnCreate");
+    const int T = 256;
     if (!rc) {
-        cublasSetStream(hb, st);
-        cusolverDnSetStream(hs, st);
-        const int T = 256;
-        // bata
+        // bata: ata = S^T S (lower), S the weighted split of J
         k_weighted_split<<<nb((size_t)m * n, T), T, 0, st>>>(m, n, a.sens, a.wmatd, a.wdfak, A);
-        const double one = 1.0, zero = 0.0;
-        if (cublasDsyrk(hb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, n, 2 * m, &one, A, 2 * m, &zero, ata, n) !=
-            CUBLAS_STATUS_SUCCESS)
-            fail(1000, "cublasDsyrk");
-    }
-    cudaFreeAsync(A, st);
-    A = nullptr;
-    if (!rc) {
-        const int T = 256;
+        dense_syrk_t(n, 2 * m, A, 2 * m, ata, st);
         k_symmetrize_lower<<<nb(nn, T), T, 0, st>>>(n, ata);
         k_diag<<<nb(n, T), T, 0, st>>>(n, ata, d);
         cudaMemcpyAsync(a.diag_ata, d, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
@@ -204,52 +187,41 @@ int run_mcm(const McmArgs &a, cudaStream_t st, std::string &msg) {
             k_reg_neighbours<<<1, 1, 0, st>>>(n, a.nk, a.lam, a.smatm, a.nachbar, ata, reg);
         k_diag<<<nb(n, T), T, 0, st>>>(n, reg, d);
         cudaMemcpyAsync(a.diag_reg, d, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
-        // bmcm: Cholesky factor and inverse
-        int lw1 = 0, lw2 = 0;
-        if (cusolverDnDpotrf_bufferSize(hs, CUBLAS_FILL_MODE_LOWER, n, reg, n, &lw1) != CUSOLVER_STATUS_SUCCESS ||
-            cusolverDnDpotri_bufferSize(hs, CUBLAS_FILL_MODE_LOWER, n, reg, n, &lw2) != CUSOLVER_STATUS_SUCCESS)
-            fail(1000, "cusolver buffer size");
-        lwork = std::max(1, std::max(lw1, lw2));
-        dal((void **)&work, sizeof(double) * (size_t)lwork);
-    }
-    if (!rc) {
+        // bmcm: Cholesky factor L of ata_reg (in place, lower)
+        cudaMemsetAsync(info, 0, sizeof(int), st);
+        dense_potrf(n, reg, info, st);
         int h_info = 0;
-        if (cusolverDnDpotrf(hs, CUBLAS_FILL_MODE_LOWER, n, reg, n, work, lwork, info) != CUSOLVER_STATUS_SUCCESS)
-            fail(1000, "cusolverDnDpotrf");
         cudaMemcpyAsync(&h_info, info, sizeof(int), cudaMemcpyDeviceToHost, st);
         cudaStreamSynchronize(st);
-        if (!rc && h_info != 0) fail(108, "CHOLD mcm :: matrix not pos definite..");  // src/bmcm_mod.f90:447-451
-        if (!rc && cusolverDnDpotri(hs, CUBLAS_FILL_MODE_LOWER, n, reg, n, work, lwork, info) !=
-                       CUSOLVER_STATUS_SUCCESS)
-            fail(1000, "cusolverDnDpotri");
+        if (h_info != 0) fail(108, "CHOLD mcm :: matrix not pos definite..");  // src/bmcm_mod.f90:447-451
     }
+    dal((void **)&Y, sizeof(double) * nn);
+    dal((void **)&cov, sizeof(double) * nn);
     if (!rc) {
-        const int T = 256;
-        k_symmetrize_lower<<<nb(nn, T), T, 0, st>>>(n, reg);  // reg = cov
-        k_diag<<<nb(n, T), T, 0, st>>>(n, reg, d);
+        // cov = L^-T L^-1 (lower), then both triangles
+        dense_potri(n, reg, Y, cov, st);
+        k_symmetrize_lower<<<nb(nn, T), T, 0, st>>>(n, cov);
+        k_diag<<<nb(n, T), T, 0, st>>>(n, cov, d);
         cudaMemcpyAsync(a.diag_cov1, d, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
         if (a.want_res) {  // bres: diag(cov ata)
-            k_diag_of_product<<<n, 256, 0, st>>>(n, reg, ata, d);
+            k_diag_of_product<<<n, 256, 0, st>>>(n, cov, ata, d);
             cudaMemcpyAsync(a.diag_res, d, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
         }
-        if (a.want_res && a.want_cov2) {  // bmcm2: diag(cov (ata cov))
-            dal((void **)&tmp, sizeof(double) * nn);
-            const double one = 1.0, zero = 0.0;
-            if (!rc && cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, ata, n, reg, n, &zero, tmp, n) !=
-                           CUBLAS_STATUS_SUCCESS)
-                fail(1000, "cublasDgemm");
-            if (!rc) {
-                k_diag_of_product<<<n, 256, 0, st>>>(n, reg, tmp, d);
-                cudaMemcpyAsync(a.diag_cov2, d, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
-            }
+    }
+    if (!rc && a.want_res && a.want_cov2) {  // bmcm2: diag(cov ata cov) = column sums of (S cov)^2
+        dal((void **)&work, sizeof(double) * (size_t)((2 * m + 63) / 64) * n);
+        if (!rc) {
+            dense_col_sq_of_product(2 * m, n, A, 2 * m, cov, work, d, st);
+            cudaMemcpyAsync(a.diag_cov2, d, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
         }
     }
     cudaError_t ce = cudaStreamSynchronize(st);
     if (!rc && ce != cudaSuccess) fail(1000, cudaGetErrorString(ce));
-    for (void *p : {(void *)A, (void *)ata, (void *)reg, (void *)tmp, (void *)d, (void *)work, (void *)info})
+    ce = cudaGetLastError();
+    if (!rc && ce != cudaSuccess) fail(1000, cudaGetErrorString(ce));
+    for (void *p : {(void *)A, (void *)ata, (void *)reg, (void *)Y, (void *)cov, (void *)d, (void *)work,
+                    (void *)info})
         if (p) cudaFreeAsync(p, st);
-    if (hb) cublasDestroy(hb);
-    if (hs) cusolverDnDestroy(hs);
     return rc;
 }
 
