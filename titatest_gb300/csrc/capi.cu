@@ -26,7 +26,7 @@ struct RefineCount {
     double z;  // largest relative correction of the step
 };
 constexpr int kRefineCap = 64;  // refinement steps at most (crgpu_set_refinement)
-constexpr int kRefineSlots = 8;  // counter arrays: one per factor round of a pipelined forward
+constexpr int kRefineSlots = 2;  // counter arrays: the full rounds' solves and the last round's
 
 int fail(crgpu_ctx *c, int code, const std::string &msg) {
     if (c) c->last_error = msg;
@@ -393,32 +393,22 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
             e = solve_view(c, B, fuse != 0, c->st, 0);
             if (e) return e;
         } else {
-            // full rounds of 2 blocks per SM, one launch each on st; each round's solves
-            // run on st_solve beside the next round's factor (a sweep block fits beside
-            // the two factor blocks of an SM).  The last, partial round starts on st_hi
-            // once the full rounds are factored and is solved there.
-            const int round = 2 * c->nsm, nfull = (ns - tail) / round;
-            for (int r = 0; r < nfull; r++) {
-                const DevBatch Br = sub_view(c, B, r * round, round);
-                e = run_factor_view(c, Br, fuse, c->st);
-                if (e) return e;
-                cudaEvent_t er = c->ev_round[std::min(r, 7)];
-                CUCHECK(c, cudaEventRecord(er, c->st));
-                CUCHECK(c, cudaStreamWaitEvent(c->st_solve, er, 0));
-                e = solve_view(c, Br, fuse != 0, c->st_solve, std::min(r, kRefineSlots - 2));
-                if (e) return e;
-            }
-            if (!cap) cudaEventRecord(f1, c->st);
-            const DevBatch Bt = sub_view(c, B, ns - tail, tail);
-            CUCHECK(c, cudaEventRecord(c->ev_join2, c->st));
-            CUCHECK(c, cudaStreamWaitEvent(c->st_hi, c->ev_join2, 0));
+            // full rounds on st; the last, partial round starts on st_hi once they are
+            // done, beside the full rounds' solves, and is solved there.  (Factor
+            // launches per round with each round's solves beside the next round's
+            // factor were slower: the sweeps' blocks slowed the latency-bound factor
+            // more than they gained, 46.8 against 37.2 ms per unit on config 2.)
+            const DevBatch Bf = sub_view(c, B, 0, ns - tail), Bt = sub_view(c, B, ns - tail, tail);
+            e = run_factor_view(c, Bf, fuse, c->st);
+            if (e) return e;
+            cudaEventRecord(f1, c->st);
+            CUCHECK(c, cudaStreamWaitEvent(c->st_hi, f1, 0));
             e = run_factor_view(c, Bt, fuse, c->st_hi, true);  // SMs of its own
-            if (!e) e = solve_view(c, Bt, fuse != 0, c->st_hi, kRefineSlots - 1);
+            if (!e) e = solve_view(c, Bt, fuse != 0, c->st_hi, 1);
+            if (!e) e = solve_view(c, Bf, fuse != 0, c->st, 0);
             if (e) return e;
             CUCHECK(c, cudaEventRecord(c->ev_join, c->st_hi));
             CUCHECK(c, cudaStreamWaitEvent(c->st, c->ev_join, 0));
-            CUCHECK(c, cudaEventRecord(c->ev_join2, c->st_solve));
-            CUCHECK(c, cudaStreamWaitEvent(c->st, c->ev_join2, 0));
         }
         launch_kpot(P, B, nr, c->d_kpot, c->d_kpot32, c->st);
         c->stats.kernel_launches += 1;
@@ -628,10 +618,7 @@ int crgpu_create2(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precis
         cudaDeviceGetStreamPriorityRange(&lo, &hi);
         ce = cudaStreamCreateWithPriority(&c->st_hi, cudaStreamNonBlocking, hi);
     }
-    if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&c->st_solve, cudaStreamNonBlocking);
     if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
-    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&c->ev_join2, cudaEventDisableTiming);
-    for (int q = 0; q < 8 && ce == cudaSuccess; q++) ce = cudaEventCreateWithFlags(&c->ev_round[q], cudaEventDisableTiming);
     if (ce != cudaSuccess) {
         c->last_error = cudaGetErrorString(ce);
         *out = c;
@@ -792,10 +779,6 @@ int crgpu_destroy(crgpu_ctx *c) {
     if (c->own_st) cudaStreamDestroy(c->own_st);
     if (c->copy_st) cudaStreamDestroy(c->copy_st);
     if (c->st_hi) cudaStreamDestroy(c->st_hi);
-    if (c->st_solve) cudaStreamDestroy(c->st_solve);
-    if (c->ev_join2) cudaEventDestroy(c->ev_join2);
-    for (auto &ev_ : c->ev_round)
-        if (ev_) cudaEventDestroy(ev_);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     delete c;
     return 0;

@@ -22,9 +22,7 @@ struct crgpu_ctx {
     cudaStream_t st = nullptr, own_st = nullptr;
     cudaStream_t copy_st = nullptr;  // device -> host copies overlapped with compute
     cudaStream_t st_hi = nullptr;    // high priority: the last, partial round of factors and its solves
-    cudaStream_t st_solve = nullptr; // the solves of a factor round while the next round is factored
-    cudaEvent_t ev_join = nullptr, ev_join2 = nullptr;
-    cudaEvent_t ev_round[8] = {};    // end of each factor round (pipelined forward)
+    cudaEvent_t ev_join = nullptr;
     int nsm = 0, device = 0;
     std::vector<void *> allocs;
     // device state
@@ -46,13 +44,13 @@ struct crgpu_ctx {
     // refinement step counters on the device, one array per sub-batch of the
     // current batch: {active count, pad, largest relative correction} per step
     void *d_refine = nullptr;
-    int refine_used[8] = {};  // steps launched on each array since the last collection
+    int refine_used[2] = {};  // steps launched on each array since the last collection
     // forward + Jacobian as one CUDA graph (crgpu_forward_sens_graph)
     bool capturing = false;       // recording: no host copies, synchronisation or timing
     cudaGraphExec_t graph = nullptr;
     const void *graph_key[3] = {nullptr, nullptr, nullptr};  // sigma, volt, sens of the recorded graph
     int graph_mode = -1;
-    int graph_refine_used[8] = {};  // refinement steps recorded in the graph per counter array
+    int graph_refine_used[2] = {};  // refinement steps recorded in the graph per counter array
     int64_t mem_budget = 0;
     bool have_forward = false;
     bool factors_resident = false;  // band factors of every system still in Bmax (one batch)

@@ -62,6 +62,7 @@ constexpr int kTcCols = 256;   // TMEM columns = MMA N
 constexpr int kTcNB = kTcWP / 4;
 constexpr int kTcThreads = 192;
 constexpr int kTcNNB = 4;      // buffers of entering rows
+constexpr int kTcSmemRequest = 110 * 1024;  // at most two blocks (2 x 256 TMEM columns) per SM
 
 struct TcOperands {
     // K-major canonical layout without swizzle: 8-row x 16-byte core
@@ -90,12 +91,6 @@ struct TcSmem {
     int panel_fail;
     int stop_issue;
 };
-
-// the layout rounded up to 1 KB: two blocks fit an SM (2 x 256 TMEM columns)
-// and leave room for a sweep block of the previous round's solves; three
-// never fit, so no block waits for tensor memory
-constexpr int kTcSmemRequest = ((int)sizeof(TcSmem) + 1023) / 1024 * 1024;
-static_assert(3 * (kTcSmemRequest + 1024) > 228 * 1024, "a third block would wait for tensor memory");
 
 // barrier of the 128 panel threads that also returns the OR of `fail`
 __device__ __forceinline__ bool panel_bar_or(bool fail) {
