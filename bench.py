@@ -432,7 +432,8 @@ def run_gpu(args):
 
 def run_ensemble(args):
     """Config 5: 256 independent problems of uneven size (forward + Jacobian
-    each), run concurrently on worker streams; value = problems per second."""
+    each), run concurrently on the contexts' streams from a pool of worker
+    threads; value = problems per second."""
     import torch
 
     from titatest_gb300 import MIXED, synth
@@ -466,7 +467,8 @@ def run_ensemble(args):
         "vs_baseline": None, "dtype": "c64 factor + f64 refinement",
         "data": "synthetic (seeded meshes 40x15..300x80 quads, 24-128 electrodes, 200-6000 quadrupoles)",
         "config": {"workload": f"config5: {len(probs)} problems, {sum(p.grid.sanz for p in probs)} nodes in total",
-                   "workers": args.workers, "parallelism": "single GPU, concurrent streams"},
+                   "workers": args.workers, "parallelism": "single GPU, concurrent streams",
+                   "band_order": "geometric node order for mixed bands beyond the tensor-core window"},
         "clocks": clk.summary(),
     }
     print(json.dumps(line))

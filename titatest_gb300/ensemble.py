@@ -1,11 +1,13 @@
 """Forward + Jacobian of many independent problems (uneven meshes) at once.
 
-Each problem gets its own context (its own band width, pattern and batch
-buffers).  Problems are sorted by their band-factor work (n * mb^2 * number of
-systems), largest first, and handed to a pool of worker threads.  Each worker
-owns a CUDA stream, so the kernels of different problems run concurrently on
-the GPU.  The C ABI releases the GIL, so the workers do not serialise on the
-host.
+Each problem gets its own context (its own band width, pattern, batch
+buffers and CUDA stream).  Problems are sorted by their band-factor work
+(n * mb^2 * number of systems), largest first, and handed to a pool of
+worker threads; every context issues its work on its own stream, so the
+kernels of different problems run concurrently on the GPU.  The C ABI
+releases the GIL, so the workers do not serialise on the host.  Only the C
+ABI is used: sigma and the voltages cross as host arrays, and the Jacobian
+stays on the device (crgpu_sens with no host buffer) unless it is asked for.
 
 The per-worker memory budget is the free device memory divided by the number
 of workers.  A problem whose band factors do not fit is processed in batches
@@ -13,7 +15,6 @@ by its own context.
 """
 from __future__ import annotations
 
-import threading
 from concurrent.futures import ThreadPoolExecutor
 from typing import List, Optional, Sequence
 
@@ -46,40 +47,22 @@ class Ensemble:
             budget_bytes = int(0.5 * free / self.workers)
         self.budget = budget_bytes
         self.order = sorted(range(len(self.problems)), key=lambda i: -problem_work(self.problems[i]))
-        self._tls = threading.local()
-
-    def _stream(self):
-        import torch
-        if not hasattr(self._tls, "stream"):
-            self._tls.stream = torch.cuda.Stream()
-        return self._tls.stream
 
     def _one(self, i: int, sens_mode: Optional[int], keep_sens: bool):
-        import torch
-
         p = self.problems[i]
-        st = self._stream()
-        with torch.cuda.stream(st):
-            sig = torch.from_numpy(np.ascontiguousarray(p.sigma, np.complex128)).to("cuda", non_blocking=False)
-            volt = torch.empty(p.survey.nanz, dtype=torch.complex128, device="cuda")
-            with CRMod(p.grid, p.survey, precision=self.precision) as m:
-                m.set_stream(st.cuda_stream)
-                m.set_refinement(*self.refine)
-                m.set_memory_budget(self.budget)
-                if self.autotune:
-                    m.autotune(p.sigma)
-                m.forward_device(sig.data_ptr(), volt.data_ptr())
-                out = {"index": i, "nanz": p.survey.nanz, "elanz": p.grid.elanz}
-                if sens_mode is not None:
-                    sens = torch.empty((p.grid.elanz, p.survey.nanz), dtype=torch.complex128, device="cuda")
-                    m.sens_device(int(sens_mode), sens.data_ptr())
-                    if keep_sens:
-                        out["sens"] = sens.T.cpu().numpy()
-                    else:  # a checksum keeps the result observable without the copy
-                        out["sens_abs_sum"] = float(sens.abs().sum())
-                out["stats"] = m.stats()
-            out["volt"] = volt.cpu().numpy()
-        st.synchronize()
+        with CRMod(p.grid, p.survey, precision=self.precision) as m:
+            m.set_refinement(*self.refine)
+            m.set_memory_budget(self.budget)
+            if self.autotune:
+                m.autotune(p.sigma)
+            out = {"index": i, "nanz": p.survey.nanz, "elanz": p.grid.elanz}
+            out["volt"] = m.forward(p.sigma)["volt"]
+            if sens_mode is not None:
+                if keep_sens:
+                    out["sens"] = m.sens(int(sens_mode))
+                else:
+                    m.sens_on_device(int(sens_mode))
+            out["stats"] = m.stats()
         return out
 
     def run(self, sens_mode: Optional[int] = 0, keep_sens: bool = False) -> List[dict]:
