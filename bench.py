@@ -446,15 +446,16 @@ def run_ensemble(args):
     # config 5: 25.4 problems/s tuned against 27.1 with the built-in choices)
     ens = Ensemble(probs, precision=MIXED, workers=args.workers, refine_maxit=args.refine_maxit,
                    refine_tol=args.refine_tol, autotune=args.autotune_ensemble)
+    go = (lambda: ens.run_batched(sens_mode=0)) if args.ensemble_batched else (lambda: ens.run(sens_mode=0))
     for _ in range(max(1, args.warmup)):
-        ens.run(sens_mode=0)
+        go()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(0) as clk:
         ev0.record()
         t0 = time.time()
         for _ in range(args.steps):
-            ens.run(sens_mode=0)
+            go()
         torch.cuda.synchronize()
         wall = time.time() - t0
         ev1.record()
@@ -467,7 +468,10 @@ def run_ensemble(args):
         "vs_baseline": None, "dtype": "c64 factor + f64 refinement",
         "data": "synthetic (seeded meshes 40x15..300x80 quads, 24-128 electrodes, 200-6000 quadrupoles)",
         "config": {"workload": f"config5: {len(probs)} problems, {sum(p.grid.sanz for p in probs)} nodes in total",
-                   "workers": args.workers, "parallelism": "single GPU, concurrent streams",
+                   "workers": args.workers,
+                   "parallelism": ("single GPU, waves of problems: one tensor-core factor launch over all "
+                                   "systems of a wave, the other steps on the problems' streams" if args.ensemble_batched
+                                   else "single GPU, one context per problem on concurrent streams"),
                    "band_order": "geometric node order for mixed bands beyond the tensor-core window"},
         "clocks": clk.summary(),
     }
@@ -631,6 +635,9 @@ def main():
                          "1e-6 / 1e-5; both errors are measured and checked in every line), 1e-2 elsewhere")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--workers", type=int, default=8, help="config 5: concurrent worker streams")
+    ap.add_argument("--ensemble-batched", action="store_true",
+                    help="config 5: waves of problems with one factor launch each (crgpu_forward_sens_batch) "
+                         "instead of one context per problem on worker streams")
     ap.add_argument("--ensemble-count", type=int, default=256, help="config 5: number of problems")
     ap.add_argument("--case", action="store_true",
                     help="plain timings of one forward of --config (the command the ncu captures run)")

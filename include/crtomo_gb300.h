@@ -177,6 +177,26 @@ int crgpu_forward_device(crgpu_ctx *ctx, const void *sigma_device, int32_t volt_
 int crgpu_sens(crgpu_ctx *ctx, int32_t mode, double *sens);
 int crgpu_sens_device(crgpu_ctx *ctx, int32_t mode, void *sens_device);
 
+/* Several problems at once (uneven meshes; no single counterpart in the
+ * reference, which runs one mesh per CRMod call: src/fem.f90:327-470 for each).
+ * The forward of every context (sigma[p] host, elanz complex), its voltages
+ * into volt[p] (host, nanz complex: V for volt_mode 0, the CRTomo data for
+ * 1) and, for sens_mode 0 or 1, its Jacobian kept on the device (as
+ * crgpu_sens(ctx, mode, NULL)); sens_mode -1: none.  The band factors of all
+ * problems' systems run in one persistent tensor-core launch over a table of
+ * (problem, system) items, longest systems first; assembly and the solves run
+ * on each context's own stream.  Every context must be CRGPU_MIXED with a band
+ * that fits the tensor-core window (as created; see crgpu_create2), without
+ * singularity removal, DC mode or boundary values, and its systems must fit
+ * one batch in device memory (crgpu_memory_need); else 1002 or a CUDA error. */
+int crgpu_forward_sens_batch(crgpu_ctx *const *ctxs, int32_t nprob, const double *const *sigma, int32_t volt_mode,
+                             double *const *volt, int32_t sens_mode);
+
+/* No counterpart in the reference.  Device memory a forward + Jacobian of
+ * this context still has to allocate (its batch of all systems and the
+ * Jacobian), for hosts that group problems to fit. */
+int crgpu_memory_need(const crgpu_ctx *ctx, int64_t *bytes);
+
 /* Device buffers of the last forward (valid until the next call):
  * kpot(sanz, eanz, kwnanz), hpot(sanz, eanz), fak per system. */
 int crgpu_device_buffers(crgpu_ctx *ctx, void **kpot_device, void **hpot_device);

@@ -32,6 +32,7 @@ EXPORTS = (
     "crgpu_adjoint", "crgpu_adjoint_device", "crgpu_autotune", "crgpu_get_tune", "crgpu_forward_sens_graph",
     "crgpu_set_boundary_values", "crgpu_update_fpi", "crgpu_blam0_jtj", "crgpu_set_dc", "crgpu_update_dc",
     "crgpu_mcm", "crgpu_column_sums", "crgpu_device_memory", "crgpu_create2", "crgpu_node_order",
+    "crgpu_forward_sens_batch", "crgpu_memory_need",
 )
 
 

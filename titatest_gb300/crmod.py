@@ -264,6 +264,12 @@ class CRMod:
     def sens_device(self, mode: int, sens_ptr: int):
         _check(self._h, lib().crgpu_sens_device(self._h, int(mode), C.c_void_p(sens_ptr)))
 
+    def memory_need(self) -> int:
+        """crgpu_memory_need: device bytes a forward + Jacobian still allocates."""
+        b = C.c_int64(0)
+        _check(self._h, lib().crgpu_memory_need(self._h, C.byref(b)))
+        return b.value
+
     def node_order(self) -> np.ndarray:
         """crgpu_node_order: the grid node (1-based) in each position of the
         context's device arrays."""
@@ -375,3 +381,22 @@ def run_tomodir(exe_dir: str, precision: int = PLAIN, write: bool = True):
         return out
     finally:
         m.close()
+
+
+def forward_sens_batch(models, sigmas, sens_mode: int = 0, volt_mode: int = 0):
+    """crgpu_forward_sens_batch: the forward of every model (MIXED contexts
+    whose bands fit the tensor-core window), their band factors in one
+    persistent launch; the Jacobians (sens_mode 0 or 1; -1 none) stay on the
+    devices of the contexts.  Returns the voltages, one array per model."""
+    n = len(models)
+    sig = [np.ascontiguousarray(s, np.complex128) for s in sigmas]
+    volts = [np.zeros(m.survey.nanz, np.complex128) for m in models]
+    ctxs = (C.c_void_p * n)(*[m._h.value for m in models])
+    sp = (C.c_void_p * n)(*[s.ctypes.data for s in sig])
+    vp = (C.c_void_p * n)(*[v.ctypes.data for v in volts])
+    code = lib().crgpu_forward_sens_batch(ctxs, n, sp, int(volt_mode), vp, int(sens_mode))
+    if code:
+        bad = next((m for m in models if lib().crgpu_last_error(m._h)), models[0])
+        raise CRGPUError(code, lib().crgpu_last_error(bad._h).decode())
+    return volts
+

@@ -999,6 +999,118 @@ int crgpu_sens_device(crgpu_ctx *c, int32_t mode, void *sens_device) {
 // The Jacobian to host memory: computed in chunks of elements, each chunk's
 // columns (contiguous in sens(nanz, manz)) copied by a second stream while
 // the next chunk is computed.
+int crgpu_memory_need(const crgpu_ctx *c, int64_t *bytes) {
+    if (!c || !bytes) return ERR_ARG;
+    const int nsys = (int)c->sys_k.size();
+    int64_t need = c->batch_cap >= nsys ? 0 : (int64_t)bytes_per_system(c) * nsys;
+    if (!c->d_sens) need += (int64_t)c->nanz * c->hg.elanz * (int64_t)sizeof(double2);
+    *bytes = need;
+    return 0;
+}
+
+// Forward and Jacobian of several mixed-precision contexts (uneven meshes):
+// each problem is assembled on its own stream, the band factors of all their
+// systems run in one persistent tensor-core launch over a table of (problem,
+// system) items, longest systems first, and each problem's solves,
+// refinement, back-transform, voltages and Jacobian then run on its own
+// stream again.  Every problem must fit one batch (crgpu_memory_need).
+int crgpu_forward_sens_batch(crgpu_ctx *const *ctxs, int32_t nprob, const double *const *sigma, int32_t volt_mode,
+                             double *const *volt, int32_t sens_mode) {
+    if (!ctxs || nprob <= 0 || !sigma || !volt || (sens_mode < -1 || sens_mode > 1)) return ERR_ARG;
+    for (int p = 0; p < nprob; p++) {
+        crgpu_ctx *c = ctxs[p];
+        if (!c || !sigma[p] || !volt[p]) return ERR_ARG;
+        if (c->precision != CRGPU_MIXED || c->hg.mb + 4 > 128 || c->lsr || c->P.ldc || c->P.lrandb2 ||
+            c->nrhs != 1 || c->device != ctxs[0]->device)
+            return fail(c, ERR_UNSUPPORTED, "batched forward: mixed precision on the tensor-core window only");
+    }
+    cudaStream_t st0 = ctxs[0]->st;
+    std::vector<DevProblem> hp(nprob);
+    std::vector<DevBatch> hb(nprob);
+    std::vector<int> order(nprob);
+    for (int p = 0; p < nprob; p++) {  // assembly and right-hand sides, each on its stream
+        crgpu_ctx *c = ctxs[p];
+        const int ns = (int)c->sys_k.size();
+        c->stats = crgpu_stats{};
+        c->factors_resident = false;
+        drop_graph(c);
+        int e = ensure_batch(c, ns);
+        if (e) return e;
+        CUCHECK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+        CUCHECK(c, cudaMemcpyAsync(c->d_sigma, sigma[p], sizeof(double2) * c->hg.elanz, cudaMemcpyHostToDevice, c->st));
+        launch_adom(c->P, c->d_sigma, c->d_adom, c->st);
+        e = load_batch(c, 0, ns);
+        if (!e) e = assemble_batch(c, c->d_sigma, ns);
+        if (e) return e;
+        const DevBatch B = batch_view(c, ns);
+        launch_rhs(c->P, B, 1, c->lsink, c->nsink, c->st);
+        c->stats.kernel_launches += 3;
+        c->stats.nsystems = ns;
+        CUCHECK(c, cudaEventRecord(c->ev_join, c->st));
+        CUCHECK(c, cudaStreamWaitEvent(st0, c->ev_join, 0));
+        hp[p] = c->P;
+        hb[p] = B;
+        order[p] = p;
+    }
+    // the item table, longest systems first
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return ctxs[a]->hg.n > ctxs[b]->hg.n; });
+    std::vector<int2> items;
+    for (int p : order)
+        for (int q = 0; q < hb[p].nsys; q++) items.push_back(make_int2(p, q));
+    DevProblem *dP = nullptr;
+    DevBatch *dB = nullptr;
+    int2 *dI = nullptr;
+    crgpu_ctx *c0 = ctxs[0];
+    CUCHECK(c0, cudaMallocAsync((void **)&dP, sizeof(DevProblem) * nprob, st0));
+    CUCHECK(c0, cudaMallocAsync((void **)&dB, sizeof(DevBatch) * nprob, st0));
+    CUCHECK(c0, cudaMallocAsync((void **)&dI, sizeof(int2) * items.size(), st0));
+    CUCHECK(c0, cudaMemcpyAsync(dP, hp.data(), sizeof(DevProblem) * nprob, cudaMemcpyHostToDevice, st0));
+    CUCHECK(c0, cudaMemcpyAsync(dB, hb.data(), sizeof(DevBatch) * nprob, cudaMemcpyHostToDevice, st0));
+    CUCHECK(c0, cudaMemcpyAsync(dI, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice, st0));
+    launch_factor_tc_multi(dP, dB, dI, (int)items.size(), 1, c0->nsm, st0);
+    CUCHECK(c0, cudaGetLastError());
+    CUCHECK(c0, cudaEventRecord(c0->ev_join, st0));
+    for (int p = 0; p < nprob; p++) {  // solves, refinement, voltages and Jacobian, each on its stream
+        crgpu_ctx *c = ctxs[p];
+        if (p > 0) CUCHECK(c, cudaStreamWaitEvent(c->st, c0->ev_join, 0));
+        int e = solve_view(c, hb[p], true, c->st, 0);
+        if (e) return e;
+        launch_kpot(c->P, hb[p], 1, c->d_kpot, c->d_kpot32, c->st);
+        launch_rtrafo(c->P, c->d_kpot, c->d_hpot, c->st);
+        launch_bvolt(c->P, c->d_hpot, volt_mode, nullptr, c->d_volt, c->d_sigmaa, c->st);
+        c->stats.kernel_launches += 4;
+        if (sens_mode >= 0) {
+            if (!c->d_sens) {
+                e = dalloc(c, &c->d_sens, (size_t)c->nanz * c->hg.elanz);
+                if (e) return e;
+            }
+            launch_bsens(c->P, c->d_kpot, c->d_kpot32, c->d_sigma, c->d_volt, sens_mode, true, c->d_sens, c->st);
+            c->stats.kernel_launches += 1;
+            c->last_sens = c->d_sens;
+        }
+    }
+    // the voltages once every problem's work is queued (a copy into pageable
+    // host memory returns only when it is done)
+    int worst = 0;
+    for (int p = 0; p < nprob; p++) {
+        crgpu_ctx *c = ctxs[p];
+        CUCHECK(c, cudaMemcpyAsync(volt[p], volt_mode == 0 ? c->d_volt : c->d_sigmaa, sizeof(double2) * c->nanz,
+                                   cudaMemcpyDeviceToHost, c->st));
+        c->stats.kernel_launches += p == 0 ? 1 : 0;  // the shared factor launch
+        int e = check_device_errors(c, hb[p].status, hb[p].nsys);
+        if (!e) e = collect_refine_stats(c);
+        if (e && !worst) worst = e;
+        c->have_forward = !e;
+        c->factors_resident = !e;
+        c->stats.nbatches = 1;
+    }
+    cudaFreeAsync(dP, st0);
+    cudaFreeAsync(dB, st0);
+    cudaFreeAsync(dI, st0);
+    CUCHECK(c0, cudaStreamSynchronize(st0));
+    return worst;
+}
+
 int crgpu_sens(crgpu_ctx *c, int32_t mode, double *sens) {
     if (!c || (mode != 0 && mode != 1)) return ERR_ARG;
     if (!c->have_forward) return fail(c, ERR_ARG, "crgpu_sens before crgpu_forward");

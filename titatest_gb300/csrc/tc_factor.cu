@@ -168,14 +168,20 @@ __device__ __forceinline__ void issue_range(uint32_t tbase, const TcOperands &o,
 
 }  // namespace
 
-__global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBatch B, int fuse) {
+// MULTI = false: the systems of one batch (P1, B1).  MULTI = true: a table of
+// (problem, system) items over several problems (uneven meshes), whose
+// descriptors Ps[p], Bs[p] are in device memory; the table lists the longest
+// systems first, so the persistent blocks finish together.
+template <bool MULTI>
+__global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P1, DevBatch B1,
+                                                             const DevProblem *__restrict__ Ps,
+                                                             const DevBatch *__restrict__ Bs,
+                                                             const int2 *__restrict__ items, int nitems, int fuse) {
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
     TcSmem &S = *reinterpret_cast<TcSmem *>(tc_smem_raw);
     volatile int *abort_flag = &S.abort_flag;
-    const int n = P.n, mb = P.mb, Wb = mb + 1, rw = P.rw;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const bool is_panel = warp < 4, is_stage = warp == 4, is_mma = warp == 5;
-    const int nblk = (n + 3) / 4;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&S.tmem_base)),
@@ -190,7 +196,13 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
     const uint32_t tlane = tbase + ((uint32_t)(32 * (warp & 3)) << 16);  // this warp's lanes
 
     bool stop = false;
-    for (int s = blockIdx.x; s < B.nsys && !stop; s += gridDim.x) {
+    const int total = MULTI ? nitems : B1.nsys;
+    for (int it = blockIdx.x; it < total && !stop; it += gridDim.x) {
+        const DevProblem &P = MULTI ? Ps[items[it].x] : P1;
+        const DevBatch &B = MULTI ? Bs[items[it].x] : B1;
+        const int s = MULTI ? items[it].y : it;
+        const int n = P.n, mb = P.mb, Wb = mb + 1, rw = P.rw;
+        const int nblk = (n + 3) / 4;
         float2 *L = (float2 *)B.L + (size_t)s * B.lpitch;
         float2 *yv = (float2 *)B.y + (size_t)s * n;
         const double2 *as = B.As + (size_t)s * P.nnz;
@@ -596,8 +608,7 @@ __global__ __launch_bounds__(kTcThreads, 2) void k_factor_tc(DevProblem P, DevBa
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tbase), "r"(kTcCols) : "memory");
 }
 
-int launch_factor_tc(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st, bool exclusive) {
-    if (P.mb + 4 > kTcWP) return ERR_UNSUPPORTED;
+static int tc_smem_optin() {
     static std::once_flag once;
     static int optin = kTcSmemRequest;
     std::call_once(once, [] {
@@ -605,13 +616,30 @@ int launch_factor_tc(const DevProblem &P, const DevBatch &B, int fuse, int nsm, 
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         if (optin < kTcSmemRequest) optin = kTcSmemRequest;
-        cudaFuncSetAttribute(k_factor_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_factor_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_factor_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     });
+    return optin;
+}
+
+int launch_factor_tc(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st, bool exclusive) {
+    if (P.mb + 4 > kTcWP) return ERR_UNSUPPORTED;
+    const int optin = tc_smem_optin();
     static_assert(sizeof(TcSmem) <= kTcSmemRequest, "shared memory layout exceeds the request");
     const int per_sm = exclusive ? 1 : 2;
     const int grid = B.nsys < per_sm * nsm ? B.nsys : per_sm * nsm;
-    k_factor_tc<<<grid, kTcThreads, exclusive ? optin : kTcSmemRequest, st>>>(P, B, fuse);
+    k_factor_tc<false><<<grid, kTcThreads, exclusive ? optin : kTcSmemRequest, st>>>(P, B, nullptr, nullptr, nullptr, 0,
+                                                                                      fuse);
     return 0;
+}
+
+// the band factors of several problems' batches in one launch: items (problem,
+// system) in device memory, every problem's mb + 4 <= 128 (checked by the caller)
+void launch_factor_tc_multi(const DevProblem *Ps, const DevBatch *Bs, const int2 *items, int nitems, int fuse, int nsm,
+                            cudaStream_t st) {
+    tc_smem_optin();
+    const int grid = nitems < 2 * nsm ? nitems : 2 * nsm;
+    k_factor_tc<true><<<grid, kTcThreads, kTcSmemRequest, st>>>(DevProblem{}, DevBatch{}, Ps, Bs, items, nitems, fuse);
 }
 
 }  // namespace crgpu

@@ -21,7 +21,8 @@ from typing import List, Optional, Sequence
 import numpy as np
 
 from . import MIXED, CRMod
-from ._lib import device_memory
+from ._lib import CRGPUError, device_memory
+from .crmod import forward_sens_batch
 
 
 def problem_work(p) -> float:
@@ -71,4 +72,56 @@ class Ensemble:
         with ThreadPoolExecutor(max_workers=self.workers) as ex:
             for r in ex.map(lambda i: self._one(i, sens_mode, keep_sens), self.order):
                 results[r["index"]] = r
+        return results  # type: ignore[return-value]
+
+    def run_batched(self, sens_mode: Optional[int] = 0, reserve_frac: float = 0.1) -> List[dict]:
+        """Runs every problem in waves that fit device memory: per wave one
+        crgpu_forward_sens_batch (all band factors of the wave in one
+        persistent launch, longest systems first).  The contexts of a wave are
+        created by the worker threads (the C ABI releases the GIL).  Problems
+        the batched call does not take (bands beyond the tensor-core window)
+        run one by one."""
+        results: List[Optional[dict]] = [None] * len(self.problems)
+        _, total = device_memory()
+        reserve = int(reserve_frac * total)
+        order = list(self.order)
+
+        def create(q):
+            p = self.problems[q]
+            m = CRMod(p.grid, p.survey, precision=self.precision)
+            m.set_refinement(*self.refine)
+            return q, m, m.memory_need()
+
+        def run_wave(wave):
+            try:
+                volts = forward_sens_batch([m for _, m in wave], [self.problems[q].sigma for q, _ in wave],
+                                           sens_mode=-1 if sens_mode is None else int(sens_mode))
+                for (q, m), v in zip(wave, volts):
+                    results[q] = {"index": q, "volt": v, "stats": m.stats()}
+            except CRGPUError:
+                for q, m in wave:  # one by one
+                    results[q] = self._one(q, sens_mode, False)
+            finally:
+                for _, m in wave:
+                    m.close()
+
+        with ThreadPoolExecutor(max_workers=self.workers) as ex:
+            i = 0
+            while i < len(order):
+                wave, pending = [], 0
+                while i < len(order):
+                    made = list(ex.map(create, order[i:i + self.workers]))
+                    free, _ = device_memory()  # the contexts made so far hold their own memory
+                    stop = False
+                    for q, m, need in made:
+                        if stop or (wave and need + pending > free - reserve):
+                            m.close()
+                            stop = True
+                            continue
+                        wave.append((q, m))
+                        pending += need
+                        i += 1
+                    if stop:
+                        break
+                run_wave(wave)
         return results  # type: ignore[return-value]
