@@ -124,6 +124,53 @@ def fp64_dgemm_tflops(stream) -> float:
     return 2.0 * 4096 ** 3 / (best * 1e-3) / 1e12
 
 
+def fp32_sgemm_tflops(stream) -> float:
+    """The FP32 FMA-pipe rate of this GPU as cuBLAS SGEMM reaches it (TF32
+    off, 8192^3, best of 3, CUDA events): the denominator of the SIMT
+    complex64 factor kernels' roofline."""
+    import torch
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        a = torch.randn(8192, 8192, dtype=torch.float32, device="cuda")
+        b = torch.randn(8192, 8192, dtype=torch.float32, device="cuda")
+        torch.matmul(a, b)
+        best = float("inf")
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            torch.matmul(a, b)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+    return 2.0 * 8192 ** 3 / (best * 1e-3) / 1e12
+
+
+def factored_band(m, g) -> int:
+    """Band width of the matrix a context factors: the grid's, or that of its
+    geometric node order (crgpu_node_order)."""
+    order = np.asarray(m.node_order(), dtype=np.int64) - 1  # grid node at each position
+    pos = np.empty(g.sanz, np.int64)
+    pos[order] = np.arange(g.sanz)
+    area = np.asarray(g.nrel[: g.nelanz[0]], dtype=np.int64) - 1
+    p = pos[area]
+    return int((p.max(axis=1) - p.min(axis=1)).max())
+
+
+FACTOR_KERNELS = {"tensor cores": ("k_factor_tc", "tensor"), "SIMT warp per system": ("k_factor_warp", "fp32"),
+                  "SIMT register tiles": ("k_factor_mixed", "fp32"),
+                  "SIMT shared-memory tiles": ("k_factor_mixed_smem", "fp32")}
+
+
+FACTOR_NOTES = {
+    "k_factor_warp": "latency-bound band factor: a serial chain per column (pivot, reciprocal, rank-1 update of "
+                     "the 64-slot window held in one warp's registers), one system per warp, 12 warps an SM",
+    "k_factor_tc": "latency-bound band factor: each 4-column step is a serial panel plus 4 tf32 MMAs (3 hi/lo "
+                   "products + row injection) on a 128x128 complex window"}
+
+
 def read_profile_traffic(name: str):
     """DRAM bytes per launch recorded from an ncu capture (profiles/<name>)."""
     p = os.path.join(ROOT, "profiles", name)
@@ -270,7 +317,7 @@ def run_gpu(args):
     volt_dev = torch.zeros(2 * nanz, dtype=torch.float64, device="cuda")
     sens_dev = torch.zeros(2 * nanz * manz, dtype=torch.float64, device="cuda")
 
-    mixed = CRMod(g, sv, precision=MIXED)
+    mixed = CRMod(g, sv, precision=MIXED, band_order=args.band_order)
     mixed.set_stream(stream.cuda_stream)
     mixed.set_refinement(args.refine_maxit, args.refine_tol)
     tune = mixed.autotune(s.sigma) if not args.no_autotune else mixed.tune()
@@ -355,7 +402,7 @@ def run_gpu(args):
 
     # ---- plain complex128 on the same inputs
     mixed_stats = mixed.stats()
-    plain = CRMod(g, sv, precision=PLAIN)
+    plain = CRMod(g, sv, precision=PLAIN, band_order=args.band_order)
     plain.set_stream(stream.cuda_stream)
     unit(plain)  # warm-up
     torch.cuda.synchronize()
@@ -374,16 +421,24 @@ def run_gpu(args):
     err_j = float(np.abs(sens_mixed - sens_plain).max() / np.abs(sens_plain).max())
     plain.close()
 
-    # ---- roofline of the dominant kernel (the complex64 band factorisation on
-    #      the tensor cores); algorithmic work = complex L L^T of every system
+    # ---- roofline of the dominant kernel (the complex64 band factorisation of
+    #      the band the context factors); algorithmic work = complex L L^T of
+    #      every system, 4 n mb^2 flops
     n, mb = g.sanz, g.mb
+    mb_mixed = factored_band(mixed, g)
     nsys = K * sv.eanz
-    flops_factor = nsys * 4.0 * n * mb * mb  # 8 flops per complex multiply-add, n*mb^2/2 of them
+    flops_factor = nsys * 4.0 * n * mb * mb  # the grid's band: the complex128 arm factors it
+    flops_mixed = nsys * 4.0 * n * mb_mixed * mb_mixed
     fp64_peak = fp64_dgemm_tflops(stream)
     fac_avg_ms = statistics.mean(fac_ms)
-    achieved = flops_factor / (fac_avg_ms * 1e-3) / 1e12
-    peak, peak_source = tensor_peak_tflops()
-    traffic = read_profile_traffic("k_factor_tc_cfg2.txt")
+    achieved = flops_mixed / (fac_avg_ms * 1e-3) / 1e12
+    kname, bound = FACTOR_KERNELS.get(tune["factor"], ("k_factor_tc", "tensor"))
+    if bound == "tensor":
+        peak, peak_source = tensor_peak_tflops()
+    else:
+        peak = fp32_sgemm_tflops(stream)
+        peak_source = "cuBLAS SGEMM 8192^3, TF32 off, measured in this run (best of 3, CUDA events)"
+    traffic = read_profile_traffic(f"{kname}_cfg2.txt")
     line = {
         "metric": METRIC, "value": value, "unit": "units/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -412,12 +467,14 @@ def run_gpu(args):
         "accuracy_target": {"volt": 1e-6, "jacobian": 1e-5, "met": bool(err_v < 1e-6 and err_j < 1e-5)},
         "phases_ms": {"factor": fac_avg_ms, "solve": mixed_stats["ms_solve"],
                       "forward": mixed_stats["ms_forward"], "sens": statistics.mean(sens_ms)},
-        "roofline": {"kernel": "k_factor_tc", "bound": "tensor", "achieved": achieved, "peak": peak,
+        "factor_band": {"grid_mb": mb, "factored_mb": mb_mixed,
+                        "node_order": "geometric" if mb_mixed != mb else "grid"},
+        "roofline": {"kernel": kname, "bound": bound, "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_source,
-                     "algorithmic": "4*n*mb^2 flops per band system (complex L L^T), all systems of one forward",
-                     "note": "latency-bound band factor: each 4-column step is a serial panel plus 4 tf32 MMAs "
-                             "(3 hi/lo products + row injection) on a 128x128 complex window"},
+                     "algorithmic": "4*n*mb^2 flops per band system (complex L L^T) at the factored band, all "
+                                    "systems of one forward",
+                     "note": FACTOR_NOTES.get(kname, "")},
     }
     kwn, kwnwi = mixed.kwn, mixed.kwnwi
     mixed.close()
@@ -578,8 +635,10 @@ def run_case(args):
 
     s = synth.make(args.config)
     prec = MIXED if args.precision == "mixed" else PLAIN
-    with CRMod(s.grid, s.survey, precision=prec) as m:
+    with CRMod(s.grid, s.survey, precision=prec, band_order=args.band_order) as m:
         m.set_refinement(args.refine_maxit, args.refine_tol)
+        if args.autotune_case:
+            print("tune", m.autotune(s.sigma), flush=True)
         if args.batch:
             g = s.grid
             esz = 8 if prec == MIXED else 16
@@ -642,6 +701,10 @@ def main():
     ap.add_argument("--case", action="store_true",
                     help="plain timings of one forward of --config (the command the ncu captures run)")
     ap.add_argument("--precision", choices=["mixed", "plain"], default="mixed", help="--case: precision")
+    ap.add_argument("--band-order", type=int, default=1, choices=[0, 1, 2],
+                    help="crgpu_create2 band order: 0 the grid's band, 1 geometric for mixed bands beyond the "
+                         "tensor-core window, 2 geometric whenever narrower")
+    ap.add_argument("--autotune-case", action="store_true", help="--case: autotune the factor kernel first")
     ap.add_argument("--batch", type=int, default=0, help="--case: systems per factor batch (0: as many as fit)")
     ap.add_argument("--repeat", type=int, default=1, help="--case: forwards to run")
     ap.add_argument("--sens", action="store_true", help="--case: also the Jacobian")

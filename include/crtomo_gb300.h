@@ -86,12 +86,15 @@ int crgpu_create(const crgpu_grid *grid, const crgpu_survey *survey, int32_t pre
 /* crgpu_create with the choice of the complex64 factor's node order (no
  * counterpart in the reference, which factors in the cutmckee band):
  * band_order 0 keeps the grid's band; 1 (crgpu_create's default) lets a
- * CRGPU_MIXED context whose band is too wide for the tensor-core window
- * (mb > 124) number its nodes by their coordinate along the mesh's longer
- * extent when that band fits the window.  The refinement's FP64 residuals
- * use the same matrix, so only the preconditioner changes; potentials,
+ * CRGPU_MIXED context number its nodes by their coordinate along the mesh's
+ * longer extent when that band is narrower than the grid's (for a grid band
+ * too wide for the tensor-core window, mb > 124, only when the new band fits
+ * it); 2 lets any context (either precision) factor in that order whenever
+ * its band is narrower.  The refinement's FP64 residuals use the same matrix, so only the
+ * preconditioner changes; potentials,
  * voltages and sensitivities come back in the grid's order and numbering.
- * Such a context returns 1002 from crgpu_factor_system; its device buffers
+ * Such a context returns 1002 from crgpu_factor_system and
+ * crgpu_factor_system_noalloc; its device buffers
  * (crgpu_device_buffers) are in the order crgpu_node_order reports. */
 int crgpu_create2(const crgpu_grid *grid, const crgpu_survey *survey, int32_t precision, int32_t band_order,
                   crgpu_ctx **ctx);
@@ -343,8 +346,9 @@ int crgpu_forward_sens_graph(crgpu_ctx *ctx, const void *sigma_device, void *vol
                              void *sens_device);
 
 /* Autotuner (mixed precision): times the band-factor kernels that can run
- * this problem (tensor cores; SIMT register tiles at 1, 2 and 4 blocks per
- * SM; SIMT shared-memory tiles) on its first batch of systems, and the two
+ * this problem (one warp per system; tensor cores; SIMT register tiles at
+ * 1, 2 and 4 blocks per SM; SIMT shared-memory tiles) on its first batch of
+ * systems, and the two
  * CRMod Jacobian kernels (tensor-core Gram form, SIMT direct form), for the
  * conductivities sigma (elanz complex, host), and keeps the fastest for
  * this context.  Choices are cached for the process by problem shape (n, mb,
@@ -353,10 +357,15 @@ int crgpu_forward_sens_graph(crgpu_ctx *ctx, const void *sigma_device, void *vol
 int crgpu_autotune(crgpu_ctx *ctx, const double *sigma, int32_t flags);
 
 /* The context's launch choices: out[0] factor kernel (0 default, 1 tensor
- * cores, 2 SIMT register tiles, 3 SIMT shared-memory tiles), out[1] SIMT
+ * cores, 2 SIMT register tiles, 3 SIMT shared-memory tiles, 4 one warp per
+ * system with the window in its registers, mb <= 63), out[1] SIMT
  * blocks per SM (0 default), out[2] CRMod Jacobian (0 default, 1 tensor
  * cores, 2 SIMT). */
 int crgpu_get_tune(const crgpu_ctx *ctx, int32_t *out);
+
+/* Sets the launch choices in the layout of crgpu_get_tune (a kernel that
+ * cannot run this problem falls back to the default); blocks per SM 0..8. */
+int crgpu_set_tune(crgpu_ctx *ctx, const int32_t *in);
 
 #ifdef __cplusplus
 }

@@ -201,7 +201,8 @@ def test_tensor_core_factor_matches_oracle_chol(gpu_lib):
     assert g.mb + 4 <= 128
     P = O.Problem(g, sv)
     kwn, kwnwi = P.rwaven()
-    with CRMod(g, sv, kwn, kwnwi, precision=MIXED) as m:
+    with CRMod(g, sv, kwn, kwnwi, precision=MIXED, band_order=0) as m:  # the grid's own band
+        m.set_tune(1)  # tensor cores
         for k, l in [(1, 1), (len(kwn), sv.eanz)]:
             a_ref, fak_ref = P.factor(sig, kwn, k, l)
             a, fak = m.factor_system(sig, k, l)
@@ -209,6 +210,49 @@ def test_tensor_core_factor_matches_oracle_chol(gpu_lib):
             for i in range(g.sanz):
                 lo = max(0, g.mb - i)
                 assert relerr(a[i, lo:], a_ref[i, lo:]) < 1e-3, (k, l, i)
+
+
+def _strip_case(nx, nz, ne, seed=23):
+    """A strip of nx x nz quads in its natural numbering (x fastest): band
+    width nx + 2, (nx+1)(nz+1) nodes, ne surface electrodes."""
+    from titatest_gb300 import formats, synth
+    grid, surface, X, Y = synth._quad_grid(np.arange(nx + 1, dtype=float), np.arange(nz + 1, dtype=float))
+    area = grid.nrel[: grid.nelanz[0]]
+    grid.mb = int((area.max(axis=1) - area.min(axis=1)).max())
+    enr = surface[np.linspace(0, nx, ne).astype(int)]
+    s, v = synth._encode(synth.dipole_dipole(ne, [1], [1, 2]))
+    survey = formats.Survey(enr=enr, strnr=s, vnr=v, strom=np.ones(len(s)))
+    mag, pha = synth.random_model(grid, np.random.default_rng(seed))
+    return grid, survey, synth._sigma_from(mag, pha)
+
+
+@pytest.mark.parametrize("nx,nz", [(5, 4), (20, 6), (61, 3)])
+def test_warp_factor_matches_oracle_chol(gpu_lib, nx, nz):
+    """The one-warp-per-system complex64 factor (window in registers) against
+    the oracle's chol rows and, through refinement, the complex128 forward:
+    fewer nodes than the window (36), a node count that is not a multiple of
+    the 8-column block (147), and the widest band it takes (mb = 63)."""
+    from titatest_gb300 import MIXED, PLAIN, CRMod
+    g, sv, sig = _strip_case(nx, nz, ne=min(nx + 1, 8))
+    assert g.mb == nx + 2 and g.mb <= 63
+    P = O.Problem(g, sv)
+    kwn, kwnwi = P.rwaven()
+    with CRMod(g, sv, kwn, kwnwi, precision=MIXED, band_order=0) as m:
+        m.set_tune(4)
+        assert m.tune()["factor"] == "SIMT warp per system"
+        for k, l in [(1, 1), (len(kwn), sv.eanz)]:
+            a_ref, fak_ref = P.factor(sig, kwn, k, l)
+            a, fak = m.factor_system(sig, k, l)
+            np.testing.assert_allclose(fak, fak_ref, rtol=1e-14)
+            for i in range(g.sanz):
+                lo = max(0, g.mb - i)
+                assert relerr(a[i, lo:], a_ref[i, lo:]) < 1e-3, (k, l, i)
+        m.set_refinement(10, 1e-10)
+        om = m.forward(sig, kpot=True)
+    with CRMod(g, sv, kwn, kwnwi, precision=PLAIN) as m:
+        op = m.forward(sig, kpot=True)
+    assert relerr(om["kpot"], op["kpot"]) < MIXED_VOLT_TOL
+    assert relerr(om["volt"], op["volt"]) < MIXED_VOLT_TOL
 
 
 def test_wide_band_mixed_factor_shared_memory_window(gpu_lib):

@@ -29,7 +29,7 @@ EXPORTS = (
     "crgpu_set_memory_budget", "crgpu_forward", "crgpu_forward_device", "crgpu_sens",
     "crgpu_sens_device", "crgpu_device_buffers", "crgpu_factor_system", "crgpu_update",
     "crgpu_rwaven", "crgpu_cutmck", "crgpu_bkfak", "crgpu_get_stats", "crgpu_factor_system_noalloc",
-    "crgpu_adjoint", "crgpu_adjoint_device", "crgpu_autotune", "crgpu_get_tune", "crgpu_forward_sens_graph",
+    "crgpu_adjoint", "crgpu_adjoint_device", "crgpu_autotune", "crgpu_get_tune", "crgpu_set_tune", "crgpu_forward_sens_graph",
     "crgpu_set_boundary_values", "crgpu_update_fpi", "crgpu_blam0_jtj", "crgpu_set_dc", "crgpu_update_dc",
     "crgpu_mcm", "crgpu_column_sums", "crgpu_device_memory", "crgpu_create2", "crgpu_node_order",
     "crgpu_forward_sens_batch", "crgpu_memory_need",

@@ -67,9 +67,10 @@ class CRMod:
 
     precision: PLAIN (complex128, the reference arithmetic) or MIXED (complex64
     factorisation with FP64 iterative refinement).
-    band_order: 1 (default) lets a MIXED context whose band is too wide for
-    the tensor-core window factor in the geometric node order when that band
-    fits (crgpu_create2); 0 keeps the grid's band.
+    band_order: 1 (default) lets a MIXED context factor in the geometric node
+    order when that band is narrower (crgpu_create2); 2 lets any context
+    factor in that order whenever its band is narrower; 0 keeps the grid's
+    band.
     """
 
     def __init__(self, grid: formats.Grid, survey: formats.Survey, kwn=None, kwnwi=None,
@@ -317,9 +318,17 @@ class CRMod:
     def tune(self) -> dict:
         out = np.zeros(3, np.int32)
         _check(self._h, lib().crgpu_get_tune(self._h, out.ctypes.data_as(i32p)))
-        names = {0: "default", 1: "tensor cores", 2: "SIMT register tiles", 3: "SIMT shared-memory tiles"}
+        names = {0: "default", 1: "tensor cores", 2: "SIMT register tiles", 3: "SIMT shared-memory tiles",
+                 4: "SIMT warp per system"}
         return {"factor": names[int(out[0])], "factor_blocks_per_sm": int(out[1]),
                 "jacobian": {0: "default", 1: "tensor cores", 2: "SIMT"}[int(out[2])]}
+
+    def set_tune(self, factor: int = 0, blocks_per_sm: int = 0, jacobian: int = 0):
+        """crgpu_set_tune: factor 0 default, 1 tensor cores, 2 SIMT register
+        tiles, 3 SIMT shared-memory tiles, 4 one warp per system (mb <= 63);
+        jacobian 0 default, 1 tensor cores, 2 SIMT."""
+        a = np.array([factor, blocks_per_sm, jacobian], np.int32)
+        _check(self._h, lib().crgpu_set_tune(self._h, a.ctypes.data_as(i32p)))
 
     def stats(self) -> dict:
         s = CStats()

@@ -321,7 +321,7 @@ int run_factor(crgpu_ctx *c, int ns, int fuse) { return run_factor_view(c, batch
 // (two resident blocks per SM): they are factored and solved on the high
 // priority stream while the full rounds' systems are solved.  0: no split.
 int tail_systems(const crgpu_ctx *c, int ns) {
-    if (c->precision != CRGPU_MIXED || c->hg.mb + 4 > 128 || c->nsm <= 0) return 0;
+    if (c->precision != CRGPU_MIXED || mixed_factor_kind(c->P) != 1 || c->nsm <= 0) return 0;
     const int round = 2 * c->nsm, tail = ns % round;
     return (ns > round && tail > 0 && tail <= round / 2) ? tail : 0;
 }
@@ -579,16 +579,21 @@ int crgpu_create2(const crgpu_grid *grid, const crgpu_survey *sv, int32_t precis
         e = ERR_ARG;
         c->last_error = "precision";
     }
-    if (!e && (band_order < 0 || band_order > 1)) {
+    if (!e && (band_order < 0 || band_order > 2)) {
         e = ERR_ARG;
         c->last_error = "band_order";
     }
-    // complex64 factor of a band too wide for the tensor-core window: factor
-    // in the geometric node order when its band fits (the results are mapped
-    // back to the grid's node order at the boundary)
-    if (!e && band_order == 1 && precision == CRGPU_MIXED && c->hg.mb + 4 > 128) {
+    // band_order 1: a complex64 context factors in the geometric node order
+    // when that band is narrower (a narrower band is fewer factor flops and
+    // fewer bytes for every sweep; a band too wide for the tensor-core window
+    // only when the geometric band fits it); 2: either precision, whenever
+    // narrower.  The results are mapped back to the grid's node order at the
+    // boundary.
+    const bool mixed = precision == CRGPU_MIXED;
+    if (!e && (band_order == 2 || (band_order == 1 && mixed))) {
         const int mb2 = host_geometric_order(c->hg, c->old_of_new, c->new_of_old);
-        if (mb2 + 4 <= 128 && mb2 < c->hg.mb) {
+        const bool fits = band_order == 2 || c->hg.mb + 4 <= 128 || mb2 + 4 <= 128;
+        if (fits && mb2 < c->hg.mb) {
             host_permute_grid(c->hg, c->old_of_new, c->new_of_old, mb2);
         } else {
             c->old_of_new.clear();
@@ -1364,6 +1369,7 @@ int crgpu_autotune(crgpu_ctx *c, const double *sigma, int32_t flags) {
     DevBatch B = batch_view(c, ns);
     launch_rhs(P, B, c->nrhs, c->lsink, c->nsink, c->st);
     std::vector<std::array<int, 2>> cand;
+    if (P.mb + 1 <= 64 && P.rw <= 32) cand.push_back({4, 0});
     if (P.mb + 4 <= 128) cand.push_back({1, 0});
     if (mixed_window_supported(P.mb + 1) <= 176 && mixed_window_supported(P.mb + 1) > 0)
         for (int k : {1, 2, 4}) cand.push_back({2, k});
@@ -1411,6 +1417,15 @@ int crgpu_autotune(crgpu_ctx *c, const double *sigma, int32_t flags) {
     if (e) return e;
     std::lock_guard<std::mutex> g(g_tune_mu);
     g_tune[key] = {P.tune_factor, P.tune_ctas, P.tune_sens};
+    return 0;
+}
+
+int crgpu_set_tune(crgpu_ctx *c, const int32_t *in) {
+    if (!c || !in || in[0] < 0 || in[0] > 4 || in[1] < 0 || in[1] > 8 || in[2] < 0 || in[2] > 2) return ERR_ARG;
+    drop_graph(c);
+    c->P.tune_factor = in[0];
+    c->P.tune_ctas = in[1];
+    c->P.tune_sens = in[2];
     return 0;
 }
 

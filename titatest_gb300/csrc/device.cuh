@@ -14,7 +14,8 @@ struct DevProblem {
     int lsr;              // singularity removal
     int ldc;              // DC (src/kompadc.f90 ... src/bsendc.f90): Re(sigma), pivots > 0 (src/choldc.f90)
     // launch choices of the autotuner (0: the built-in default)
-    int tune_factor;      // mixed factor: 1 tensor cores, 2 SIMT register tiles, 3 SIMT shared-memory tiles
+    int tune_factor;      // mixed factor: 1 tensor cores, 2 SIMT register tiles, 3 SIMT shared-memory tiles,
+                          // 4 one warp per system (mb <= 63)
     int tune_ctas;        // SIMT factor: blocks per SM
     int tune_sens;        // mixed CRMod Jacobian: 1 tensor cores (Gram form), 2 SIMT (direct form)
     double sytop;

@@ -176,7 +176,7 @@ __device__ __forceinline__ void factor_diag4(float2 (&w)[4][4], int j0, int n, f
 }
 
 template <int WP>
-__global__ __launch_bounds__(MixCfg<WP>::NT, 1) void k_factor_mixed(DevProblem P, DevBatch B, int fuse) {
+__global__ __launch_bounds__(MixCfg<WP>::NT, (WP <= 64 ? 4 : 1)) void k_factor_mixed(DevProblem P, DevBatch B, int fuse) {
     constexpr int NB = MixCfg<WP>::NB, T = MixCfg<WP>::T;
     constexpr int D = kStageSteps;
     const int n = P.n, mb = P.mb, Wb = mb + 1, rw = P.rw;
@@ -415,16 +415,24 @@ int mixed_window_supported(int W) {
     return mixed_smem_window_supported(W);
 }
 
-// Kernel by P.tune_factor (0: tensor cores when the band fits their window,
-// else the smallest SIMT window), blocks per SM of the SIMT kernels by
-// P.tune_ctas (0: one).
+// Kernel by P.tune_factor (0: one warp per system when mb <= 63, else tensor
+// cores when the band fits their window, else the smallest SIMT window),
+// blocks per SM of the SIMT tile kernels by P.tune_ctas (0: one).
+int mixed_factor_kind(const DevProblem &P) {
+    const int W = P.mb + 1;
+    int kind = P.tune_factor;
+    if (kind == 4 && (W > 64 || P.rw > 32)) kind = 0;
+    if (kind == 1 && P.mb + 4 > 128) kind = 0;
+    if (kind == 2 && mixed_window_supported(W) > 176) kind = 0;
+    if (kind == 0) kind = (W <= 64 && P.rw <= 32) ? 4 : P.mb + 4 <= 128 ? 1 : (mixed_window_supported(W) <= 176 ? 2 : 3);
+    return kind;
+}
+
 int launch_factor_mixed(const DevProblem &P, const DevBatch &B, int fuse, int nsm, bool exclusive,
                         cudaStream_t st) {
     const int W = P.mb + 1;
-    int kind = P.tune_factor;
-    if (kind == 1 && P.mb + 4 > 128) kind = 0;
-    if (kind == 2 && mixed_window_supported(W) > 176) kind = 0;
-    if (kind == 0) kind = P.mb + 4 <= 128 ? 1 : (mixed_window_supported(W) <= 176 ? 2 : 3);
+    const int kind = mixed_factor_kind(P);
+    if (kind == 4) return launch_factor_warp(P, B, fuse, st) ? 0 : ERR_UNSUPPORTED;
     if (kind == 1) return launch_factor_tc(P, B, fuse, nsm, st, exclusive);
     const int per_sm = P.tune_ctas > 0 ? P.tune_ctas : 1;
     if (kind == 3) return launch_factor_mixed_smem(P, B, fuse, nsm * per_sm, st);

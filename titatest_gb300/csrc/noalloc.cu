@@ -51,6 +51,8 @@ extern "C" int crgpu_factor_system_noalloc(crgpu_ctx *c, const void *sigma_devic
     if (k < 1 || k > c->K || l < 1 || l > c->eanz) return fail(c, ERR_ARG, "system (k, l) out of range");
     if (c->precision != CRGPU_PLAIN) return fail(c, ERR_UNSUPPORTED, "no-alloc factor: plain precision only");
     if (c->P.ldc) return fail(c, ERR_UNSUPPORTED, "no-alloc factor: not available in DC mode");
+    if (!c->old_of_new.empty())
+        return fail(c, ERR_UNSUPPORTED, "no-alloc factor: the context factors in the geometric node order");
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev != c->device || dev >= kMaxDevices)
         return fail(c, ERR_ARG, "no-alloc factor: the context's device must be current");
