@@ -223,13 +223,18 @@ __device__ __forceinline__ void tile_update(float2 (&R)[8][8], const WarpTile &t
         default: CALL(7); break;    \
     }
 
-// one column: pivot slot p = 8P+pp, column j, buffer pb.  pp selects the
+// One column: pivot slot p = 8P+pp, column j, buffer pb.  pp selects the
 // register positions of publish/enter through a switch; the rest of the
 // column (the bulk of the instructions) is shared by the eight positions.
+// The scalar chain of the pivot (reciprocal, scaled copy) sits between the
+// two __syncwarp; the L entries, the right-hand side and the staging follow
+// the tile update, branch-free, so that they interleave with its
+// multiply-adds.
+template <int FUSE>
 __device__ __forceinline__ void warp_column(float2 (&R)[8][8], float2 &d0, float2 &d1, float2 &b0, float2 &b1,
                                             const WarpTile &t, const WarpPred &w, WarpSmem &S, const DevProblem &P,
                                             const double2 *as, const double2 *bv, float2 *L, float2 *yv, int j,
-                                            int p, int pp, int lane, int fuse, int &bad) {
+                                            int p, int pp, int lane, int &bad) {
     const int n = P.n, mb = P.mb, Wb = mb + 1;
     const int pb = j & 1;
     float2 *pc = S.pcol[pb];
@@ -242,28 +247,38 @@ __device__ __forceinline__ void warp_column(float2 (&R)[8][8], float2 &d0, float
     // the raw row scattered below (committed kRaw - 1 groups ago) has landed
     cp_wait<kRaw - 1>();
     __syncwarp();
-    // ---- 2. pivot, scaled copy, L entries, right-hand side; the dense slot of
+    // ---- 2. pivot, reciprocal, scaled copy, square root; the dense slot of
     //      row j+63 (entered at column j-1) is cleared for row j+63+kDense
     const float2 app = pc[pad(p)];
     const float r2 = app.x * app.x + app.y * app.y;
-    if (!(r2 > 0.f) || !isfinite(r2) || (P.ldc && !(app.x > 0.f))) bad = 28;  // src/chol.f90:67-71, choldc.f90:66-70
+    bad |= (!(r2 > 0.f) || !(r2 < INFINITY) || (P.ldc && !(app.x > 0.f))) ? 28 : 0;  // src/chol.f90:67-71, choldc.f90:66-70
     const float ir2 = __fdividef(1.f, r2);
     const float2 inv = cf(app.x * ir2, -app.y * ir2);
     const float2 pc0 = pc[pad(lane)], pc1 = pc[pad(lane + 32)];
     const float2 ps0 = cmulf(pc0, inv), ps1 = cmulf(pc1, inv);
     ps[pad(lane)] = ps0;
     ps[pad(lane + 32)] = ps1;
+    const int qd = (j + kWW - 1) & (kDense - 1);  // dense slot of rows j+63 and j+63+kDense
+    *reinterpret_cast<float4 *>(&S.dense[qd][pad(2 * lane)]) = make_float4(0.f, 0.f, 0.f, 0.f);
+    d0 = cfmsf(d0, pc0, ps0);
+    d1 = cfmsf(d1, pc1, ps1);
     const float2 sq = csqrt_fast(app);
     const float2 isq = cmulf(sq, inv);  // 1/sqrt(a_pp) = sqrt(a_pp)/a_pp
+    __syncwarp();
+    // ---- 3. rank-1 update of the tile; in the same basic block (branch-free)
+    //      the L entries of column j (Cholesky form, as src/chol.f90 stores
+    //      them), the fused forward substitution and the staging of row
+    //      j+63+kDense from its raw pattern row into dense slot qd, then the
+    //      raw row kRaw further ahead into the freed raw slot
+    tile_update(R, t, pc, ps);
     const float2 l0 = cmulf(pc0, isq), l1 = cmulf(pc1, isq);
     {
         const int dd0 = (lane - p) & (kWW - 1), dd1 = (lane + 32 - p) & (kWW - 1);
-        if (dd0 == 0) L[(size_t)j * Wb + mb] = sq;
-        else if (dd0 <= mb && j + dd0 < n) L[(size_t)(j + dd0) * Wb + (mb - dd0)] = l0;
-        if (dd1 == 0) L[(size_t)j * Wb + mb] = sq;
-        else if (dd1 <= mb && j + dd1 < n) L[(size_t)(j + dd1) * Wb + (mb - dd1)] = l1;
+        if (dd0 == 0 || dd1 == 0) L[(size_t)j * Wb + mb] = sq;
+        if (dd0 != 0 && dd0 <= mb && j + dd0 < n) L[(size_t)(j + dd0) * Wb + (mb - dd0)] = l0;
+        if (dd1 != 0 && dd1 <= mb && j + dd1 < n) L[(size_t)(j + dd1) * Wb + (mb - dd1)] = l1;
     }
-    if (fuse) {
+    if (FUSE) {
         const float2 bsel = (p >> 5) ? b1 : b0;
         const float2 bp = cf(__shfl_sync(0xffffffffu, bsel.x, p & 31), __shfl_sync(0xffffffffu, bsel.y, p & 31));
         const float2 yj = cmulf(bp, isq);
@@ -271,13 +286,14 @@ __device__ __forceinline__ void warp_column(float2 (&R)[8][8], float2 &d0, float
         b0 = cfmsf(b0, l0, yj);
         b1 = cfmsf(b1, l1, yj);
     }
-    const int qd = (j + kWW - 1) & (kDense - 1);  // dense slot of rows j+63 and j+63+kDense
-    *reinterpret_cast<float4 *>(&S.dense[qd][pad(2 * lane)]) = make_float4(0.f, 0.f, 0.f, 0.f);
-    __syncwarp();
-    // ---- 3. rank-1 update of the tile and the diagonal
-    tile_update(R, t, pc, ps);
-    d0 = cfmsf(d0, pc0, ps0);
-    d1 = cfmsf(d1, pc1, ps1);
+    {
+        const int r = j + kWW - 1 + kDense, q = r & (kRaw - 1);
+        const bool live = r < n && lane < P.rw;
+        const int c = live ? S.raw_col[q][lane] : -1;
+        if (c >= 0) S.dense[qd][pad(c & (kWW - 1))] = to_f(S.raw_val[q][lane]);
+        if (lane == 31) S.dense_b[qd] = (FUSE && r < n) ? to_f(S.raw_b[q]) : cf(0.f, 0.f);
+        raw_issue(P, as, bv, r + kRaw, FUSE, S, lane);
+    }
     // ---- 4. row j+64 enters slot p
     {
         const int qe = j & (kDense - 1);
@@ -285,32 +301,15 @@ __device__ __forceinline__ void warp_column(float2 (&R)[8][8], float2 &d0, float
 #define CRGPU_ENT(K) enter<K>(R, t, w, nr)
         CRGPU_PP_SWITCH(pp, CRGPU_ENT)
 #undef CRGPU_ENT
-        if (lane == (p & 31)) {
-            const float2 nd = nr[pad(p)];
+        const float2 nd = nr[pad(p)];
+        const bool own = lane == (p & 31), hi = p >> 5;
+        d0 = (own && !hi) ? nd : d0;
+        d1 = (own && hi) ? nd : d1;
+        if (FUSE) {
             const float2 nbv = S.dense_b[qe];
-            if (p >> 5) {
-                d1 = nd;
-                b1 = nbv;
-            } else {
-                d0 = nd;
-                b0 = nbv;
-            }
+            b0 = (own && !hi) ? nbv : b0;
+            b1 = (own && hi) ? nbv : b1;
         }
-    }
-    // ---- staging: row j+63+kDense from its raw pattern row into dense slot qd,
-    //      then the raw row kRaw further ahead into the freed raw slot
-    {
-        const int r = j + kWW - 1 + kDense, q = r & (kRaw - 1);
-        if (r < n) {
-            if (lane < P.rw) {
-                const int c = S.raw_col[q][lane];
-                if (c >= 0) S.dense[qd][pad(c & (kWW - 1))] = to_f(S.raw_val[q][lane]);
-            }
-            if (lane == 31) S.dense_b[qd] = fuse ? to_f(S.raw_b[q]) : cf(0.f, 0.f);
-        } else if (lane == 31) {
-            S.dense_b[qd] = cf(0.f, 0.f);
-        }
-        raw_issue(P, as, bv, r + kRaw, fuse, S, lane);
     }
 }
 
@@ -331,7 +330,9 @@ __device__ __forceinline__ void warp_enter_initial(float2 (&R)[8][8], float2 &d0
     __syncwarp();
 }
 
-__global__ __launch_bounds__(32, 12) void k_factor_warp(DevProblem P, DevBatch B, int fuse) {
+template <int FUSE>
+__global__ __launch_bounds__(32, 12) void k_factor_warp(DevProblem P, DevBatch B) {
+    constexpr int fuse = FUSE;
     __shared__ WarpSmem S;
     const int lane = threadIdx.x;
     const int s = blockIdx.x;
@@ -379,7 +380,7 @@ __global__ __launch_bounds__(32, 12) void k_factor_warp(DevProblem P, DevBatch B
         const int j0 = 8 * J8;
 #pragma unroll 1
         for (int pp = 0; pp < 8 && j0 + pp < n; pp++)
-            warp_column(R, d0, d1, b0, b1, t, w, S, P, as, bv, L, yv, j0 + pp, 8 * P8 + pp, pp, lane, fuse, bad);
+            warp_column<FUSE>(R, d0, d1, b0, b1, t, w, S, P, as, bv, L, yv, j0 + pp, 8 * P8 + pp, pp, lane, bad);
     }
     cp_wait<0>();
     bad = __reduce_or_sync(0xffffffffu, bad);
@@ -391,7 +392,10 @@ __global__ __launch_bounds__(32, 12) void k_factor_warp(DevProblem P, DevBatch B
 bool launch_factor_warp(const DevProblem &P, const DevBatch &B, int fuse, cudaStream_t st) {
     if (P.mb + 1 > kWW || P.rw > kRawCap || P.rw > 32) return false;
     if (B.nsys <= 0) return true;
-    k_factor_warp<<<B.nsys, 32, 0, st>>>(P, B, fuse);
+    if (fuse)
+        k_factor_warp<1><<<B.nsys, 32, 0, st>>>(P, B);
+    else
+        k_factor_warp<0><<<B.nsys, 32, 0, st>>>(P, B);
     return true;
 }
 
