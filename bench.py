@@ -642,7 +642,8 @@ def run_case(args):
         if args.batch:
             g = s.grid
             esz = 8 if prec == MIXED else 16
-            per = g.sanz * (g.mb + 1) * esz + (g.sanz * 12 * 16) + g.sanz * 8 + g.sanz * (3 * 16 + esz) + 64
+            mbf = factored_band(m, g)
+            per = g.sanz * (mbf + 1) * esz + (g.sanz * 12 * 16) + g.sanz * 8 + g.sanz * (3 * 16 + esz) + 64
             m.set_memory_budget(int(per * args.batch + per // 2))
         for _ in range(args.repeat):
             t = time.time()
