@@ -226,12 +226,13 @@ def _strip_case(nx, nz, ne, seed=23):
     return grid, survey, synth._sigma_from(mag, pha)
 
 
-@pytest.mark.parametrize("nx,nz", [(5, 4), (20, 6), (61, 3)])
+@pytest.mark.parametrize("nx,nz", [(5, 4), (20, 6), (60, 2), (61, 3)])
 def test_warp_factor_matches_oracle_chol(gpu_lib, nx, nz):
     """The one-warp-per-system complex64 factor (window in registers) against
     the oracle's chol rows and, through refinement, the complex128 forward:
-    fewer nodes than the window (36), a node count that is not a multiple of
-    the 8-column block (147), and the widest band it takes (mb = 63)."""
+    fewer nodes than the window (30), odd node counts that are not a multiple
+    of the 8-column block (147, 183), the widest band of the two-column step
+    (mb = 62) and the widest band of the kernel (mb = 63, one column a step)."""
     from titatest_gb300 import MIXED, PLAIN, CRMod
     g, sv, sig = _strip_case(nx, nz, ne=min(nx + 1, 8))
     assert g.mb == nx + 2 and g.mb <= 63
