@@ -432,7 +432,7 @@ int launch_factor_mixed(const DevProblem &P, const DevBatch &B, int fuse, int ns
                         cudaStream_t st) {
     const int W = P.mb + 1;
     const int kind = mixed_factor_kind(P);
-    if (kind == 4) return launch_factor_warp(P, B, fuse, st) ? 0 : ERR_UNSUPPORTED;
+    if (kind == 4) return launch_factor_warp(P, B, fuse, nsm, st) ? 0 : ERR_UNSUPPORTED;
     if (kind == 1) return launch_factor_tc(P, B, fuse, nsm, st, exclusive);
     const int per_sm = P.tune_ctas > 0 ? P.tune_ctas : 1;
     if (kind == 3) return launch_factor_mixed_smem(P, B, fuse, nsm * per_sm, st);

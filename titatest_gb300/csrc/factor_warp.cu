@@ -26,8 +26,9 @@
 //   4. the row j+64 enters slot p: the positions of slot p take its values
 //      from a dense row staged two-level ahead (cp.async of the sparse
 //      pattern row, then expanded by slot).
-// Two __syncwarp per column, no block barrier; a block is one warp, so nine
-// systems share an SM (206 registers a thread) and their columns interleave.
+// Two __syncwarp per column, no block barrier; a block is one warp.  Two
+// register budgets: 168 registers (12 systems an SM resident) for launches of
+// more than 8 systems an SM, else ~250 (8 an SM, each column ~1.3x faster).
 #include "async.cuh"
 #include "crgpu_internal.h"
 #include "device.cuh"
@@ -330,8 +331,12 @@ __device__ __forceinline__ void warp_enter_initial(float2 (&R)[8][8], float2 &d0
     __syncwarp();
 }
 
-template <int FUSE>
-__global__ __launch_bounds__(32, 12) void k_factor_warp(DevProblem P, DevBatch B) {
+// MINB: warps an SM the register budget is sized for.  12 (168 registers)
+// keeps up to 12 systems an SM resident; 8 leaves the compiler ~206
+// registers, which makes one system's column ~1.5x faster, for launches of
+// at most 8 systems an SM.
+template <int FUSE, int MINB>
+__global__ __launch_bounds__(32, MINB) void k_factor_warp(DevProblem P, DevBatch B) {
     constexpr int fuse = FUSE;
     __shared__ WarpSmem S;
     const int lane = threadIdx.x;
@@ -389,13 +394,14 @@ __global__ __launch_bounds__(32, 12) void k_factor_warp(DevProblem P, DevBatch B
 
 }  // namespace
 
-bool launch_factor_warp(const DevProblem &P, const DevBatch &B, int fuse, cudaStream_t st) {
+bool launch_factor_warp(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st) {
     if (P.mb + 1 > kWW || P.rw > kRawCap || P.rw > 32) return false;
     if (B.nsys <= 0) return true;
-    if (fuse)
-        k_factor_warp<1><<<B.nsys, 32, 0, st>>>(P, B);
+    const bool few = B.nsys <= 8 * nsm;
+    if (few)
+        fuse ? k_factor_warp<1, 8><<<B.nsys, 32, 0, st>>>(P, B) : k_factor_warp<0, 8><<<B.nsys, 32, 0, st>>>(P, B);
     else
-        k_factor_warp<0><<<B.nsys, 32, 0, st>>>(P, B);
+        fuse ? k_factor_warp<1, 12><<<B.nsys, 32, 0, st>>>(P, B) : k_factor_warp<0, 12><<<B.nsys, 32, 0, st>>>(P, B);
     return true;
 }
 

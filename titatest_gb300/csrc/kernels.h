@@ -31,7 +31,7 @@ void launch_factor_plain(const DevProblem &P, const DevBatch &B, int fuse, int n
 // complex128 factor with the window in registers (factor_plain.cu); false
 // when the band is too wide for it
 bool launch_factor_plain_reg(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st);
-bool launch_factor_warp(const DevProblem &P, const DevBatch &B, int fuse, cudaStream_t st);
+bool launch_factor_warp(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st);
 // the complex64 factor kernel launch_factor_mixed runs (the values of tune_factor)
 int mixed_factor_kind(const DevProblem &P);
 // the tensor-core factors of several problems' batches in one persistent
