@@ -60,8 +60,9 @@ struct WarpSmem {
 };
 
 // row r's lower pattern into dense slot sl (zeros elsewhere), plain loads
+template <class SM>
 __device__ __forceinline__ void load_dense_row(const DevProblem &P, const double2 *as, const double2 *bv, int r,
-                                               int fuse, WarpSmem &S, int sl, int lane) {
+                                               int fuse, SM &S, int sl, int lane) {
     S.dense[sl][pad(lane)] = cf(0.f, 0.f);
     S.dense[sl][pad(lane + 32)] = cf(0.f, 0.f);
     __syncwarp();
@@ -75,8 +76,9 @@ __device__ __forceinline__ void load_dense_row(const DevProblem &P, const double
     __syncwarp();
 }
 
+template <class SM>
 __device__ __forceinline__ void raw_issue(const DevProblem &P, const double2 *as, const double2 *bv, int r, int fuse,
-                                          WarpSmem &S, int lane) {
+                                          SM &S, int lane) {
     const int q = r & (kRaw - 1);
     if (r < P.n) {
         if (lane < P.rw) {
@@ -84,6 +86,24 @@ __device__ __forceinline__ void raw_issue(const DevProblem &P, const double2 *as
             cp_async4(&S.raw_col[q][lane], P.col + (size_t)r * P.rw + lane);
         }
         if (lane == 31 && fuse) cp_async16(&S.raw_b[q], bv + r);
+    }
+    cp_commit();
+}
+
+// the pattern rows r and r+1 into their raw slots, one commit group
+template <class SM>
+__device__ __forceinline__ void raw_issue2(const DevProblem &P, const double2 *as, const double2 *bv, int r,
+                                           int fuse, SM &S, int lane) {
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        const int rr = r + u, q = rr & (kRaw - 1);
+        if (rr < P.n) {
+            if (lane < P.rw) {
+                cp_async16(&S.raw_val[q][lane], as + (size_t)rr * P.rw + lane);
+                cp_async4(&S.raw_col[q][lane], P.col + (size_t)rr * P.rw + lane);
+            }
+            if (lane == 31 && fuse) cp_async16(&S.raw_b[q], bv + rr);
+        }
     }
     cp_commit();
 }
@@ -314,9 +334,9 @@ __device__ __forceinline__ void warp_column(float2 (&R)[8][8], float2 &d0, float
     }
 }
 
-template <int PP>
+template <int PP, class SM>
 __device__ __forceinline__ void warp_enter_initial(float2 (&R)[8][8], float2 &d0, float2 &d1, float2 &b0,
-                                                   float2 &b1, const WarpTile &t, const WarpPred &w, WarpSmem &S,
+                                                   float2 &b1, const WarpTile &t, const WarpPred &w, SM &S,
                                                    int p, int lane) {
     enter<PP>(R, t, w, S.dense[0]);
     if (lane == (p & 31)) {
@@ -392,16 +412,222 @@ __global__ __launch_bounds__(32, MINB) void k_factor_warp(DevProblem P, DevBatch
     if (lane == 0 && bad) atomicCAS(&B.status[s], 0, bad);
 }
 
+// ---------------------------------------------------------------------------
+// Two columns a step (mb <= 62).  The pivot slots p1 = 8P+2h, p2 = p1+1 lie in
+// one block; their columns are published together, the 2x2 pivot block is
+// factored (L D L^T) in every lane, and the tile takes the two rank-1 updates
+// back to back.  The rows j+64 and j+65 then enter slots p1 and p2: with
+// mb <= 62 neither has an entry in column j+1 (63 or more columns before it),
+// so no entering row misses an update of the step.
+// ---------------------------------------------------------------------------
+struct WarpSmem2 {
+    __align__(16) float2 pcol[2][2][kPad];  // [step parity][column of the step] by padded slot; the second
+                                            // column after the first's elimination
+    __align__(16) float2 pcs[2][2][kPad];   // scaled: pcol / d
+    __align__(16) float2 dense[kDense][kPad];
+    float2 dense_b[kDense];
+    __align__(16) double2 raw_val[kRaw][kRawCap];
+    int raw_col[kRaw][kRawCap];
+    __align__(16) double2 raw_b[kRaw];
+};
+
+#define CRGPU_H_SWITCH(h, CALL) \
+    switch (h) {                  \
+        case 0: CALL(0); break;   \
+        case 1: CALL(2); break;   \
+        case 2: CALL(4); break;   \
+        default: CALL(6); break;  \
+    }
+
+template <int FUSE>
+__device__ __forceinline__ void warp_step2(float2 (&R)[8][8], float2 &d0, float2 &d1, float2 &b0, float2 &b1,
+                                           const WarpTile &t, const WarpPred &w, WarpSmem2 &S, const DevProblem &P,
+                                           const double2 *as, const double2 *bv, float2 *L, float2 *yv, int j,
+                                           int p1, int h, int lane, int &bad) {
+    const int n = P.n, mb = P.mb, Wb = mb + 1;
+    const int p2 = p1 + 1, pb = (j >> 1) & 1;
+    const bool two = j + 1 < n;  // the second column exists
+    float2 *pc1 = S.pcol[pb][0], *pc2 = S.pcol[pb][1];
+    float2 *ps1 = S.pcs[pb][0], *ps2 = S.pcs[pb][1];
+    // ---- 1. publish both pivot columns
+#define CRGPU_PUB2(K)                 \
+    publish<K>(R, t, w, pc1);         \
+    publish<K + 1>(R, t, w, pc2);
+    CRGPU_H_SWITCH(h, CRGPU_PUB2)
+#undef CRGPU_PUB2
+    {
+        const bool own1 = lane == (p1 & 31), own2 = lane == (p2 & 31);
+        if (own1) pc1[pad(p1)] = (p1 >> 5) ? d1 : d0;
+        if (own2) pc2[pad(p2)] = (p2 >> 5) ? d1 : d0;
+    }
+    cp_wait<1>();  // the raw rows scattered below (committed one step before the last) have landed
+    __syncwarp();
+    // ---- 2. the 2x2 pivot block (L D L^T), the second column after the first's
+    //      elimination, the scaled copies, the diagonal, the square roots
+    const float2 a11 = pc1[pad(p1)], a21 = pc1[pad(p2)], a22 = pc2[pad(p2)];
+    const float r1 = a11.x * a11.x + a11.y * a11.y;
+    const float2 inv1 = cf(a11.x * __fdividef(1.f, r1), -a11.y * __fdividef(1.f, r1));
+    const float2 l21 = cmulf(a21, inv1);
+    const float2 dd2 = two ? cfmsf(a22, l21, a21) : cf(1.f, 0.f);
+    const float r2 = dd2.x * dd2.x + dd2.y * dd2.y;
+    const float2 inv2 = cf(dd2.x * __fdividef(1.f, r2), -dd2.y * __fdividef(1.f, r2));
+    bad |= (!(r1 > 0.f) || !(r1 < INFINITY) || (P.ldc && !(a11.x > 0.f))) ? 28 : 0;  // src/chol.f90:67-71, choldc.f90:66-70
+    bad |= (!(r2 > 0.f) || !(r2 < INFINITY) || (P.ldc && !(dd2.x > 0.f))) ? 28 : 0;
+    const float2 c10 = pc1[pad(lane)], c11 = pc1[pad(lane + 32)];
+    const float2 c20 = two ? cfmsf(pc2[pad(lane)], l21, c10) : cf(0.f, 0.f);
+    const float2 c21 = two ? cfmsf(pc2[pad(lane + 32)], l21, c11) : cf(0.f, 0.f);
+    const float2 s10 = cmulf(c10, inv1), s11 = cmulf(c11, inv1);
+    const float2 s20 = cmulf(c20, inv2), s21 = cmulf(c21, inv2);
+    __syncwarp();  // every lane has read pc2 before it takes the eliminated values
+    pc2[pad(lane)] = c20;
+    pc2[pad(lane + 32)] = c21;
+    ps1[pad(lane)] = s10;
+    ps1[pad(lane + 32)] = s11;
+    ps2[pad(lane)] = s20;
+    ps2[pad(lane + 32)] = s21;
+    d0 = cfmsf(cfmsf(d0, c10, s10), c20, s20);
+    d1 = cfmsf(cfmsf(d1, c11, s11), c21, s21);
+    const int qa = (j + kWW - 2) & (kDense - 1), qb = (j + kWW - 1) & (kDense - 1);  // slots of rows j+62, j+63
+    *reinterpret_cast<float4 *>(&S.dense[qa][pad(2 * lane)]) = make_float4(0.f, 0.f, 0.f, 0.f);
+    *reinterpret_cast<float4 *>(&S.dense[qb][pad(2 * lane)]) = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 sq1 = csqrt_fast(a11), isq1 = cmulf(sq1, inv1);
+    const float2 sq2 = csqrt_fast(dd2), isq2 = cmulf(sq2, inv2);
+    __syncwarp();
+    // ---- 3. the two rank-1 updates of the tile
+    tile_update(R, t, pc1, ps1);
+    if (two) tile_update(R, t, pc2, ps2);
+    // ---- the L entries of columns j and j+1 (Cholesky form) and the fused
+    //      forward substitution
+    {
+        const float2 l10 = cmulf(c10, isq1), l11 = cmulf(c11, isq1);
+        const float2 l20 = cmulf(c20, isq2), l21c = cmulf(c21, isq2);
+        const int e0 = (lane - p1) & (kWW - 1), e1 = (lane + 32 - p1) & (kWW - 1);  // row offsets from j
+        if (e0 == 0 || e1 == 0) L[(size_t)j * Wb + mb] = sq1;
+        if (e0 != 0 && e0 <= mb && j + e0 < n) L[(size_t)(j + e0) * Wb + (mb - e0)] = l10;
+        if (e1 != 0 && e1 <= mb && j + e1 < n) L[(size_t)(j + e1) * Wb + (mb - e1)] = l11;
+        if (two) {
+            if (e0 == 1 || e1 == 1) L[(size_t)(j + 1) * Wb + mb] = sq2;
+            if (e0 > 1 && e0 - 1 <= mb && j + e0 < n) L[(size_t)(j + e0) * Wb + (mb - e0 + 1)] = l20;
+            if (e1 > 1 && e1 - 1 <= mb && j + e1 < n) L[(size_t)(j + e1) * Wb + (mb - e1 + 1)] = l21c;
+        }
+        if (FUSE) {
+            const float2 bs1 = (p1 >> 5) ? b1 : b0;
+            const float2 bp1 = cf(__shfl_sync(0xffffffffu, bs1.x, p1 & 31), __shfl_sync(0xffffffffu, bs1.y, p1 & 31));
+            const float2 y1 = cmulf(bp1, isq1);
+            b0 = cfmsf(b0, l10, y1);
+            b1 = cfmsf(b1, l11, y1);
+            const float2 bs2 = (p2 >> 5) ? b1 : b0;
+            const float2 bp2 = cf(__shfl_sync(0xffffffffu, bs2.x, p2 & 31), __shfl_sync(0xffffffffu, bs2.y, p2 & 31));
+            const float2 y2 = cmulf(bp2, isq2);
+            if (lane == (p1 & 31)) yv[j] = y1;
+            if (two && lane == (p2 & 31)) yv[j + 1] = y2;
+            if (two) {
+                b0 = cfmsf(b0, l20, y2);
+                b1 = cfmsf(b1, l21c, y2);
+            }
+        }
+    }
+    // ---- staging: rows j+66, j+67 from their raw pattern rows into the dense
+    //      slots cleared above, then the raw rows four further ahead
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        const int r = j + kWW + 2 + u, q = r & (kRaw - 1), qd = r & (kDense - 1);
+        const bool live = r < n && lane < P.rw;
+        const int c = live ? S.raw_col[q][lane] : -1;
+        if (c >= 0) S.dense[qd][pad(c & (kWW - 1))] = to_f(S.raw_val[q][lane]);
+        if (lane == 31) S.dense_b[qd] = (FUSE && r < n) ? to_f(S.raw_b[q]) : cf(0.f, 0.f);
+    }
+    raw_issue2(P, as, bv, j + kWW + 6, FUSE, S, lane);
+    // ---- 4. rows j+64 and j+65 enter slots p1 and p2 (in this order: the pair
+    //      (p1, p2) takes its value from row j+65's pattern)
+    {
+        const float2 *na = S.dense[(j + kWW) & (kDense - 1)], *nb = S.dense[(j + kWW + 1) & (kDense - 1)];
+#define CRGPU_ENT2(K)              \
+    enter<K>(R, t, w, na);         \
+    enter<K + 1>(R, t, w, nb);
+        CRGPU_H_SWITCH(h, CRGPU_ENT2)
+#undef CRGPU_ENT2
+        const bool hi = p1 >> 5;  // p1, p2 lie in the same half
+        const bool own1 = lane == (p1 & 31), own2 = lane == (p2 & 31);
+        const float2 nd1 = na[pad(p1)], nd2 = nb[pad(p2)];
+        d0 = (own1 && !hi) ? nd1 : (own2 && !hi) ? nd2 : d0;
+        d1 = (own1 && hi) ? nd1 : (own2 && hi) ? nd2 : d1;
+        if (FUSE) {
+            const float2 nb1 = S.dense_b[(j + kWW) & (kDense - 1)], nb2 = S.dense_b[(j + kWW + 1) & (kDense - 1)];
+            b0 = (own1 && !hi) ? nb1 : (own2 && !hi) ? nb2 : b0;
+            b1 = (own1 && hi) ? nb1 : (own2 && hi) ? nb2 : b1;
+        }
+    }
+}
+
+template <int FUSE, int MINB>
+__global__ __launch_bounds__(32, MINB) void k_factor_warp2(DevProblem P, DevBatch B) {
+    constexpr int fuse = FUSE;
+    __shared__ WarpSmem2 S;
+    const int lane = threadIdx.x;
+    const int s = blockIdx.x;
+    if (s >= B.nsys) return;
+    const int n = P.n, mb = P.mb, Wb = mb + 1;
+    float2 *L = (float2 *)B.L + (size_t)s * B.lpitch;
+    float2 *yv = (float2 *)B.y + (size_t)s * n;
+    const double2 *as = B.As + (size_t)s * P.nnz;
+    const double2 *bv = B.b + (size_t)s * n;
+    const WarpTile t = warp_tile(lane);
+    int bad = 0;
+    for (int q = lane; q < mb * Wb; q += 32) {
+        const int r = q / Wb, o = q % Wb;
+        if (r < n && o < mb - r) L[(size_t)r * Wb + o] = cf(0.f, 0.f);
+    }
+    float2 R[8][8];
+#pragma unroll
+    for (int a = 0; a < 8; a++)
+#pragma unroll
+        for (int c = 0; c < 8; c++) R[a][c] = cf(0.f, 0.f);
+    float2 d0 = cf(0.f, 0.f), d1 = cf(0.f, 0.f), b0 = cf(0.f, 0.f), b1 = cf(0.f, 0.f);
+    for (int P8 = 0; P8 < 8; P8++) {
+        const WarpPred w = warp_pred(t, P8);
+#define CRGPU_ENTER0(PP)                                                          \
+    load_dense_row(P, as, bv, 8 * P8 + PP, fuse, S, 0, lane);                    \
+    warp_enter_initial<PP>(R, d0, d1, b0, b1, t, w, S, 8 * P8 + PP, lane);
+        CRGPU_ENTER0(0) CRGPU_ENTER0(1) CRGPU_ENTER0(2) CRGPU_ENTER0(3)
+        CRGPU_ENTER0(4) CRGPU_ENTER0(5) CRGPU_ENTER0(6) CRGPU_ENTER0(7)
+#undef CRGPU_ENTER0
+    }
+    // rows 64, 65 (step 0) as dense rows; 66..69 in flight, two per group
+    load_dense_row(P, as, bv, kWW, fuse, S, kWW & (kDense - 1), lane);
+    load_dense_row(P, as, bv, kWW + 1, fuse, S, (kWW + 1) & (kDense - 1), lane);
+    raw_issue2(P, as, bv, kWW + 2, fuse, S, lane);
+    raw_issue2(P, as, bv, kWW + 4, fuse, S, lane);
+    const int nstep = (n + 7) / 8;
+    for (int J8 = 0; J8 < nstep; J8++) {
+        const int P8 = J8 & 7;
+        const WarpPred w = warp_pred(t, P8);
+        const int j0 = 8 * J8;
+#pragma unroll 1
+        for (int h = 0; h < 4 && j0 + 2 * h < n; h++)
+            warp_step2<FUSE>(R, d0, d1, b0, b1, t, w, S, P, as, bv, L, yv, j0 + 2 * h, 8 * P8 + 2 * h, h, lane, bad);
+    }
+    cp_wait<0>();
+    bad = __reduce_or_sync(0xffffffffu, bad);
+    if (lane == 0 && bad) atomicCAS(&B.status[s], 0, bad);
+}
+
 }  // namespace
 
 bool launch_factor_warp(const DevProblem &P, const DevBatch &B, int fuse, int nsm, cudaStream_t st) {
     if (P.mb + 1 > kWW || P.rw > kRawCap || P.rw > 32) return false;
     if (B.nsys <= 0) return true;
     const bool few = B.nsys <= 8 * nsm;
-    if (few)
+    if (P.mb <= 62) {  // two columns a step
+        if (few)
+            fuse ? k_factor_warp2<1, 8><<<B.nsys, 32, 0, st>>>(P, B) : k_factor_warp2<0, 8><<<B.nsys, 32, 0, st>>>(P, B);
+        else
+            fuse ? k_factor_warp2<1, 12><<<B.nsys, 32, 0, st>>>(P, B) : k_factor_warp2<0, 12><<<B.nsys, 32, 0, st>>>(P, B);
+    } else if (few) {
         fuse ? k_factor_warp<1, 8><<<B.nsys, 32, 0, st>>>(P, B) : k_factor_warp<0, 8><<<B.nsys, 32, 0, st>>>(P, B);
-    else
+    } else {
         fuse ? k_factor_warp<1, 12><<<B.nsys, 32, 0, st>>>(P, B) : k_factor_warp<0, 12><<<B.nsys, 32, 0, st>>>(P, B);
+    }
     return true;
 }
 
