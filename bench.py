@@ -167,6 +167,9 @@ FACTOR_KERNELS = {"tensor cores": ("k_factor_tc", "tensor"), "SIMT warp per syst
 FACTOR_NOTES = {
     "k_factor_warp": "latency-bound band factor: a serial chain per column (pivot, reciprocal, rank-1 update of "
                      "the 64-slot window held in one warp's registers), one system per warp, 12 warps an SM",
+    "k_factor_warp2": "latency-bound band factor, two columns a step (2x2 pivot block, two rank-1 updates of the "
+                      "64-slot window held in one warp's registers), one system per warp, 8 warps an SM; the "
+                      "systems beyond 8 an SM are factored on the tensor cores beside the solves",
     "k_factor_tc": "latency-bound band factor: each 4-column step is a serial panel plus 4 tf32 MMAs (3 hi/lo "
                    "products + row injection) on a 128x128 complex window"}
 
@@ -428,11 +431,20 @@ def run_gpu(args):
     mb_mixed = factored_band(mixed, g)
     nsys = K * sv.eanz
     flops_factor = nsys * 4.0 * n * mb * mb  # the grid's band: the complex128 arm factors it
-    flops_mixed = nsys * 4.0 * n * mb_mixed * mb_mixed
+    kname, bound = FACTOR_KERNELS.get(tune["factor"], ("k_factor_tc", "tensor"))
+    nsys_main = nsys
+    if kname == "k_factor_warp":
+        # the library's split: up to 8 systems an SM in the timed factor launch,
+        # the excess (at most one an SM) on the tensor cores beside the solves
+        nsm = torch.cuda.get_device_properties(0).multi_processor_count
+        if 0 < nsys - 8 * nsm <= nsm:
+            nsys_main = 8 * nsm
+        if mb_mixed <= 62:
+            kname = "k_factor_warp2"
+    flops_mixed = nsys_main * 4.0 * n * mb_mixed * mb_mixed
     fp64_peak = fp64_dgemm_tflops(stream)
     fac_avg_ms = statistics.mean(fac_ms)
     achieved = flops_mixed / (fac_avg_ms * 1e-3) / 1e12
-    kname, bound = FACTOR_KERNELS.get(tune["factor"], ("k_factor_tc", "tensor"))
     if bound == "tensor":
         peak, peak_source = tensor_peak_tflops()
     else:
@@ -472,8 +484,9 @@ def run_gpu(args):
         "roofline": {"kernel": kname, "bound": bound, "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_source,
-                     "algorithmic": "4*n*mb^2 flops per band system (complex L L^T) at the factored band, all "
-                                    "systems of one forward",
+                     "algorithmic": "4*n*mb^2 flops per band system (complex L L^T) at the factored band, "
+                                    "the systems of the timed factor launch",
+                     "systems": nsys_main,
                      "note": FACTOR_NOTES.get(kname, "")},
     }
     kwn, kwnwi = mixed.kwn, mixed.kwnwi

@@ -304,9 +304,12 @@ int assemble_batch(crgpu_ctx *c, const double2 *d_sigma, int ns) {
 
 // band factorisation of the current batch (src/chol.f90); with fuse the
 // forward sweep of the right-hand sides in B.b runs inside the factor
-int run_factor_view(crgpu_ctx *c, const DevBatch &B, int fuse, cudaStream_t st, bool exclusive = false) {
+int run_factor_view(crgpu_ctx *c, const DevBatch &B, int fuse, cudaStream_t st, bool exclusive = false,
+                    int kind = 0) {
     if (c->precision == CRGPU_MIXED) {
-        int e = launch_factor_mixed(c->P, B, fuse, c->nsm, exclusive, st);
+        DevProblem P = c->P;
+        if (kind) P.tune_factor = kind;
+        int e = launch_factor_mixed(P, B, fuse, c->nsm, exclusive, st);
         if (e) return fail(c, e, "mixed precision: band width beyond the supported window");
     } else {
         launch_factor_plain(c->P, B, fuse, c->nsm, st);
@@ -317,13 +320,24 @@ int run_factor_view(crgpu_ctx *c, const DevBatch &B, int fuse, cudaStream_t st, 
 
 int run_factor(crgpu_ctx *c, int ns, int fuse) { return run_factor_view(c, batch_view(c, ns), fuse, c->st); }
 
-// systems of a batch beyond the last full round of the tensor-core factor
-// (two resident blocks per SM): they are factored and solved on the high
-// priority stream while the full rounds' systems are solved.  0: no split.
+// systems of a batch beyond the last full round of the factor: they are
+// factored and solved on the high priority stream while the full rounds'
+// systems are solved.  0: no split.  Tensor cores: rounds of two blocks per
+// SM.  One warp per system: up to 8 systems an SM take the faster register
+// budget in one wave, so a batch at most one system an SM beyond that splits
+// off the excess (config 2: 1248 = 1216 + 32).
 int tail_systems(const crgpu_ctx *c, int ns) {
-    if (c->precision != CRGPU_MIXED || mixed_factor_kind(c->P) != 1 || c->nsm <= 0) return 0;
-    const int round = 2 * c->nsm, tail = ns % round;
-    return (ns > round && tail > 0 && tail <= round / 2) ? tail : 0;
+    if (c->precision != CRGPU_MIXED || c->nsm <= 0) return 0;
+    const int kind = mixed_factor_kind(c->P);
+    if (kind == 1) {
+        const int round = 2 * c->nsm, tail = ns % round;
+        return (ns > round && tail > 0 && tail <= round / 2) ? tail : 0;
+    }
+    if (kind == 4) {
+        const int wave = 8 * c->nsm, tail = ns - wave;
+        return (tail > 0 && tail <= c->nsm) ? tail : 0;
+    }
+    return 0;
 }
 
 // the forward block on device-resident sigma
@@ -403,7 +417,10 @@ int run_forward(crgpu_ctx *c, const double2 *d_sigma, int volt_mode, const doubl
             if (e) return e;
             cudaEventRecord(f1, c->st);
             CUCHECK(c, cudaStreamWaitEvent(c->st_hi, f1, 0));
-            e = run_factor_view(c, Bt, fuse, c->st_hi, true);  // SMs of its own
+            // SMs of their own; the few tail systems of the warp-per-system factor
+            // take the tensor cores, which factor one lone system faster
+            const int tkind = (mixed_factor_kind(P) == 4 && P.mb + 4 <= 128) ? 1 : 0;
+            e = run_factor_view(c, Bt, fuse, c->st_hi, true, tkind);
             if (!e) e = solve_view(c, Bt, fuse != 0, c->st_hi, 1);
             if (!e) e = solve_view(c, Bf, fuse != 0, c->st, 0);
             if (e) return e;
