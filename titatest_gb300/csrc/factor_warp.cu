@@ -1,6 +1,8 @@
 // Complex64 band factorisation (src/chol.f90:7-88, with the forward
 // substitution of src/vre.f90:45-56 fused in) of narrow bands, mb <= 63, with
-// one warp per system and the whole active window in that warp's registers.
+// one warp per system and the whole active window in that warp's registers:
+// k_factor_warp one column a step (below), k_factor_warp2 two columns a step
+// for mb <= 62 (further down).
 //
 // Window: rows j .. j+63, row r in slot r mod 64, slots in 8 blocks of 8.
 // The window is complex symmetric; its strictly lower slot pairs are held
