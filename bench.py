@@ -124,6 +124,16 @@ def fp64_dgemm_tflops(stream) -> float:
     return 2.0 * 4096 ** 3 / (best * 1e-3) / 1e12
 
 
+def hbm_peak_gbs():
+    """The copy bandwidth of MEASURED_PEAKS.json (measured on this
+    pool), else the fallback 6.8 TB/s."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (of measured)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback 6.8 TB/s (of fallback)"
+
+
 def fp32_sgemm_tflops(stream) -> float:
     """The FP32 FMA-pipe rate of this GPU as cuBLAS SGEMM reaches it (TF32
     off, 8192^3, best of 3, CUDA events): the denominator of the SIMT
@@ -445,6 +455,16 @@ def run_gpu(args):
     fp64_peak = fp64_dgemm_tflops(stream)
     fac_avg_ms = statistics.mean(fac_ms)
     achieved = flops_mixed / (fac_avg_ms * 1e-3) / 1e12
+    # the same launch on the HBM lens: its algorithmic bytes (the complex64
+    # factor written once, the scaled complex128 pattern rows and the
+    # right-hand side read once) over its time
+    alg_bytes = nsys_main * (n * (mb_mixed + 1) * 8.0 + n * 8.0 + n * 16.0)
+    hbm_peak, hbm_src = hbm_peak_gbs()
+    hbm_ach = alg_bytes / (fac_avg_ms * 1e-3) / 1e9
+    hbm_view = {"bound": "hbm", "achieved": hbm_ach, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_ach / hbm_peak,
+                "peak_source": hbm_src,
+                "algorithmic": "per system: n (mb+1) 8 B of complex64 factor and n 8 B of forward substitution "
+                               "written, n 16 B of right-hand side read (the pattern rows' reads excluded)"}
     if bound == "tensor":
         peak, peak_source = tensor_peak_tflops()
     else:
@@ -487,6 +507,7 @@ def run_gpu(args):
                      "algorithmic": "4*n*mb^2 flops per band system (complex L L^T) at the factored band, "
                                     "the systems of the timed factor launch",
                      "systems": nsys_main,
+                     "hbm_view": hbm_view,
                      "note": FACTOR_NOTES.get(kname, "")},
     }
     kwn, kwnwi = mixed.kwn, mixed.kwnwi
