@@ -92,24 +92,6 @@ __device__ __forceinline__ void raw_issue(const DevProblem &P, const double2 *as
     cp_commit();
 }
 
-// the pattern rows r and r+1 into their raw slots, one commit group
-template <class SM>
-__device__ __forceinline__ void raw_issue2(const DevProblem &P, const double2 *as, const double2 *bv, int r,
-                                           int fuse, SM &S, int lane) {
-#pragma unroll
-    for (int u = 0; u < 2; u++) {
-        const int rr = r + u, q = rr & (kRaw - 1);
-        if (rr < P.n) {
-            if (lane < P.rw) {
-                cp_async16(&S.raw_val[q][lane], as + (size_t)rr * P.rw + lane);
-                cp_async4(&S.raw_col[q][lane], P.col + (size_t)rr * P.rw + lane);
-            }
-            if (lane == 31 && fuse) cp_async16(&S.raw_b[q], bv + rr);
-        }
-    }
-    cp_commit();
-}
-
 // Lane tile and its padded slot bases.  xl/xh: base of the rows of the lower /
 // upper part (c < a / c > a) of R, yl/yh: of its columns.
 struct WarpTile {
@@ -428,10 +410,27 @@ struct WarpSmem2 {
     __align__(16) float2 pcs[2][2][kPad];   // scaled: pcol / d
     __align__(16) float2 dense[kDense][kPad];
     float2 dense_b[kDense];
-    __align__(16) double2 raw_val[kRaw][kRawCap];
-    int raw_col[kRaw][kRawCap];
-    __align__(16) double2 raw_b[kRaw];
 };
+
+// Two pattern rows one step ahead in registers (plain loads, so nothing waits
+// on them until the next step scatters them): lane e < rw holds entry e of
+// each row, lane 31 also its right-hand side.
+struct RowsAhead {
+    int col[2];
+    double2 val[2], b[2];
+};
+
+__device__ __forceinline__ void rows_load(RowsAhead &A, const DevProblem &P, const double2 *as, const double2 *bv,
+                                          int r, int fuse, int lane) {
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        const int rr = r + u;
+        const bool live = rr < P.n && lane < P.rw;
+        A.col[u] = live ? P.col[(size_t)rr * P.rw + lane] : -1;
+        A.val[u] = live ? as[(size_t)rr * P.rw + lane] : make_double2(0.0, 0.0);
+        A.b[u] = (rr < P.n && fuse && lane == 31) ? bv[rr] : make_double2(0.0, 0.0);
+    }
+}
 
 #define CRGPU_H_SWITCH(h, CALL) \
     switch (h) {                  \
@@ -443,9 +442,9 @@ struct WarpSmem2 {
 
 template <int FUSE>
 __device__ __forceinline__ void warp_step2(float2 (&R)[8][8], float2 &d0, float2 &d1, float2 &b0, float2 &b1,
-                                           const WarpTile &t, const WarpPred &w, WarpSmem2 &S, const DevProblem &P,
-                                           const double2 *as, const double2 *bv, float2 *L, float2 *yv, int j,
-                                           int p1, int h, int lane, int &bad) {
+                                           const WarpTile &t, const WarpPred &w, WarpSmem2 &S, RowsAhead &A,
+                                           const DevProblem &P, const double2 *as, const double2 *bv, float2 *L,
+                                           float2 *yv, int j, int p1, int h, int lane, int &bad) {
     const int n = P.n, mb = P.mb, Wb = mb + 1;
     const int p2 = p1 + 1, pb = (j >> 1) & 1;
     const bool two = j + 1 < n;  // the second column exists
@@ -462,7 +461,6 @@ __device__ __forceinline__ void warp_step2(float2 (&R)[8][8], float2 &d0, float2
         if (own1) pc1[pad(p1)] = (p1 >> 5) ? d1 : d0;
         if (own2) pc2[pad(p2)] = (p2 >> 5) ? d1 : d0;
     }
-    cp_wait<1>();  // the raw rows scattered below (committed one step before the last) have landed
     __syncwarp();
     // ---- 2. the 2x2 pivot block (L D L^T), the second column after the first's
     //      elimination, the scaled copies, the diagonal, the square roots
@@ -529,17 +527,15 @@ __device__ __forceinline__ void warp_step2(float2 (&R)[8][8], float2 &d0, float2
             }
         }
     }
-    // ---- staging: rows j+66, j+67 from their raw pattern rows into the dense
-    //      slots cleared above, then the raw rows four further ahead
+    // ---- staging: rows j+66, j+67 (loaded one step ago) into the dense slots
+    //      cleared above; then rows j+68, j+69 into registers for the next step
 #pragma unroll
     for (int u = 0; u < 2; u++) {
-        const int r = j + kWW + 2 + u, q = r & (kRaw - 1), qd = r & (kDense - 1);
-        const bool live = r < n && lane < P.rw;
-        const int c = live ? S.raw_col[q][lane] : -1;
-        if (c >= 0) S.dense[qd][pad(c & (kWW - 1))] = to_f(S.raw_val[q][lane]);
-        if (lane == 31) S.dense_b[qd] = (FUSE && r < n) ? to_f(S.raw_b[q]) : cf(0.f, 0.f);
+        const int qd = (j + kWW + 2 + u) & (kDense - 1);
+        if (A.col[u] >= 0) S.dense[qd][pad(A.col[u] & (kWW - 1))] = to_f(A.val[u]);
+        if (lane == 31) S.dense_b[qd] = to_f(A.b[u]);
     }
-    raw_issue2(P, as, bv, j + kWW + 6, FUSE, S, lane);
+    rows_load(A, P, as, bv, j + kWW + 4, FUSE, lane);
     // ---- 4. rows j+64 and j+65 enter slots p1 and p2 (in this order: the pair
     //      (p1, p2) takes its value from row j+65's pattern)
     {
@@ -595,11 +591,11 @@ __global__ __launch_bounds__(32, MINB) void k_factor_warp2(DevProblem P, DevBatc
         CRGPU_ENTER0(4) CRGPU_ENTER0(5) CRGPU_ENTER0(6) CRGPU_ENTER0(7)
 #undef CRGPU_ENTER0
     }
-    // rows 64, 65 (step 0) as dense rows; 66..69 in flight, two per group
+    // rows 64, 65 (step 0) as dense rows; 66, 67 in registers
     load_dense_row(P, as, bv, kWW, fuse, S, kWW & (kDense - 1), lane);
     load_dense_row(P, as, bv, kWW + 1, fuse, S, (kWW + 1) & (kDense - 1), lane);
-    raw_issue2(P, as, bv, kWW + 2, fuse, S, lane);
-    raw_issue2(P, as, bv, kWW + 4, fuse, S, lane);
+    RowsAhead A;
+    rows_load(A, P, as, bv, kWW + 2, fuse, lane);
     const int nstep = (n + 7) / 8;
     for (int J8 = 0; J8 < nstep; J8++) {
         const int P8 = J8 & 7;
@@ -607,7 +603,7 @@ __global__ __launch_bounds__(32, MINB) void k_factor_warp2(DevProblem P, DevBatc
         const int j0 = 8 * J8;
 #pragma unroll 1
         for (int h = 0; h < 4 && j0 + 2 * h < n; h++)
-            warp_step2<FUSE>(R, d0, d1, b0, b1, t, w, S, P, as, bv, L, yv, j0 + 2 * h, 8 * P8 + 2 * h, h, lane, bad);
+            warp_step2<FUSE>(R, d0, d1, b0, b1, t, w, S, A, P, as, bv, L, yv, j0 + 2 * h, 8 * P8 + 2 * h, h, lane, bad);
     }
     cp_wait<0>();
     bad = __reduce_or_sync(0xffffffffu, bad);
