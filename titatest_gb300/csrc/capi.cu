@@ -1398,7 +1398,18 @@ int crgpu_autotune(crgpu_ctx *c, const double *sigma, int32_t flags) {
         P.tune_factor = cd[0];
         P.tune_ctas = cd[1];
         int fe = 0;
-        const float ms = time_on(c, [&] { fe = fe ? fe : run_factor(c, ns, fuse); });
+        // as the forward runs it: a batch that splits (tail_systems) is timed as
+        // its main launch and then its tail launch
+        const int tail = tail_systems(c, ns);
+        const float ms = time_on(c, [&] {
+            if (!tail) {
+                fe = fe ? fe : run_factor(c, ns, fuse);
+                return;
+            }
+            const int tkind = (mixed_factor_kind(P) == 4 && P.mb + 4 <= 128) ? 1 : 0;
+            fe = fe ? fe : run_factor_view(c, sub_view(c, B, 0, ns - tail), fuse, c->st);
+            fe = fe ? fe : run_factor_view(c, sub_view(c, B, ns - tail, tail), fuse, c->st, true, tkind);
+        });
         if (fe) return fe;
         int ce = check_device_errors(c, B.status, ns);
         if (ce) return ce;
