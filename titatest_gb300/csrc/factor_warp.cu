@@ -410,7 +410,28 @@ struct WarpSmem2 {
     __align__(16) float2 pcs[2][2][kPad];   // scaled: pcol / d
     __align__(16) float2 dense[kDense][kPad];
     float2 dense_b[kDense];
+    // the cp.async ring of the 12-warp variant (no registers to spare for rows ahead)
+    __align__(16) double2 raw_val[kRaw][kRawCap];
+    int raw_col[kRaw][kRawCap];
+    __align__(16) double2 raw_b[kRaw];
 };
+
+// the pattern rows r and r+1 into their raw slots, one commit group
+__device__ __forceinline__ void raw_issue2(const DevProblem &P, const double2 *as, const double2 *bv, int r,
+                                           int fuse, WarpSmem2 &S, int lane) {
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        const int rr = r + u, q = rr & (kRaw - 1);
+        if (rr < P.n) {
+            if (lane < P.rw) {
+                cp_async16(&S.raw_val[q][lane], as + (size_t)rr * P.rw + lane);
+                cp_async4(&S.raw_col[q][lane], P.col + (size_t)rr * P.rw + lane);
+            }
+            if (lane == 31 && fuse) cp_async16(&S.raw_b[q], bv + rr);
+        }
+    }
+    cp_commit();
+}
 
 // Two pattern rows one step ahead in registers (plain loads, so nothing waits
 // on them until the next step scatters them): lane e < rw holds entry e of
@@ -440,7 +461,7 @@ __device__ __forceinline__ void rows_load(RowsAhead &A, const DevProblem &P, con
         default: CALL(6); break;  \
     }
 
-template <int FUSE>
+template <int FUSE, int MINB>
 __device__ __forceinline__ void warp_step2(float2 (&R)[8][8], float2 &d0, float2 &d1, float2 &b0, float2 &b1,
                                            const WarpTile &t, const WarpPred &w, WarpSmem2 &S, RowsAhead &A,
                                            const DevProblem &P, const double2 *as, const double2 *bv, float2 *L,
@@ -461,6 +482,7 @@ __device__ __forceinline__ void warp_step2(float2 (&R)[8][8], float2 &d0, float2
         if (own1) pc1[pad(p1)] = (p1 >> 5) ? d1 : d0;
         if (own2) pc2[pad(p2)] = (p2 >> 5) ? d1 : d0;
     }
+    if (MINB != 8) cp_wait<1>();  // the raw rows scattered below (committed one step before the last) have landed
     __syncwarp();
     // ---- 2. the 2x2 pivot block (L D L^T), the second column after the first's
     //      elimination, the scaled copies, the diagonal, the square roots
@@ -527,15 +549,29 @@ __device__ __forceinline__ void warp_step2(float2 (&R)[8][8], float2 &d0, float2
             }
         }
     }
-    // ---- staging: rows j+66, j+67 (loaded one step ago) into the dense slots
-    //      cleared above; then rows j+68, j+69 into registers for the next step
+    // ---- staging: rows j+66, j+67 into the dense slots cleared above; 8 warps an
+    //      SM: loaded into registers one step ago, and rows j+68, j+69 are loaded
+    //      now; 12 warps an SM: from the cp.async ring, which then takes the
+    //      rows four further ahead
+    if (MINB == 8) {
 #pragma unroll
-    for (int u = 0; u < 2; u++) {
-        const int qd = (j + kWW + 2 + u) & (kDense - 1);
-        if (A.col[u] >= 0) S.dense[qd][pad(A.col[u] & (kWW - 1))] = to_f(A.val[u]);
-        if (lane == 31) S.dense_b[qd] = to_f(A.b[u]);
+        for (int u = 0; u < 2; u++) {
+            const int qd = (j + kWW + 2 + u) & (kDense - 1);
+            if (A.col[u] >= 0) S.dense[qd][pad(A.col[u] & (kWW - 1))] = to_f(A.val[u]);
+            if (lane == 31) S.dense_b[qd] = to_f(A.b[u]);
+        }
+        rows_load(A, P, as, bv, j + kWW + 4, FUSE, lane);
+    } else {
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int r = j + kWW + 2 + u, q = r & (kRaw - 1), qd = r & (kDense - 1);
+            const bool live = r < n && lane < P.rw;
+            const int c = live ? S.raw_col[q][lane] : -1;
+            if (c >= 0) S.dense[qd][pad(c & (kWW - 1))] = to_f(S.raw_val[q][lane]);
+            if (lane == 31) S.dense_b[qd] = (FUSE && r < n) ? to_f(S.raw_b[q]) : cf(0.f, 0.f);
+        }
+        raw_issue2(P, as, bv, j + kWW + 6, FUSE, S, lane);
     }
-    rows_load(A, P, as, bv, j + kWW + 4, FUSE, lane);
     // ---- 4. rows j+64 and j+65 enter slots p1 and p2 (in this order: the pair
     //      (p1, p2) takes its value from row j+65's pattern)
     {
@@ -595,7 +631,12 @@ __global__ __launch_bounds__(32, MINB) void k_factor_warp2(DevProblem P, DevBatc
     load_dense_row(P, as, bv, kWW, fuse, S, kWW & (kDense - 1), lane);
     load_dense_row(P, as, bv, kWW + 1, fuse, S, (kWW + 1) & (kDense - 1), lane);
     RowsAhead A;
-    rows_load(A, P, as, bv, kWW + 2, fuse, lane);
+    if (MINB == 8) {
+        rows_load(A, P, as, bv, kWW + 2, fuse, lane);
+    } else {
+        raw_issue2(P, as, bv, kWW + 2, fuse, S, lane);
+        raw_issue2(P, as, bv, kWW + 4, fuse, S, lane);
+    }
     const int nstep = (n + 7) / 8;
     for (int J8 = 0; J8 < nstep; J8++) {
         const int P8 = J8 & 7;
@@ -603,7 +644,8 @@ __global__ __launch_bounds__(32, MINB) void k_factor_warp2(DevProblem P, DevBatc
         const int j0 = 8 * J8;
 #pragma unroll 1
         for (int h = 0; h < 4 && j0 + 2 * h < n; h++)
-            warp_step2<FUSE>(R, d0, d1, b0, b1, t, w, S, A, P, as, bv, L, yv, j0 + 2 * h, 8 * P8 + 2 * h, h, lane, bad);
+            warp_step2<FUSE, MINB>(R, d0, d1, b0, b1, t, w, S, A, P, as, bv, L, yv, j0 + 2 * h, 8 * P8 + 2 * h, h,
+                                   lane, bad);
     }
     cp_wait<0>();
     bad = __reduce_or_sync(0xffffffffu, bad);
